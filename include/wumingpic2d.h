@@ -1,0 +1,176 @@
+/*
+ * wumingpic2d.h -- C ABI of the GB300 implementation of the WumingPIC2D time step.
+ *
+ * Two layers:
+ *
+ * 1. Module-procedure mirror.  One entry point per public procedure of the reference's
+ *    common/ modules, with the same arguments in the same order.  Arrays are host pointers in the
+ *    reference's Fortran layout (column-major, first element of each custom-bounded array):
+ *        up, gp  (ndim, np, nys:nye, nsp)     uf, df (6, nxgs-2:nxge+2, nys-2:nye+2)
+ *        uj      (3, nxgs-2:nxge+2, nys-2:nye+2)
+ *        cumcnt  (nxgs:nxge+1, nys:nye, nsp)  np2 (nys:nye, nsp)   [int32]
+ *        mom     (7, nxgs-1:nxge+1, nys-1:nye+1, nsp)
+ *        phi     (nxs-1:nxe+1, nys-1:nye+1)
+ *    Like the Fortran modules, each *_init stores its arguments as module state; the SAVE'd work
+ *    arrays of field__fdtd_i (df, uj, gkl) live on the GPU between calls.  Each call copies its
+ *    array arguments to the GPU, runs the hand-written sm_103a kernels and copies the results
+ *    back; elements the reference routine does not write keep their values.  MPI arguments
+ *    (mnpi, mnpr, ncomw, opsum, nerr, nstat, nup, ndown) are accepted and ignored: one process
+ *    owns the whole periodic domain (nys = nygs, nye = nyge).  A Fortran application binds these
+ *    through ISO_C_BINDING; where the reference calls `stop`, these return a nonzero status.
+ *
+ * 2. Resident simulation (wm_sim_*).  Particles and fields stay on the GPU across steps in a
+ *    compact structure-of-arrays layout sorted by (species, row, cell); host arrays in the
+ *    reference layout are read at load and written at store.  wm_sim_step runs the main-loop
+ *    body of proj/weibel/app.f90:102-107 (particle__solv, field__fdtd_i, bc__particle_x,
+ *    bc__particle_y, sort__bucket) with periodic boundaries.
+ *
+ * Every function returns WM_OK (0) or one of the WM_ERR_* codes; wm_status_string names them.
+ */
+#ifndef WUMINGPIC2D_H
+#define WUMINGPIC2D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    WM_OK = 0,
+    WM_ERR_CG_MAXITER = 1,   /* CG reached ite_max (field.f90:427-430 stops the program there)   */
+    WM_ERR_OVERFLOW = 2,     /* a row needs more than np slots (boundary_periodic.f90:231-234)     */
+    WM_ERR_BAD_ARG = 3,      /* unsupported or inconsistent argument                               */
+    WM_ERR_CELL = 4,         /* a particle outside nxs..nxe, or moved more than one row in a step  */
+    WM_ERR_CUDA = 5,         /* a CUDA runtime call failed                                         */
+    WM_ERR_NOT_INIT = 6,     /* *_init was not called first (the reference stops there)           */
+    WM_ERR_UNSUPPORTED = 7   /* option outside the periodic single-GPU path                        */
+};
+
+enum { WM_PREC_FP64 = 0, WM_PREC_MIXED = 1 };
+
+/* ---------------------------------------------------------------- particle.f90 */
+/* particle__init, common/particle.f90:18-45 */
+int wm_particle_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, double delx,
+                     double delt, double c, const double *q, const double *r);
+/* particle__solv(gp, up, uf, cumcnt, nxs, nxe), common/particle.f90:48-177 */
+int wm_particle_solv(double *gp, const double *up, const double *uf, const int *cumcnt, int nxs, int nxe);
+
+/* ------------------------------------------------------------------- field.f90 */
+/* field__init, common/field.f90:22-63 */
+int wm_field_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, int mnpr, int ncomw,
+                  int opsum, int nerr, double delx, double delt, double c, const double *q, const double *r, double gfac);
+/* field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, bc_dfield, bc_curre, bc_phi), common/field.f90:66-186.
+ * The three procedure arguments are the boundary routines of the module whose *_init ran last
+ * (boundary_periodic here); the device applies that boundary kind. */
+int wm_field_fdtd_i(double *uf, const double *up, const double *gp, const int *cumcnt, int nxs, int nxe);
+
+/* -------------------------------------------------------------------- sort.f90 */
+/* sort__init, common/sort.f90:16-33 */
+int wm_sort_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye);
+/* sort__bucket(gp, up, cumcnt, np2, nxs, nxe), common/sort.f90:36-82: gp is the output */
+int wm_sort_bucket(double *gp, const double *up, int *cumcnt, const int *np2, int nxs, int nxe);
+
+/* ---------------------------------------------------------------- mom_calc.f90 */
+/* mom_calc__init, common/mom_calc.f90:18-45 */
+int wm_mom_calc_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, double delx,
+                     double delt, double c, const double *q, const double *r);
+/* mom_calc__accl(gp, up, uf, cumcnt, nxs, nxe), common/mom_calc.f90:48-164 */
+int wm_mom_calc_accl(double *gp, const double *up, const double *uf, const int *cumcnt, int nxs, int nxe);
+/* mom_calc__nvt(mom, up, np2), common/mom_calc.f90:167-249 */
+int wm_mom_calc_nvt(double *mom, const double *up, const int *np2);
+
+/* ------------------------------------------------------- boundary_periodic.f90 */
+/* boundary_periodic__init, common/boundary_periodic.f90:26-58 */
+int wm_bc_periodic_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, int nup,
+                        int ndown, int mnpi, int mnpr, int ncomw, int nerr, const int *nstat, int nstat_len, double delx,
+                        double delt, double c);
+/* boundary_periodic__particle_x(up, np2), :61-96 */
+int wm_bc_periodic_particle_x(double *up, const int *np2);
+/* boundary_periodic__particle_y(up, np2), :99-248 */
+int wm_bc_periodic_particle_y(double *up, int *np2);
+/* boundary_periodic__dfield(df, nxs, nxe, nys, nye, nxgs, nxge), :251-354 */
+int wm_bc_periodic_dfield(double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge);
+/* boundary_periodic__curre(uj, nxs, nxe, nys, nye, nxgs, nxge), :357-508 */
+int wm_bc_periodic_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge);
+/* boundary_periodic__phi(phi, nxs, nxe, nys, nye, l), :511-568 */
+int wm_bc_periodic_phi(double *phi, int nxs, int nxe, int nys, int nye, int l);
+/* boundary_periodic__mom(mom), :571-636 */
+int wm_bc_periodic_mom(double *mom);
+
+/* ------------------------------------------------------------- diagnostics */
+/* Energy sums of energy_history, proj/weibel/app.f90:479-545:
+ * out[0..nsp-1] = sum m_s (gamma-1), out[nsp] = sum E^2/8pi, out[nsp+1] = sum B^2/8pi.
+ * Uses the dimensions of the last particle/field init. */
+int wm_energy_sums(const double *up, const double *uf, const int *np2, double *out);
+/* CG iterations per component (Bx, By, Bz) of the last field__fdtd_i call. */
+int wm_field_cg_iters(int *iters3);
+/* The SAVE'd work arrays of field__fdtd_i (field.f90:98): df (6,..) carries the previous step's
+ * delta-B as the next CG initial guess, uj (3,..) is the last deposited current.  No
+ * counterpart in the reference's public interface; used for restart and parity checks. */
+int wm_field_get_work(double *df, double *uj);
+int wm_field_set_work(const double *df);
+/* Release every GPU buffer held by the module-procedure layer. */
+int wm_finalize(void);
+
+const char *wm_status_string(int status);
+/* Library build string: architecture and precision paths compiled in. */
+const char *wm_build_info(void);
+
+/* -------------------------------------------------------- resident simulation */
+typedef struct wm_sim wm_sim;
+
+typedef struct wm_sim_config {
+    int nx, ny, nsp;      /* interior cells; species (<= 4) */
+    int np;               /* slots per row in the host reference layout used by load/store */
+    double delx, delt, c, gfac;
+    double q[4], r[4];    /* charge and mass per species */
+    double cg_err;        /* relative CG tolerance (field.f90:339 uses 1e-6) */
+    int cg_itemax;        /* CG iteration limit (field.f90:337 uses 100) */
+    int precision;        /* WM_PREC_FP64 or WM_PREC_MIXED */
+    int64_t capacity;     /* particle slots held on the GPU; 0 = 1.05 x loaded count */
+} wm_sim_config;
+
+int wm_sim_create(const wm_sim_config *cfg, wm_sim **out);
+int wm_sim_destroy(wm_sim *s);
+/* Copy a host state (reference layout) to the GPU and cell-sort it (sort__bucket). */
+int wm_sim_load(wm_sim *s, const double *up, const double *uf, const int *np2);
+/* Copy the GPU state to host arrays in the reference layout: up slots 1..np2(j) of each row
+ * (slots after that and up to the largest np2 are zeroed), uf, np2 and cumcnt. */
+int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2, int *cumcnt);
+/* Advance nsteps steps on the GPU. */
+int wm_sim_step(wm_sim *s, int nsteps);
+/* The step with host buffers: load (up, uf, np2), nsteps steps, store (up, uf, np2, cumcnt).
+ * up must be cell-sorted with a matching cumcnt on entry (the state the step loop keeps). */
+int wm_sim_step_host(wm_sim *s, double *up, double *uf, int *np2, int *cumcnt, int nsteps);
+int wm_sim_energy(wm_sim *s, double *out);
+/* mom_calc__accl + mom_calc__nvt + boundary_periodic__mom on the resident state, into a host
+ * array mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp). */
+int wm_sim_moments(wm_sim *s, double *mom);
+/* CG iterations per component of the last step. */
+int wm_sim_cg_iters(wm_sim *s, int *iters3);
+/* Per-kernel GPU time of the last wm_sim_step call, from CUDA events on the simulation's
+ * stream: names[i] (static strings) and milliseconds ms[i]; *n in = capacity, out = count. */
+int wm_sim_kernel_times(wm_sim *s, const char **names, double *ms, int *n);
+/* Enable (1) or disable (0) the per-kernel event timing of wm_sim_step. */
+int wm_sim_set_timing(wm_sim *s, int on);
+/* Number of kernel launches of the last wm_sim_step call. */
+int wm_sim_launches(wm_sim *s, int64_t *count);
+/* Particle count and device bytes held. */
+int wm_sim_info(wm_sim *s, int64_t *nparticles, int64_t *device_bytes);
+/* Block until every launched step has finished. */
+int wm_sim_sync(wm_sim *s);
+
+/* The SAVE'd field work arrays of the resident simulation (see wm_field_get_work). */
+int wm_sim_get_work(wm_sim *s, double *df, double *uj);
+int wm_sim_set_work(wm_sim *s, const double *df);
+
+/* Page-lock (pin) a host buffer so that copies from and to it run at full link speed. */
+int wm_host_register(void *ptr, size_t bytes);
+int wm_host_unregister(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WUMINGPIC2D_H */

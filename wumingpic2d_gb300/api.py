@@ -1,0 +1,182 @@
+"""The reference's common/ module procedures, on the GPU.
+
+Same names and argument lists as the Fortran module procedures used through
+common/wuming2d.f90; arrays are numpy arrays in the reference layout (see
+layout.py).  Each call runs the sm_103a kernels of libwmpic2d.so; errors where
+the reference calls `stop` raise WmError.
+
+    particle__init / particle__solv         common/particle.f90:18-177
+    field__init / field__fdtd_i             common/field.f90:22-186
+    sort__init / sort__bucket               common/sort.f90:16-82
+    mom_calc__init / __accl / __nvt         common/mom_calc.f90:18-249
+    boundary_periodic__init / __particle_x / __particle_y / __dfield /
+        __curre / __phi / __mom             common/boundary_periodic.f90:26-636
+
+field__fdtd_i takes the three boundary procedures as arguments in the
+reference; here they are the boundary_periodic ones, and the module whose
+*__init ran last supplies them (pass them for symmetry, they are checked).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._native import check, lib
+
+_MPI_DUMMY = 0
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data
+
+
+def _f64(a, name):
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not (a.flags.f_contiguous or a.ndim == 1):
+        raise TypeError(f"{name} must be a Fortran-ordered float64 array")
+    return a
+
+
+def _i32(a, name):
+    if not isinstance(a, np.ndarray) or a.dtype != np.int32 or not (a.flags.f_contiguous or a.ndim == 1):
+        raise TypeError(f"{name} must be a Fortran-ordered int32 array")
+    return a
+
+
+def _qr(a, nsp):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if a.size != nsp:
+        raise ValueError("q and r need one value per species")
+    return a
+
+
+# ---------------------------------------------------------------- particle.f90
+def particle__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, delx, delt, c, q, r):
+    q = _qr(q, nsp)
+    r = _qr(r, nsp)
+    check(lib().wm_particle_init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, delx, delt, c, _p(q), _p(r)),
+          "particle__init")
+
+
+def particle__solv(gp, up, uf, cumcnt, nxs, nxe):
+    check(lib().wm_particle_solv(_p(_f64(gp, "gp")), _p(_f64(up, "up")), _p(_f64(uf, "uf")), _p(_i32(cumcnt, "cumcnt")),
+                                 nxs, nxe), "particle__solv")
+
+
+# ------------------------------------------------------------------- field.f90
+def field__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, mnpr, ncomw, opsum, nerr, delx, delt, c, q, r, gfac):
+    q = _qr(q, nsp)
+    r = _qr(r, nsp)
+    check(lib().wm_field_init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, mnpr, ncomw, opsum, nerr, delx, delt, c,
+                              _p(q), _p(r), gfac), "field__init")
+
+
+def field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, set_boundary_dfield=None, set_boundary_curre=None,
+                  set_boundary_phi=None):
+    for f, want in ((set_boundary_dfield, boundary_periodic__dfield), (set_boundary_curre, boundary_periodic__curre),
+                    (set_boundary_phi, boundary_periodic__phi)):
+        if f is not None and f is not want:
+            raise NotImplementedError("only the boundary_periodic procedures run on the GPU")
+    check(lib().wm_field_fdtd_i(_p(_f64(uf, "uf")), _p(_f64(up, "up")), _p(_f64(gp, "gp")), _p(_i32(cumcnt, "cumcnt")),
+                                nxs, nxe), "field__fdtd_i")
+
+
+def field__cg_iters() -> np.ndarray:
+    out = np.zeros(3, dtype=np.int32)
+    check(lib().wm_field_cg_iters(_p(out)), "field cg iters")
+    return out
+
+
+def field__get_work(df=None, uj=None):
+    check(lib().wm_field_get_work(_p(df) if df is not None else None, _p(uj) if uj is not None else None),
+          "field work")
+
+
+def field__set_work(df):
+    check(lib().wm_field_set_work(_p(_f64(df, "df"))), "field work")
+
+
+# -------------------------------------------------------------------- sort.f90
+def sort__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye):
+    check(lib().wm_sort_init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye), "sort__init")
+
+
+def sort__bucket(gp, up, cumcnt, np2, nxs, nxe):
+    check(lib().wm_sort_bucket(_p(_f64(gp, "gp")), _p(_f64(up, "up")), _p(_i32(cumcnt, "cumcnt")), _p(_i32(np2, "np2")),
+                               nxs, nxe), "sort__bucket")
+
+
+# ---------------------------------------------------------------- mom_calc.f90
+def mom_calc__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, delx, delt, c, q, r):
+    q = _qr(q, nsp)
+    r = _qr(r, nsp)
+    check(lib().wm_mom_calc_init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, delx, delt, c, _p(q), _p(r)),
+          "mom_calc__init")
+
+
+def mom_calc__accl(gp, up, uf, cumcnt, nxs, nxe):
+    check(lib().wm_mom_calc_accl(_p(_f64(gp, "gp")), _p(_f64(up, "up")), _p(_f64(uf, "uf")), _p(_i32(cumcnt, "cumcnt")),
+                                 nxs, nxe), "mom_calc__accl")
+
+
+def mom_calc__nvt(mom, up, np2):
+    check(lib().wm_mom_calc_nvt(_p(_f64(mom, "mom")), _p(_f64(up, "up")), _p(_i32(np2, "np2"))), "mom_calc__nvt")
+
+
+# ------------------------------------------------------- boundary_periodic.f90
+def boundary_periodic__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, nup, ndown, mnpi, mnpr, ncomw, nerr,
+                            nstat, delx, delt, c):
+    st = np.ascontiguousarray(np.asarray(nstat if nstat is not None else [0], dtype=np.int32))
+    check(lib().wm_bc_periodic_init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, nup, ndown, mnpi, mnpr, ncomw, nerr,
+                                    _p(st), st.size, delx, delt, c), "boundary_periodic__init")
+
+
+def boundary_periodic__particle_x(up, np2):
+    check(lib().wm_bc_periodic_particle_x(_p(_f64(up, "up")), _p(_i32(np2, "np2"))), "boundary_periodic__particle_x")
+
+
+def boundary_periodic__particle_y(up, np2):
+    check(lib().wm_bc_periodic_particle_y(_p(_f64(up, "up")), _p(_i32(np2, "np2"))), "boundary_periodic__particle_y")
+
+
+def boundary_periodic__dfield(df, nxs, nxe, nys, nye, nxgs, nxge):
+    check(lib().wm_bc_periodic_dfield(_p(_f64(df, "df")), nxs, nxe, nys, nye, nxgs, nxge), "boundary_periodic__dfield")
+
+
+def boundary_periodic__curre(uj, nxs, nxe, nys, nye, nxgs, nxge):
+    check(lib().wm_bc_periodic_curre(_p(_f64(uj, "uj")), nxs, nxe, nys, nye, nxgs, nxge), "boundary_periodic__curre")
+
+
+def boundary_periodic__phi(phi, nxs, nxe, nys, nye, l):
+    check(lib().wm_bc_periodic_phi(_p(_f64(phi, "phi")), nxs, nxe, nys, nye, l), "boundary_periodic__phi")
+
+
+def boundary_periodic__mom(mom):
+    check(lib().wm_bc_periodic_mom(_p(_f64(mom, "mom"))), "boundary_periodic__mom")
+
+
+# ------------------------------------------------------------- diagnostics
+def energy_sums(up, uf, np2, nsp) -> np.ndarray:
+    """energy_history's sums (proj/weibel/app.f90:507-534): [KE_1..KE_nsp, E^2/8pi, B^2/8pi]."""
+    out = np.zeros(nsp + 2)
+    check(lib().wm_energy_sums(_p(_f64(up, "up")), _p(_f64(uf, "uf")), _p(_i32(np2, "np2")), _p(out)), "energy_sums")
+    return out
+
+
+def finalize():
+    check(lib().wm_finalize(), "finalize")
+
+
+def build_info() -> str:
+    return lib().wm_build_info().decode()
+
+
+def init_all(dims, delt, q, r, c=1.0, delx=1.0, gfac=0.501):
+    """Call every module's *__init the way proj/weibel/app.f90:331-347 does (single rank)."""
+    d = dims
+    args = (d.ndim, d.np, d.nsp, d.nxgs, d.nxge, d.nygs, d.nyge, d.nys, d.nye)
+    boundary_periodic__init(*args, 0, 0, _MPI_DUMMY, _MPI_DUMMY, _MPI_DUMMY, 0, None, delx, delt, c)
+    particle__init(*args, delx, delt, c, q, r)
+    field__init(*args, _MPI_DUMMY, _MPI_DUMMY, _MPI_DUMMY, 0, delx, delt, c, q, r, gfac)
+    sort__init(*args)
+    mom_calc__init(*args, delx, delt, c, q, r)

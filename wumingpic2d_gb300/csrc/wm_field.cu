@@ -1,0 +1,583 @@
+// wm_field.cu -- implicit field update of common/field.f90:66-186 on sm_103a, FP64.
+//
+// The three delta-B components are solved together: every CG kernel walks the grid once and
+// handles each component that is still iterating, so one launch serves three solves.  Each
+// component follows the reference's sequence exactly (field.f90:347-459): lagged stop test on
+// the residual norm before the update, first test against ||b||^2, ite_max limit.  The global
+// sums are deterministic: each CTA reduces its cells in a fixed order, writes one partial, and
+// the last CTA to finish (an atomic ticket, no spin-wait) adds the partials in index order and
+// updates the per-component scalars (alpha, beta, counters) in device memory, so no host round
+// trip is needed between kernels.  Periodic halos of the CG vectors are index wraps
+// (boundary_periodic__phi, :511-568); the field ghost layers are filled by the same copy
+// pattern as boundary_periodic__dfield (:251-354) and __curre (:357-508).
+#include <algorithm>
+
+#include "wm_launch.cuh"
+
+struct CgScal {
+    double sum_g, eps, sumr, sum2, sum1, av, bv, pad;
+    int ite, active, status, pad2;
+};
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int CG_THREADS = 256;
+
+// ------------------------------------------------------------ ghost patterns
+template <class FV>
+__global__ void k_curre_bc_y(WmGeom g, FV uj)
+{
+    const int nxr = g.nx + 4;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nxr * 3) return;
+    const int ix = t % nxr, k = t / nxr;
+    // rows relative to nys-2: nys-2 -> 0, nys-1 -> 1, nys -> 2, nys+1 -> 3, nye-1 -> ny, nye -> ny+1, nye+1 -> ny+2, nye+2 -> ny+3
+    const int rs2 = 0, rs1 = 1, rs = 2, rs_1 = 3, re1m = g.ny, re = g.ny + 1, re1 = g.ny + 2, re2 = g.ny + 3;
+    const double a = uj(k, ix, rs2), b = uj(k, ix, rs1);
+    uj(k, ix, re1m) = uj(k, ix, re1m) + a;
+    uj(k, ix, re) = uj(k, ix, re) + b;
+    const double c = uj(k, ix, re1), d = uj(k, ix, re2);
+    uj(k, ix, rs) = uj(k, ix, rs) + c;
+    uj(k, ix, rs_1) = uj(k, ix, rs_1) + d;
+    uj(k, ix, re1) = uj(k, ix, rs);
+    uj(k, ix, re2) = uj(k, ix, rs_1);
+    uj(k, ix, rs2) = uj(k, ix, re1m);
+    uj(k, ix, rs1) = uj(k, ix, re);
+}
+
+template <class FV>
+__global__ void k_curre_bc_x(WmGeom g, FV uj)
+{
+    const int nyr = g.ny + 4;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nyr * 3) return;
+    const int iy = t % nyr, k = t / nyr;
+    const int cs2 = 0, cs1 = 1, cs = 2, cs_1 = 3, ce1m = g.nx, ce = g.nx + 1, ce1 = g.nx + 2, ce2 = g.nx + 3;
+    uj(k, ce1m, iy) = uj(k, ce1m, iy) + uj(k, cs2, iy);
+    uj(k, ce, iy) = uj(k, ce, iy) + uj(k, cs1, iy);
+    uj(k, cs, iy) = uj(k, cs, iy) + uj(k, ce1, iy);
+    uj(k, cs_1, iy) = uj(k, cs_1, iy) + uj(k, ce2, iy);
+    uj(k, cs2, iy) = uj(k, ce1m, iy);
+    uj(k, cs1, iy) = uj(k, ce, iy);
+    uj(k, ce1, iy) = uj(k, cs, iy);
+    uj(k, ce2, iy) = uj(k, cs_1, iy);
+}
+
+template <class FV>
+__global__ void k_dfield_bc_y(WmGeom g, FV df)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= g.nx * 6) return;
+    const int ix = 2 + t % g.nx, k = t / g.nx;  // interior columns only (:263-345)
+    df(k, ix, g.ny + 2) = df(k, ix, 2);
+    df(k, ix, g.ny + 3) = df(k, ix, 3);
+    df(k, ix, 0) = df(k, ix, g.ny);
+    df(k, ix, 1) = df(k, ix, g.ny + 1);
+}
+
+template <class FV>
+__global__ void k_dfield_bc_x(WmGeom g, FV df)
+{
+    const int nyr = g.ny + 4;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nyr * 6) return;
+    const int iy = t % nyr, k = t / nyr;
+    df(k, 0, iy) = df(k, g.nx, iy);
+    df(k, 1, iy) = df(k, g.nx + 1, iy);
+    df(k, g.nx + 2, iy) = df(k, 2, iy);
+    df(k, g.nx + 3, iy) = df(k, 3, iy);
+}
+
+// phi(nxs-1:nxe+1, nys-1:nye+1), x fastest
+__global__ void k_phi_bc_y(int nx, int ny, double *phi)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nx) return;
+    const int pw = nx + 2, ix = 1 + t;
+    phi[ix + (long long)pw * (ny + 1)] = phi[ix + (long long)pw * 1];
+    phi[ix + 0] = phi[ix + (long long)pw * ny];
+}
+__global__ void k_phi_bc_x(int nx, int ny, double *phi)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ny + 2) return;
+    const int pw = nx + 2;
+    phi[0 + (long long)pw * t] = phi[nx + (long long)pw * t];
+    phi[nx + 1 + (long long)pw * t] = phi[1 + (long long)pw * t];
+}
+
+// mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp), reference layout
+__global__ void k_mom_bc_x(WmGeom g, double *mom)
+{
+    const int mx = g.nx + 2, my = g.ny + 2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= my * g.nsp * 7) return;
+    const int k = t % 7, jy = (t / 7) % my, isp = t / (7 * my);
+    double *rowp = mom + 7 * (long long)mx * (jy + (long long)my * isp);
+    rowp[k + 7 * 1] = rowp[k + 7 * 1] + rowp[k + 7 * (mx - 1)];
+    rowp[k + 7 * (mx - 2)] = rowp[k + 7 * (mx - 2)] + rowp[k + 7 * 0];
+}
+__global__ void k_mom_bc_y(WmGeom g, double *mom)
+{
+    const int mx = g.nx + 2, my = g.ny + 2;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= mx * g.nsp * 7) return;
+    const int k = t % 7, ix = (t / 7) % mx, isp = t / (7 * mx);
+    double *col = mom + k + 7 * (ix + (long long)mx * (long long)my * isp);
+    const long long rs = (long long)7 * mx;
+    col[rs * (my - 2)] = col[rs * (my - 2)] + col[rs * 0];
+    col[rs * 1] = col[rs * 1] + col[rs * (my - 1)];
+}
+
+// ------------------------------------------------------------ transposes
+// ref (AoS, component fastest) <-> planes (SoA)
+template <int NC>
+__global__ void k_aos_to_soa(long long npts, const double *__restrict__ a, double *__restrict__ s)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < npts * NC; e += (long long)gridDim.x * blockDim.x) {
+        const long long pt = e / NC;
+        const int k = (int)(e - pt * NC);
+        s[(long long)k * npts + pt] = a[e];
+    }
+}
+template <int NC>
+__global__ void k_soa_to_aos(long long npts, const double *__restrict__ s, double *__restrict__ a)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < npts * NC; e += (long long)gridDim.x * blockDim.x) {
+        const long long pt = e / NC;
+        const int k = (int)(e - pt * NC);
+        a[e] = s[(long long)k * npts + pt];
+    }
+}
+
+// ------------------------------------------------------------- reductions
+__device__ __forceinline__ void block_sum3(double &a, double &b, double &c)
+{
+    __shared__ double sh[3][CG_THREADS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(FULL, a, o);
+        b += __shfl_down_sync(FULL, b, o);
+        c += __shfl_down_sync(FULL, c, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) {
+        sh[0][w] = a;
+        sh[1][w] = b;
+        sh[2][w] = c;
+    }
+    __syncthreads();
+    if (w == 0) {
+        a = (l < CG_THREADS / 32) ? sh[0][l] : 0.0;
+        b = (l < CG_THREADS / 32) ? sh[1][l] : 0.0;
+        c = (l < CG_THREADS / 32) ? sh[2][l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_down_sync(FULL, a, o);
+            b += __shfl_down_sync(FULL, b, o);
+            c += __shfl_down_sync(FULL, c, o);
+        }
+    }
+}
+
+// Writes this CTA's three partials; returns true in thread 0 of the last CTA to finish, with
+// tot[] = the partials summed in index order.
+__device__ bool last_block_reduce3(double a, double b, double c, double *partial, unsigned *ticket, double tot[3])
+{
+    __shared__ bool is_last;
+    block_sum3(a, b, c);
+    if (threadIdx.x == 0) {
+        partial[0 * gridDim.x + blockIdx.x] = a;
+        partial[1 * gridDim.x + blockIdx.x] = b;
+        partial[2 * gridDim.x + blockIdx.x] = c;
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        is_last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!is_last) return false;
+    __threadfence();
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+        s0 += __ldcg(&partial[0 * gridDim.x + i]);
+        s1 += __ldcg(&partial[1 * gridDim.x + i]);
+        s2 += __ldcg(&partial[2 * gridDim.x + i]);
+    }
+    block_sum3(s0, s1, s2);
+    if (threadIdx.x == 0) {
+        tot[0] = s0;
+        tot[1] = s1;
+        tot[2] = s2;
+        *ticket = 0u;
+    }
+    return threadIdx.x == 0;
+}
+
+struct FieldK {
+    double f1, f2, f3, f4, f5, gfac, pi4dt, err;
+    int itemax;
+};
+
+__device__ __forceinline__ int wrapm(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
+
+// gkl (field.f90:125-146), b = f5*gkl and ||b||^2 (:351-364).
+template <class FV6, class FV3>
+__global__ void __launch_bounds__(CG_THREADS) k_cg_rhs(WmGeom g, FieldK fk, FV6 uf, FV3 uj, double *__restrict__ b,
+                                                       double *partial, unsigned *ticket, CgScal *scal)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+        const int x = ci + 2, y = cj + 2;
+        const double g1 = +fk.f2 * (+uf(0, x, y - 1) + uf(0, x - 1, y) - 4. * uf(0, x, y) + uf(0, x + 1, y) + uf(0, x, y + 1)
+                                    + fk.f3 * (-uj(2, x, y - 1) + uj(2, x, y)))
+                          - fk.f1 * (-uf(5, x, y - 1) + uf(5, x, y));
+        const double g2 = +fk.f2 * (+uf(1, x, y - 1) + uf(1, x - 1, y) - 4. * uf(1, x, y) + uf(1, x + 1, y) + uf(1, x, y + 1)
+                                    - fk.f3 * (-uj(2, x - 1, y) + uj(2, x, y)))
+                          + fk.f1 * (-uf(5, x - 1, y) + uf(5, x, y));
+        const double g3 = +fk.f2 * (+uf(2, x, y - 1) + uf(2, x - 1, y) - 4. * uf(2, x, y) + uf(2, x + 1, y) + uf(2, x, y + 1)
+                                    + fk.f3 * (-uj(1, x - 1, y) + uj(1, x, y) + uj(0, x, y - 1) - uj(0, x, y)))
+                          - fk.f1 * (-uf(4, x - 1, y) + uf(4, x, y) + uf(3, x, y - 1) - uf(3, x, y));
+        const double b1 = fk.f5 * g1, b2 = fk.f5 * g2, b3 = fk.f5 * g3;
+        b[0 * ncell + e] = b1;
+        b[1 * ncell + e] = b2;
+        b[2 * ncell + e] = b3;
+        a0 += b1 * b1;
+        a1 += b2 * b2;
+        a2 += b3 * b3;
+    }
+    double tot[3];
+    if (last_block_reduce3(a0, a1, a2, partial, ticket, tot)) {
+        for (int l = 0; l < 3; ++l) {
+            scal[l].sum_g = tot[l];
+            scal[l].eps = sqrt(tot[l]) * fk.err;
+        }
+    }
+}
+
+// r = b + (phi neighbours) - f4 phi, p = r, ||r||^2 (:366-385); phi = df(l) interior.
+template <class FV6>
+__global__ void __launch_bounds__(CG_THREADS) k_cg_resid(WmGeom g, FieldK fk, FV6 df, const double *__restrict__ b,
+                                                         double *__restrict__ r, double *__restrict__ p, double *partial,
+                                                         unsigned *ticket, CgScal *scal)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+        const int xm = wrapm(ci - 1, g.nx) + 2, xp = wrapm(ci + 1, g.nx) + 2, ym = wrapm(cj - 1, g.ny) + 2,
+                  yp = wrapm(cj + 1, g.ny) + 2, x = ci + 2, y = cj + 2;
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+            const double rv = b[l * ncell + e] + df(l, x, ym) + df(l, xm, y) - fk.f4 * df(l, x, y) + df(l, xp, y) + df(l, x, yp);
+            r[l * ncell + e] = rv;
+            p[l * ncell + e] = rv;
+            acc[l] += rv * rv;
+        }
+    }
+    double tot[3];
+    if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot)) {
+        for (int l = 0; l < 3; ++l) {
+            scal[l].sumr = tot[l];
+            scal[l].ite = 0;
+            scal[l].status = 0;
+            scal[l].active = (sqrt(tot[l]) > scal[l].eps) && (scal[l].sum_g > scal[l].eps);
+        }
+    }
+}
+
+// ap = A p and p.ap (:395-415).
+__global__ void __launch_bounds__(CG_THREADS) k_cg_ap(WmGeom g, FieldK fk, const double *__restrict__ p, double *__restrict__ ap,
+                                                      double *partial, unsigned *ticket, CgScal *scal)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    const bool act[3] = {scal[0].active != 0, scal[1].active != 0, scal[2].active != 0};
+    if (!act[0] && !act[1] && !act[2]) return;  // uniform across the grid: no CTA takes a ticket
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+        const long long em = (long long)cj * g.nx + wrapm(ci - 1, g.nx), ep = (long long)cj * g.nx + wrapm(ci + 1, g.nx);
+        const long long es = (long long)wrapm(cj - 1, g.ny) * g.nx + ci, en = (long long)wrapm(cj + 1, g.ny) * g.nx + ci;
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+            if (!act[l]) continue;
+            const double *pl = p + l * ncell;
+            const double pc = pl[e];
+            const double a = -pl[es] - pl[em] + fk.f4 * pc - pl[ep] - pl[en];
+            ap[l * ncell + e] = a;
+            acc[l] += pc * a;
+        }
+    }
+    double tot[3];
+    if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot)) {
+        for (int l = 0; l < 3; ++l)
+            if (act[l]) {
+                scal[l].sum2 = tot[l];
+                scal[l].av = scal[l].sumr / tot[l];
+                scal[l].ite += 1;
+            }
+    }
+}
+
+// phi += av p, r -= av ap, ||r||^2; then the lagged stop test and beta (:417-443).
+template <class FV6>
+__global__ void __launch_bounds__(CG_THREADS) k_cg_update(WmGeom g, FieldK fk, FV6 df, const double *__restrict__ p,
+                                                          double *__restrict__ r, const double *__restrict__ ap, double *partial,
+                                                          unsigned *ticket, CgScal *scal)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    const bool act[3] = {scal[0].active != 0, scal[1].active != 0, scal[2].active != 0};
+    if (!act[0] && !act[1] && !act[2]) return;
+    const double av[3] = {scal[0].av, scal[1].av, scal[2].av};
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+            if (!act[l]) continue;
+            df(l, ci + 2, cj + 2) = df(l, ci + 2, cj + 2) + av[l] * p[l * ncell + e];
+            const double rv = r[l * ncell + e] - av[l] * ap[l * ncell + e];
+            r[l * ncell + e] = rv;
+            acc[l] += rv * rv;
+        }
+    }
+    double tot[3];
+    if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot)) {
+        for (int l = 0; l < 3; ++l)
+            if (act[l]) {
+                CgScal &s = scal[l];
+                s.sum1 = tot[l];
+                s.sum_g = sqrt(s.sumr);
+                if (s.ite >= fk.itemax) {
+                    s.status = WM_ERR_CG_MAXITER;
+                    s.active = 0;
+                } else {
+                    s.bv = tot[l] / s.sumr;
+                    s.sumr = tot[l];
+                    s.active = (s.sum_g > s.eps);
+                }
+            }
+    }
+}
+
+// p = r + bv p (:444-450) for components that keep iterating.
+__global__ void __launch_bounds__(CG_THREADS) k_cg_pupdate(WmGeom g, const double *__restrict__ r, double *__restrict__ p,
+                                                           const CgScal *scal)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    const bool act[3] = {scal[0].active != 0, scal[1].active != 0, scal[2].active != 0};
+    if (!act[0] && !act[1] && !act[2]) return;
+    const double bv[3] = {scal[0].bv, scal[1].bv, scal[2].bv};
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+            if (act[l]) p[l * ncell + e] = r[l * ncell + e] + bv[l] * p[l * ncell + e];
+    }
+}
+
+// delta-E (field.f90:154-171)
+template <class FV6, class FV3>
+__global__ void k_efield(WmGeom g, FieldK fk, FV6 df, FV6 uf, FV3 uj)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(e % g.nx) + 2, y = (int)(e / g.nx) + 2;
+        df(3, x, y) = +fk.f1 * (+fk.gfac * (-df(2, x, y) + df(2, x, y + 1)) + (-uf(2, x, y) + uf(2, x, y + 1))) - fk.pi4dt * uj(0, x, y);
+        df(4, x, y) = -fk.f1 * (+fk.gfac * (-df(2, x, y) + df(2, x + 1, y)) + (-uf(2, x, y) + uf(2, x + 1, y))) - fk.pi4dt * uj(1, x, y);
+        df(5, x, y) = +fk.f1 * (+fk.gfac * (-df(1, x, y) + df(1, x + 1, y) + df(0, x, y) - df(0, x, y + 1))
+                                + (-uf(1, x, y) + uf(1, x + 1, y) + uf(0, x, y) - uf(0, x, y + 1)))
+                      - fk.pi4dt * uj(2, x, y);
+    }
+}
+
+// uf += df over the ghosted grid (:176-184)
+template <class FV6>
+__global__ void k_field_add(WmGeom g, FV6 uf, FV6 df)
+{
+    const long long n = (long long)g.nxw * g.nyw;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int ix = (int)(e % g.nxw), iy = (int)(e / g.nxw);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) uf(k, ix, iy) = uf(k, ix, iy) + df(k, ix, iy);
+    }
+}
+
+// E^2, B^2 over the interior (proj/weibel/app.f90:521-528): partial[2][blocks]
+template <class FV6>
+__global__ void __launch_bounds__(CG_THREADS) k_energy_fields(WmGeom g, FV6 uf, double *partial)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    double be = 0.0, ee = 0.0, z = 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(e % g.nx) + 2, y = (int)(e / g.nx) + 2;
+        be += uf(0, x, y) * uf(0, x, y) + uf(1, x, y) * uf(1, x, y) + uf(2, x, y) * uf(2, x, y);
+        ee += uf(3, x, y) * uf(3, x, y) + uf(4, x, y) * uf(4, x, y) + uf(5, x, y) * uf(5, x, y);
+    }
+    block_sum3(be, ee, z);
+    if (threadIdx.x == 0) {
+        partial[blockIdx.x] = be;
+        partial[gridDim.x + blockIdx.x] = ee;
+    }
+}
+
+__global__ void k_sum_partials(const double *partial, int nparts, int nsets, double *out)
+{
+    // one thread per set, index order: deterministic
+    const int s = threadIdx.x;
+    if (s >= nsets) return;
+    double acc = 0.0;
+    for (int i = 0; i < nparts; ++i) acc += partial[(long long)s * nparts + i];
+    out[s] = acc;
+}
+
+}  // namespace
+
+// ========================================================================== host
+static unsigned grid_for(long long n, int threads) { return (unsigned)std::max<long long>(1, std::min<long long>((n + threads - 1) / threads, 152LL * 16)); }
+
+template <class FV>
+int wm_launch_curre_bc(const WmGeom &g, FV uj, cudaStream_t st)
+{
+    k_curre_bc_y<FV><<<wm_div_up((g.nx + 4) * 3, 128), 128, 0, st>>>(g, uj);
+    WM_TRY(wm_check_launch("k_curre_bc_y"));
+    k_curre_bc_x<FV><<<wm_div_up((g.ny + 4) * 3, 128), 128, 0, st>>>(g, uj);
+    return wm_check_launch("k_curre_bc_x");
+}
+
+template <class FV>
+int wm_launch_dfield_bc(const WmGeom &g, FV df, cudaStream_t st)
+{
+    k_dfield_bc_y<FV><<<wm_div_up(g.nx * 6, 128), 128, 0, st>>>(g, df);
+    WM_TRY(wm_check_launch("k_dfield_bc_y"));
+    k_dfield_bc_x<FV><<<wm_div_up((g.ny + 4) * 6, 128), 128, 0, st>>>(g, df);
+    return wm_check_launch("k_dfield_bc_x");
+}
+
+int wm_launch_phi_bc(int nx, int ny, double *phi, cudaStream_t st)
+{
+    k_phi_bc_y<<<wm_div_up(nx, 128), 128, 0, st>>>(nx, ny, phi);
+    WM_TRY(wm_check_launch("k_phi_bc_y"));
+    k_phi_bc_x<<<wm_div_up(ny + 2, 128), 128, 0, st>>>(nx, ny, phi);
+    return wm_check_launch("k_phi_bc_x");
+}
+
+int wm_launch_mom_bc(const WmGeom &g, double *mom, cudaStream_t st)
+{
+    k_mom_bc_x<<<wm_div_up((g.ny + 2) * g.nsp * 7, 128), 128, 0, st>>>(g, mom);
+    WM_TRY(wm_check_launch("k_mom_bc_x"));
+    k_mom_bc_y<<<wm_div_up((g.nx + 2) * g.nsp * 7, 128), 128, 0, st>>>(g, mom);
+    return wm_check_launch("k_mom_bc_y");
+}
+
+int wm_launch_aos_to_soa(int nc, long long npts, const double *a, double *s, cudaStream_t st)
+{
+    if (nc == 6) k_aos_to_soa<6><<<grid_for(npts * 6, 256), 256, 0, st>>>(npts, a, s);
+    else if (nc == 3) k_aos_to_soa<3><<<grid_for(npts * 3, 256), 256, 0, st>>>(npts, a, s);
+    else return WM_ERR_BAD_ARG;
+    return wm_check_launch("k_aos_to_soa");
+}
+
+int wm_launch_soa_to_aos(int nc, long long npts, const double *s, double *a, cudaStream_t st)
+{
+    if (nc == 6) k_soa_to_aos<6><<<grid_for(npts * 6, 256), 256, 0, st>>>(npts, s, a);
+    else if (nc == 3) k_soa_to_aos<3><<<grid_for(npts * 3, 256), 256, 0, st>>>(npts, s, a);
+    else return WM_ERR_BAD_ARG;
+    return wm_check_launch("k_soa_to_aos");
+}
+
+// --------------------------------------------------------------- field solve
+constexpr int CG_BLOCKS = 152 * 4;
+int wm_field_cg_blocks() { return CG_BLOCKS; }
+size_t wm_field_scal_bytes() { return sizeof(CgScal) * 3; }
+
+static FieldK make_fk(const WmConst &k)
+{
+    const double pi = 3.14159265358979311599796346854418516;
+    FieldK fk;
+    fk.f1 = k.c * k.delt / k.delx;
+    fk.f2 = k.gfac * fk.f1 * fk.f1;
+    fk.f3 = 4.0 * pi * k.delx / k.c;
+    const double t = k.delx / (k.c * k.delt * k.gfac);
+    fk.f4 = 4.0 + t * t;
+    fk.f5 = t * t;
+    fk.gfac = k.gfac;
+    fk.pi4dt = 4. * pi * k.delt;
+    fk.err = k.cg_err;
+    fk.itemax = k.cg_itemax;
+    return fk;
+}
+
+
+// field__fdtd_i after the deposit: curre BC, RHS, CG, dfield BC, delta-E, dfield BC, uf += df.
+// iters[3] and the status are read back at the end.  cg_batch = CG iterations enqueued between
+// host checks of the "still iterating" flags.
+int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<3, false> uj, FView<6, false> df, WmFieldWork &w,
+                   int *iters, int cg_batch, cudaStream_t st, wm_mark_fn mark, void *mctx, long long *launches)
+{
+    const FieldK fk = make_fk(k);
+    long long nl = 0;
+    auto M = [&](const char *n) {
+        if (mark) mark(mctx, n);
+    };
+    WM_TRY(wm_launch_curre_bc(g, uj, st));
+    nl += 2;
+    M("curre_bc");
+    k_cg_rhs<FView<6, false>, FView<3, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, uf, uj, w.b, w.partial, w.ticket, w.scal);
+    WM_TRY(wm_check_launch("k_cg_rhs"));
+    k_cg_resid<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.b, w.r, w.p, w.partial, w.ticket, w.scal);
+    WM_TRY(wm_check_launch("k_cg_resid"));
+    nl += 2;
+    M("cg_setup");
+    int done_iters = 0;
+    for (;;) {
+        WM_CUDA(cudaMemcpyAsync(w.scal_host, w.scal, sizeof(CgScal) * 3, cudaMemcpyDeviceToHost, st));
+        WM_CUDA(cudaStreamSynchronize(st));
+        const bool any = w.scal_host[0].active || w.scal_host[1].active || w.scal_host[2].active;
+        if (!any || done_iters >= fk.itemax + 1) break;
+        for (int b = 0; b < cg_batch; ++b) {
+            k_cg_ap<<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, w.p, w.ap, w.partial, w.ticket, w.scal);
+            k_cg_update<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.p, w.r, w.ap, w.partial, w.ticket, w.scal);
+            k_cg_pupdate<<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, w.r, w.p, w.scal);
+            nl += 3;
+        }
+        WM_TRY(wm_check_launch("cg iteration"));
+        done_iters += cg_batch;
+    }
+    M("cg_iterate");
+    int status = WM_OK;
+    for (int l = 0; l < 3; ++l) {
+        if (iters) iters[l] = w.scal_host[l].ite;
+        if (w.scal_host[l].status) status = WM_ERR_CG_MAXITER;
+    }
+    if (status != WM_OK) return status;
+    WM_TRY(wm_launch_dfield_bc(g, df, st));
+    k_efield<FView<6, false>, FView<3, false>><<<grid_for((long long)g.nx * g.ny, 256), 256, 0, st>>>(g, fk, df, uf, uj);
+    WM_TRY(wm_check_launch("k_efield"));
+    WM_TRY(wm_launch_dfield_bc(g, df, st));
+    k_field_add<FView<6, false>><<<grid_for((long long)g.nxw * g.nyw, 256), 256, 0, st>>>(g, uf, df);
+    WM_TRY(wm_check_launch("k_field_add"));
+    nl += 6;
+    M("efield_update");
+    if (launches) *launches += nl;
+    return WM_OK;
+}
+
+int wm_launch_energy_fields(const WmGeom &g, FView<6, false> uf, double *partial, int nblocks, cudaStream_t st)
+{
+    k_energy_fields<FView<6, false>><<<nblocks, CG_THREADS, 0, st>>>(g, uf, partial);
+    return wm_check_launch("k_energy_fields");
+}
+
+int wm_launch_sum_partials(const double *partial, int nparts, int nsets, double *out, cudaStream_t st)
+{
+    k_sum_partials<<<1, 32, 0, st>>>(partial, nparts, nsets, out);
+    return wm_check_launch("k_sum_partials");
+}
+
+template int wm_launch_curre_bc<FView<3, false>>(const WmGeom &, FView<3, false>, cudaStream_t);
+template int wm_launch_curre_bc<FView<3, true>>(const WmGeom &, FView<3, true>, cudaStream_t);
+template int wm_launch_dfield_bc<FView<6, false>>(const WmGeom &, FView<6, false>, cudaStream_t);
+template int wm_launch_dfield_bc<FView<6, true>>(const WmGeom &, FView<6, true>, cudaStream_t);

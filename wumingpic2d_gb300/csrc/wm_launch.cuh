@@ -1,0 +1,65 @@
+// wm_launch.cuh -- host launchers exported by the kernel translation units.
+#pragma once
+#include "wm_internal.cuh"
+
+// wm_particles.cu
+template <class PV, class FV>
+int wm_launch_push(const WmGeom &g, const WmConst &k, PV up, PV gp, FV uf, const int *cumcnt, int half_step, int copy_pid,
+                   cudaStream_t st);
+int wm_launch_pid_copy_aos(double *gp, const double *up, long long nslots, cudaStream_t st);
+template <class PV>
+int wm_launch_deposit_cells(const WmGeom &g, const WmConst &k, PV up, PV gp, const int *cumcnt, double *pjcell,
+                            unsigned *status, cudaStream_t st);
+template <class FV3>
+int wm_launch_deposit_fold(const WmGeom &g, FV3 uj, const double *pjcell, cudaStream_t st);
+template <class PV>
+int wm_launch_mom_nvt(const WmGeom &g, const WmConst &k, PV up, const int *np2, double *mom, int max_row_count,
+                      cudaStream_t st);
+template <class PV>
+int wm_launch_energy_particles(const WmGeom &g, const WmConst &k, PV up, const int *np2, double *partial, int nblocks,
+                               cudaStream_t st);
+
+// wm_rebin.cu
+template <class PV>
+int wm_launch_wrap_classify(const WmGeom &g, double delx, PV v, const int *np2, int max_row_count, int mode,
+                            const WmRebinScratch &sc, cudaStream_t st);
+template <class PV>
+int wm_launch_place(const WmGeom &g, PV v, const int *np2, int max_row_count, const WmRebinScratch &sc, int *drow,
+                    cudaStream_t st);
+int wm_launch_np2_after_y(const WmGeom &g, const int *np2, const WmRebinScratch &sc, int *np2_new, int np_limit,
+                          cudaStream_t st);
+template <class PV>
+int wm_launch_scatter_by_P(const WmGeom &g, PV src, PV dst, const int *np2, int max_row_count, const WmRebinScratch &sc,
+                           const int *drow, int np_limit, cudaStream_t st);
+template <class PV>
+int wm_launch_slot_as_P(const WmGeom &g, PV v, const int *np2, int max_row_count, const WmRebinScratch &sc, cudaStream_t st);
+int wm_launch_scan_cells(const WmGeom &g, const WmRebinScratch &sc, int *cumcnt, int *np2_out, cudaStream_t st);
+int wm_launch_rowbase(int nrows, const int *np2, long long *rowbase, cudaStream_t st);
+template <class PV>
+int wm_launch_sort_move(const WmGeom &g, PV src, PV dst, const int *src_np2, int max_row_count, const int *cumcnt,
+                        const WmRebinScratch &sc, cudaStream_t st);
+
+// wm_field.cu
+struct CgScal;
+struct WmFieldWork {
+    double *b, *r, *p, *ap;
+    double *partial;
+    unsigned *ticket;
+    CgScal *scal;
+    CgScal *scal_host;
+};
+typedef void (*wm_mark_fn)(void *ctx, const char *name);
+int wm_field_cg_blocks();
+size_t wm_field_scal_bytes();
+template <class FV>
+int wm_launch_curre_bc(const WmGeom &g, FV uj, cudaStream_t st);
+template <class FV>
+int wm_launch_dfield_bc(const WmGeom &g, FV df, cudaStream_t st);
+int wm_launch_phi_bc(int nx, int ny, double *phi, cudaStream_t st);
+int wm_launch_mom_bc(const WmGeom &g, double *mom, cudaStream_t st);
+int wm_launch_aos_to_soa(int nc, long long npts, const double *a, double *s, cudaStream_t st);
+int wm_launch_soa_to_aos(int nc, long long npts, const double *s, double *a, cudaStream_t st);
+int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<3, false> uj, FView<6, false> df, WmFieldWork &w,
+                   int *iters, int cg_batch, cudaStream_t st, wm_mark_fn mark, void *mctx, long long *launches);
+int wm_launch_energy_fields(const WmGeom &g, FView<6, false> uf, double *partial, int nblocks, cudaStream_t st);
+int wm_launch_sum_partials(const double *partial, int nparts, int nsets, double *out, cudaStream_t st);

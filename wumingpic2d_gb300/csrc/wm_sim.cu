@@ -1,0 +1,590 @@
+// wm_sim.cu -- the resident simulation: particles and fields stay on the GPU across steps.
+//
+// Device state (FP64 path):
+//   particles  two SoA sets A (up) and B (gp) of x, y, ux, uy, uz (f64) and pid (i64), rows
+//              (species-major, then y) stored back to back at rowbase[row], each row sorted by
+//              cell with cumcnt in the reference layout;
+//   fields     uf, df (6 planes) and uj (3 planes) on the ghosted (nx+4) x (ny+4) grid;
+//   work       per-cell partial currents, CG vectors, rebin scratch.
+// One step = the main-loop body of proj/weibel/app.f90:102-107:
+//   push A->B, deposit(A,B)->uj, field solve, then particle_x + particle_y + sort__bucket fused:
+//   classify B (wrap, direction, destination cell), particle_y slots, cell counts -> cumcnt,
+//   and one gather B->A into the new cell-sorted order.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "wm_launch.cuh"
+
+namespace {
+
+__global__ void k_unpack(WmGeom g, const double *__restrict__ stage, int pitch, const int *__restrict__ np2, SoAView dst)
+{
+    const int row = blockIdx.y;
+    const int n = np2[row];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const double *a = stage + 6 * ((long long)row * pitch + s);
+        const long long p = dst.idx(row, s);
+        dst.X(p) = a[0];
+        dst.Y(p) = a[1];
+        dst.UX(p) = a[2];
+        dst.UY(p) = a[3];
+        dst.UZ(p) = a[4];
+        dst.setpid(p, __double_as_longlong(a[5]));
+    }
+}
+
+__global__ void k_pack(WmGeom g, SoAView src, const int *__restrict__ np2, int pitch, double *__restrict__ stage)
+{
+    const int row = blockIdx.y;
+    const int n = np2[row];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < pitch; s += gridDim.x * blockDim.x) {
+        double *a = stage + 6 * ((long long)row * pitch + s);
+        if (s < n) {
+            const long long p = src.idx(row, s);
+            a[0] = src.X(p);
+            a[1] = src.Y(p);
+            a[2] = src.UX(p);
+            a[3] = src.UY(p);
+            a[4] = src.UZ(p);
+            a[5] = __longlong_as_double(src.getpid(p));
+        } else {
+            for (int k = 0; k < 6; ++k) a[k] = 0.0;
+        }
+    }
+}
+
+struct Mark {
+    const char *name;
+    cudaEvent_t ev;
+};
+
+}  // namespace
+
+struct wm_sim {
+    WmGeom g{};
+    WmConst k{};
+    int precision = WM_PREC_FP64;
+    long long cap_req = 0, cap = 0, ntot = 0;
+    cudaStream_t st = nullptr;
+    DevBuf A[6], B[6];
+    DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out;
+    int cur = 0;  // index of the current rowbase/np2
+    // field and rebin work
+    DevBuf f_uf, f_uj, f_df, f_pj, f_b, f_r, f_p, f_ap, f_partial, f_ticket, f_scal;
+    CgScal *scal_host = nullptr;
+    DevBuf rb_dir, rb_ord, rb_P, rb_key, rb_holes, rb_nup, rb_ndown, rb_cellcnt, rb_pairs, rb_status;
+    unsigned *status_host = nullptr;
+    int iters[3] = {0, 0, 0};
+    int max_row = 1;
+    bool loaded = false;
+    // timing
+    bool timing = false;
+    std::vector<Mark> marks;
+    size_t nmarks = 0;
+    std::vector<const char *> t_names;
+    std::vector<double> t_ms;
+    long long launches = 0;
+
+    SoAView view(DevBuf *S, int rb) const
+    {
+        SoAView v;
+        v.x = S[0].as<double>();
+        v.y = S[1].as<double>();
+        v.ux = S[2].as<double>();
+        v.uy = S[3].as<double>();
+        v.uz = S[4].as<double>();
+        v.pid = S[5].as<long long>();
+        v.rowbase = rowbase[rb].as<long long>();
+        return v;
+    }
+    WmRebinScratch scratch() const
+    {
+        WmRebinScratch s;
+        s.dir = rb_dir.as<unsigned char>();
+        s.ord = rb_ord.as<int>();
+        s.P = rb_P.as<int>();
+        s.key = rb_key.as<int>();
+        s.holes = rb_holes.as<int>();
+        s.nup = rb_nup.as<int>();
+        s.ndown = rb_ndown.as<int>();
+        s.cellcnt = rb_cellcnt.as<int>();
+        s.pairs = rb_pairs.as<unsigned long long>();
+        s.np2_new = np2[1 - cur].as<int>();
+        s.rowbase_new = rowbase[1 - cur].as<long long>();
+        s.status = rb_status.as<unsigned>();
+        return s;
+    }
+    WmFieldWork work()
+    {
+        WmFieldWork w;
+        w.b = f_b.as<double>();
+        w.r = f_r.as<double>();
+        w.p = f_p.as<double>();
+        w.ap = f_ap.as<double>();
+        w.partial = f_partial.as<double>();
+        w.ticket = f_ticket.as<unsigned>();
+        w.scal = f_scal.as<CgScal>();
+        w.scal_host = scal_host;
+        return w;
+    }
+    FView<6, false> uf() const { return FView<6, false>{f_uf.as<double>(), g.nxw, g.nyw}; }
+    FView<6, false> df() const { return FView<6, false>{f_df.as<double>(), g.nxw, g.nyw}; }
+    FView<3, false> uj() const { return FView<3, false>{f_uj.as<double>(), g.nxw, g.nyw}; }
+
+    void mark(const char *name)
+    {
+        if (!timing) return;
+        if (nmarks == marks.size()) {
+            Mark m{name, nullptr};
+            cudaEventCreate(&m.ev);
+            marks.push_back(m);
+        }
+        marks[nmarks].name = name;
+        cudaEventRecord(marks[nmarks].ev, st);
+        ++nmarks;
+    }
+    static void mark_cb(void *self, const char *name) { static_cast<wm_sim *>(self)->mark(name); }
+
+    int alloc(long long capacity)
+    {
+        const size_t nf = (size_t)g.nxw * g.nyw, nc = (size_t)g.nx * g.ny;
+        cap = capacity;
+        for (int c = 0; c < 6; ++c) {
+            WM_TRY(A[c].ensure(8 * (size_t)cap));
+            WM_TRY(B[c].ensure(8 * (size_t)cap));
+        }
+        for (int c = 0; c < 2; ++c) {
+            WM_TRY(rowbase[c].ensure(sizeof(long long) * (g.nrows + 1)));
+            WM_TRY(np2[c].ensure(sizeof(int) * g.nrows));
+        }
+        WM_TRY(cumcnt.ensure(sizeof(int) * (size_t)(g.nx + 1) * g.nrows));
+        WM_TRY(f_uf.ensure(sizeof(double) * 6 * nf));
+        WM_TRY(f_df.ensure(sizeof(double) * 6 * nf));
+        WM_TRY(f_uj.ensure(sizeof(double) * 3 * nf));
+        WM_TRY(f_pj.ensure(sizeof(double) * 75 * nc));
+        WM_TRY(f_b.ensure(sizeof(double) * 3 * nc));
+        WM_TRY(f_r.ensure(sizeof(double) * 3 * nc));
+        WM_TRY(f_p.ensure(sizeof(double) * 3 * nc));
+        WM_TRY(f_ap.ensure(sizeof(double) * 3 * nc));
+        WM_TRY(f_partial.ensure(sizeof(double) * 3 * wm_field_cg_blocks()));
+        WM_TRY(f_ticket.ensure(sizeof(unsigned)));
+        WM_CUDA(cudaMemsetAsync(f_ticket.p, 0, sizeof(unsigned), st));
+        WM_TRY(f_scal.ensure(wm_field_scal_bytes()));
+        WM_TRY(rb_dir.ensure((size_t)cap));
+        WM_TRY(rb_ord.ensure(4 * (size_t)cap));
+        WM_TRY(rb_P.ensure(4 * (size_t)cap));
+        WM_TRY(rb_key.ensure(4 * (size_t)cap));
+        WM_TRY(rb_holes.ensure(4 * (size_t)cap));
+        WM_TRY(rb_pairs.ensure(8 * (size_t)cap));
+        WM_TRY(rb_nup.ensure(sizeof(int) * g.nrows));
+        WM_TRY(rb_ndown.ensure(sizeof(int) * g.nrows));
+        WM_TRY(rb_cellcnt.ensure(sizeof(int) * (size_t)g.nrows * g.nx));
+        WM_TRY(rb_status.ensure(sizeof(unsigned)));
+        WM_TRY(energy_partial.ensure(sizeof(double) * 304 * (g.nsp + 2)));
+        WM_TRY(energy_out.ensure(sizeof(double) * (g.nsp + 2)));
+        return WM_OK;
+    }
+
+    size_t device_bytes() const
+    {
+        size_t t = 0;
+        for (int c = 0; c < 6; ++c) t += A[c].bytes + B[c].bytes;
+        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &f_uf, &f_uj, &f_df, &f_pj,
+                                &f_b, &f_r, &f_p, &f_ap, &f_partial, &rb_dir, &rb_ord, &rb_P, &rb_key, &rb_holes, &rb_nup,
+                                &rb_ndown, &rb_cellcnt, &rb_pairs})
+            t += b->bytes;
+        return t;
+    }
+
+    void release()
+    {
+        if (st) cudaStreamSynchronize(st);
+        for (int c = 0; c < 6; ++c) {
+            A[c].release();
+            B[c].release();
+        }
+        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out,
+                          &f_uf, &f_uj, &f_df, &f_pj, &f_b, &f_r, &f_p, &f_ap, &f_partial, &f_ticket, &f_scal, &rb_dir, &rb_ord,
+                          &rb_P, &rb_key, &rb_holes, &rb_nup, &rb_ndown, &rb_cellcnt, &rb_pairs, &rb_status})
+            b->release();
+        for (Mark &m : marks) cudaEventDestroy(m.ev);
+        marks.clear();
+        if (scal_host) cudaFreeHost(scal_host);
+        if (status_host) cudaFreeHost(status_host);
+        scal_host = nullptr;
+        status_host = nullptr;
+        if (st) cudaStreamDestroy(st);
+        st = nullptr;
+    }
+
+    int check_status()
+    {
+        WM_CUDA(cudaMemcpyAsync(status_host, rb_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        WM_CUDA(cudaStreamSynchronize(st));
+        const unsigned d = *status_host;
+        if (d & WMDEV_OVERFLOW) return WM_ERR_OVERFLOW;
+        if (d & (WMDEV_CELL | WMDEV_ROWJUMP)) return WM_ERR_CELL;
+        return WM_OK;
+    }
+
+    // Upload a reference-layout particle array (np slots per row, np2 used) into set S.
+    int upload_particles(const double *up, const int *np2_h, DevBuf *S)
+    {
+        const int maxc = std::max(1, *std::max_element(np2_h, np2_h + g.nrows));
+        if (maxc > g.np) return WM_ERR_BAD_ARG;
+        WM_TRY(stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
+        WM_CUDA(cudaMemcpy2DAsync(stage.p, sizeof(double) * 6 * maxc, up, sizeof(double) * 6 * g.np, sizeof(double) * 6 * maxc,
+                                  g.nrows, cudaMemcpyHostToDevice, st));
+        WM_CUDA(cudaMemcpyAsync(np2[cur].p, np2_h, sizeof(int) * g.nrows, cudaMemcpyHostToDevice, st));
+        WM_TRY(wm_launch_rowbase(g.nrows, np2[cur].as<int>(), rowbase[cur].as<long long>(), st));
+        dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
+        k_unpack<<<grid, 256, 0, st>>>(g, stage.as<double>(), maxc, np2[cur].as<int>(), view(S, cur));
+        WM_TRY(wm_check_launch("k_unpack"));
+        max_row = maxc;
+        return WM_OK;
+    }
+
+    int upload_fields(const double *uf_h)
+    {
+        const long long npts = (long long)g.nxw * g.nyw;
+        WM_TRY(uf_aos.ensure(sizeof(double) * 6 * npts));
+        WM_CUDA(cudaMemcpyAsync(uf_aos.p, uf_h, sizeof(double) * 6 * npts, cudaMemcpyHostToDevice, st));
+        return wm_launch_aos_to_soa(6, npts, uf_aos.as<double>(), f_uf.as<double>(), st);
+    }
+
+    // sort__bucket of set B into set A (load path)
+    int sort_B_into_A()
+    {
+        WmRebinScratch sc = scratch();
+        WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
+        SoAView vb = view(B, cur);
+        WM_TRY(wm_launch_wrap_classify(g, k.delx, vb, np2[cur].as<int>(), max_row, 8, sc, st));
+        WM_TRY(wm_launch_slot_as_P(g, vb, np2[cur].as<int>(), max_row, sc, st));
+        WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
+        WM_TRY(check_status());
+        WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
+        WM_TRY(wm_launch_sort_move(g, vb, view(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
+        cur = 1 - cur;
+        return WM_OK;
+    }
+
+    int step_once()
+    {
+        WmRebinScratch sc = scratch();
+        long long nl = 0;
+        WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
+        mark("start");
+        SoAView va = view(A, cur), vb = view(B, cur);
+        WM_TRY(wm_launch_push(g, k, va, vb, uf(), cumcnt.as<int>(), 0, 1, st));
+        ++nl;
+        mark("push");
+        WM_TRY(wm_launch_deposit_cells(g, k, va, vb, cumcnt.as<int>(), f_pj.as<double>(), sc.status, st));
+        WM_TRY(wm_launch_deposit_fold(g, uj(), f_pj.as<double>(), st));
+        nl += 2;
+        mark("deposit");
+        WmFieldWork w = work();
+        const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl);
+        if (s != WM_OK) return s;
+        WM_TRY(wm_launch_wrap_classify(g, k.delx, vb, np2[cur].as<int>(), max_row, 1 | 2 | 4, sc, st));
+        nl += 1;
+        mark("classify");
+        WM_TRY(wm_launch_place(g, vb, np2[cur].as<int>(), max_row, sc, nullptr, st));
+        WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
+        WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
+        nl += 4;
+        mark("place_scan");
+        WM_TRY(wm_launch_sort_move(g, vb, view(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
+        nl += 2;
+        mark("sort_move");
+        cur = 1 - cur;
+        launches += nl;
+        return check_status();
+    }
+};
+
+extern "C" {
+
+int wm_sim_create(const wm_sim_config *cfg, wm_sim **out)
+{
+    if (!cfg || !out) return WM_ERR_BAD_ARG;
+    *out = nullptr;
+    if (cfg->precision != WM_PREC_FP64 && cfg->precision != WM_PREC_MIXED) return WM_ERR_BAD_ARG;
+    if (cfg->precision == WM_PREC_MIXED) return WM_ERR_UNSUPPORTED;
+    if (cfg->nsp < 1 || cfg->nsp > WM_MAX_SP || cfg->nx < 4 || cfg->ny < 4 || cfg->np < 1) return WM_ERR_BAD_ARG;
+    if (cfg->cg_itemax < 1 || !(cfg->cg_err > 0)) return WM_ERR_BAD_ARG;
+    wm_sim *s = new wm_sim();
+    WmGeom &g = s->g;
+    g.ndim = 6;
+    g.np = cfg->np;
+    g.nsp = cfg->nsp;
+    g.nxgs = 2;
+    g.nxge = 2 + cfg->nx - 1;
+    g.nygs = 2;
+    g.nyge = 2 + cfg->ny - 1;
+    g.nys = g.nygs;
+    g.nye = g.nyge;
+    g.nx = cfg->nx;
+    g.ny = cfg->ny;
+    g.nrows = g.nsp * g.ny;
+    g.nxw = g.nx + 4;
+    g.nyw = g.ny + 4;
+    WmConst &k = s->k;
+    k.delx = cfg->delx;
+    k.delt = cfg->delt;
+    k.c = cfg->c;
+    k.gfac = cfg->gfac;
+    for (int i = 0; i < WM_MAX_SP; ++i) {
+        k.q[i] = i < cfg->nsp ? cfg->q[i] : 0.0;
+        k.r[i] = i < cfg->nsp ? cfg->r[i] : 1.0;
+    }
+    k.cg_err = cfg->cg_err;
+    k.cg_itemax = cfg->cg_itemax;
+    s->precision = cfg->precision;
+    s->cap_req = cfg->capacity;
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost((void **)&s->scal_host, wm_field_scal_bytes()) != cudaSuccess ||
+        cudaMallocHost((void **)&s->status_host, sizeof(unsigned)) != cudaSuccess) {
+        s->release();
+        delete s;
+        return WM_ERR_CUDA;
+    }
+    *out = s;
+    return WM_OK;
+}
+
+int wm_sim_destroy(wm_sim *s)
+{
+    if (!s) return WM_ERR_BAD_ARG;
+    s->release();
+    delete s;
+    return WM_OK;
+}
+
+static int sim_load_common(wm_sim *s, const double *up, const double *uf, const int *np2_h, const int *cumcnt_h)
+{
+    const WmGeom &g = s->g;
+    long long ntot = 0;
+    for (int r = 0; r < g.nrows; ++r) {
+        if (np2_h[r] < 0 || np2_h[r] > g.np) return WM_ERR_BAD_ARG;
+        ntot += np2_h[r];
+    }
+    if (ntot >= (1LL << 32)) return WM_ERR_UNSUPPORTED;
+    long long cap = std::max<long long>(ntot, 1);
+    if (s->cap_req > cap) cap = s->cap_req;
+    if (!s->loaded || cap > s->cap) WM_TRY(s->alloc(cap));
+    s->ntot = ntot;
+    if (cumcnt_h) {  // already sorted: upload straight into A
+        WM_TRY(s->upload_particles(up, np2_h, s->A));
+        WM_CUDA(cudaMemcpyAsync(s->cumcnt.p, cumcnt_h, sizeof(int) * (size_t)(g.nx + 1) * g.nrows, cudaMemcpyHostToDevice, s->st));
+    } else {
+        WM_TRY(s->upload_particles(up, np2_h, s->B));
+        WM_TRY(s->sort_B_into_A());
+    }
+    WM_TRY(s->upload_fields(uf));
+    if (!s->loaded) {
+        const size_t nf = (size_t)g.nxw * g.nyw;
+        WM_CUDA(cudaMemsetAsync(s->f_df.p, 0, sizeof(double) * 6 * nf, s->st));
+        WM_CUDA(cudaMemsetAsync(s->f_uj.p, 0, sizeof(double) * 3 * nf, s->st));
+    }
+    s->loaded = true;
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    return WM_OK;
+}
+
+int wm_sim_load(wm_sim *s, const double *up, const double *uf, const int *np2_h)
+{
+    if (!s || !up || !uf || !np2_h) return WM_ERR_BAD_ARG;
+    return sim_load_common(s, up, uf, np2_h, nullptr);
+}
+
+int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    const WmGeom &g = s->g;
+    std::vector<int> cnt(g.nrows);
+    WM_CUDA(cudaMemcpyAsync(cnt.data(), s->np2[s->cur].p, sizeof(int) * g.nrows, cudaMemcpyDeviceToHost, s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    const int maxc = std::max(1, *std::max_element(cnt.begin(), cnt.end()));
+    if (maxc > g.np) return WM_ERR_OVERFLOW;
+    if (up) {
+        WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
+        dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
+        k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), maxc, s->stage.as<double>());
+        WM_TRY(wm_check_launch("k_pack"));
+        WM_CUDA(cudaMemcpy2DAsync(up, sizeof(double) * 6 * g.np, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * maxc,
+                                  g.nrows, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (uf) {
+        const long long npts = (long long)g.nxw * g.nyw;
+        WM_TRY(s->uf_aos.ensure(sizeof(double) * 6 * npts));
+        WM_TRY(wm_launch_soa_to_aos(6, npts, s->f_uf.as<double>(), s->uf_aos.as<double>(), s->st));
+        WM_CUDA(cudaMemcpyAsync(uf, s->uf_aos.p, sizeof(double) * 6 * npts, cudaMemcpyDeviceToHost, s->st));
+    }
+    if (cumcnt_h)
+        WM_CUDA(cudaMemcpyAsync(cumcnt_h, s->cumcnt.p, sizeof(int) * (size_t)(g.nx + 1) * g.nrows, cudaMemcpyDeviceToHost, s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    if (np2_h) std::memcpy(np2_h, cnt.data(), sizeof(int) * g.nrows);
+    return WM_OK;
+}
+
+int wm_sim_step(wm_sim *s, int nsteps)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    s->nmarks = 0;
+    s->launches = 0;
+    s->t_names.clear();
+    s->t_ms.clear();
+    for (int i = 0; i < nsteps; ++i) WM_TRY(s->step_once());
+    if (s->timing && s->nmarks > 1) {
+        WM_CUDA(cudaStreamSynchronize(s->st));
+        for (size_t m = 1; m < s->nmarks; ++m) {
+            if (std::strcmp(s->marks[m].name, "start") == 0) continue;
+            float ms = 0.f;
+            WM_CUDA(cudaEventElapsedTime(&ms, s->marks[m - 1].ev, s->marks[m].ev));
+            size_t idx = 0;
+            while (idx < s->t_names.size() && std::strcmp(s->t_names[idx], s->marks[m].name) != 0) ++idx;
+            if (idx == s->t_names.size()) {
+                s->t_names.push_back(s->marks[m].name);
+                s->t_ms.push_back(0.0);
+            }
+            s->t_ms[idx] += ms;
+        }
+    }
+    return WM_OK;
+}
+
+int wm_sim_step_host(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h, int nsteps)
+{
+    if (!s || !up || !uf || !np2_h || !cumcnt_h) return WM_ERR_BAD_ARG;
+    WM_TRY(sim_load_common(s, up, uf, np2_h, cumcnt_h));
+    WM_TRY(wm_sim_step(s, nsteps));
+    return wm_sim_store(s, up, uf, np2_h, cumcnt_h);
+}
+
+int wm_sim_energy(wm_sim *s, double *out)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    const WmGeom &g = s->g;
+    const int nb = 304;
+    double *part = s->energy_partial.as<double>();
+    WM_TRY(wm_launch_energy_particles(g, s->k, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), part, nb, s->st));
+    WM_TRY(wm_launch_energy_fields(g, s->uf(), part + (size_t)nb * g.nsp, nb, s->st));
+    WM_TRY(wm_launch_sum_partials(part, nb, g.nsp + 2, s->energy_out.as<double>(), s->st));
+    std::vector<double> tmp(g.nsp + 2);
+    WM_CUDA(cudaMemcpyAsync(tmp.data(), s->energy_out.p, sizeof(double) * (g.nsp + 2), cudaMemcpyDeviceToHost, s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    const double pi = 3.14159265358979311599796346854418516;
+    for (int i = 0; i < g.nsp; ++i) out[i] = tmp[i];
+    out[g.nsp] = tmp[g.nsp + 1] / (8 * pi);
+    out[g.nsp + 1] = tmp[g.nsp] / (8 * pi);
+    return WM_OK;
+}
+
+int wm_sim_moments(wm_sim *s, double *mom)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    const WmGeom &g = s->g;
+    SoAView va = s->view(s->A, s->cur), vb = s->view(s->B, s->cur);
+    WM_TRY(wm_launch_push(g, s->k, va, vb, s->uf(), s->cumcnt.as<int>(), 1, 0, s->st));
+    const size_t nm = (size_t)7 * (g.nx + 2) * (g.ny + 2) * g.nsp;
+    WM_TRY(s->stage.ensure(sizeof(double) * nm));
+    WM_TRY(wm_launch_mom_nvt(g, s->k, vb, s->np2[s->cur].as<int>(), s->stage.as<double>(), s->max_row, s->st));
+    WM_TRY(wm_launch_mom_bc(g, s->stage.as<double>(), s->st));
+    WM_CUDA(cudaMemcpyAsync(mom, s->stage.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    return WM_OK;
+}
+
+int wm_sim_cg_iters(wm_sim *s, int *iters3)
+{
+    if (!s) return WM_ERR_BAD_ARG;
+    for (int l = 0; l < 3; ++l) iters3[l] = s->iters[l];
+    return WM_OK;
+}
+
+int wm_sim_kernel_times(wm_sim *s, const char **names, double *ms, int *n)
+{
+    if (!s || !n) return WM_ERR_BAD_ARG;
+    const int cnt = (int)s->t_names.size();
+    for (int i = 0; i < std::min(cnt, *n); ++i) {
+        if (names) names[i] = s->t_names[i];
+        if (ms) ms[i] = s->t_ms[i];
+    }
+    *n = cnt;
+    return WM_OK;
+}
+
+int wm_sim_set_timing(wm_sim *s, int on)
+{
+    if (!s) return WM_ERR_BAD_ARG;
+    s->timing = on != 0;
+    return WM_OK;
+}
+
+int wm_sim_launches(wm_sim *s, int64_t *count)
+{
+    if (!s || !count) return WM_ERR_BAD_ARG;
+    *count = s->launches;
+    return WM_OK;
+}
+
+int wm_sim_info(wm_sim *s, int64_t *nparticles, int64_t *device_bytes)
+{
+    if (!s) return WM_ERR_BAD_ARG;
+    if (nparticles) *nparticles = s->ntot;
+    if (device_bytes) *device_bytes = (int64_t)s->device_bytes();
+    return WM_OK;
+}
+
+int wm_sim_sync(wm_sim *s)
+{
+    if (!s) return WM_ERR_BAD_ARG;
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    return WM_OK;
+}
+
+int wm_sim_get_work(wm_sim *s, double *df, double *uj)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    const WmGeom &g = s->g;
+    const long long npts = (long long)g.nxw * g.nyw;
+    WM_TRY(s->uf_aos.ensure(sizeof(double) * 6 * npts));
+    if (df) {
+        WM_TRY(wm_launch_soa_to_aos(6, npts, s->f_df.as<double>(), s->uf_aos.as<double>(), s->st));
+        WM_CUDA(cudaMemcpyAsync(df, s->uf_aos.p, sizeof(double) * 6 * npts, cudaMemcpyDeviceToHost, s->st));
+        WM_CUDA(cudaStreamSynchronize(s->st));
+    }
+    if (uj) {
+        WM_TRY(wm_launch_soa_to_aos(3, npts, s->f_uj.as<double>(), s->uf_aos.as<double>(), s->st));
+        WM_CUDA(cudaMemcpyAsync(uj, s->uf_aos.p, sizeof(double) * 3 * npts, cudaMemcpyDeviceToHost, s->st));
+        WM_CUDA(cudaStreamSynchronize(s->st));
+    }
+    return WM_OK;
+}
+
+int wm_sim_set_work(wm_sim *s, const double *df)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    const WmGeom &g = s->g;
+    const long long npts = (long long)g.nxw * g.nyw;
+    WM_TRY(s->uf_aos.ensure(sizeof(double) * 6 * npts));
+    WM_CUDA(cudaMemcpyAsync(s->uf_aos.p, df, sizeof(double) * 6 * npts, cudaMemcpyHostToDevice, s->st));
+    WM_TRY(wm_launch_aos_to_soa(6, npts, s->uf_aos.as<double>(), s->f_df.as<double>(), s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    return WM_OK;
+}
+
+int wm_host_register(void *ptr, size_t bytes)
+{
+    WM_CUDA(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));
+    return WM_OK;
+}
+
+int wm_host_unregister(void *ptr)
+{
+    WM_CUDA(cudaHostUnregister(ptr));
+    return WM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,133 @@
+"""Resident simulation: particles and fields stay on the GPU between steps.
+
+Simulation wraps the wm_sim_* entry points.  A state in the reference layout
+(up, uf, np2) is loaded once and cell-sorted on the GPU; step(n) runs the
+main-loop body of proj/weibel/app.f90:102-107 n times; store() writes the state
+back into reference-layout arrays.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._native import WM_PREC_FP64, WM_PREC_MIXED, SimConfig, check, lib
+from .layout import Dims
+
+PRECISIONS = {"fp64": WM_PREC_FP64, "mixed": WM_PREC_MIXED}
+
+
+class Simulation:
+    def __init__(self, dims: Dims, delt: float, q, r, c: float = 1.0, delx: float = 1.0, gfac: float = 0.501,
+                 cg_err: float = 1e-6, cg_itemax: int = 100, precision: str = "fp64", capacity: int = 0):
+        if dims.nxgs != 2 or dims.nygs != 2:
+            raise ValueError("the resident simulation uses nxgs = nygs = 2 like the reference apps")
+        self.dims = dims
+        cfg = SimConfig()
+        cfg.nx, cfg.ny, cfg.nsp, cfg.np = dims.nx, dims.ny, dims.nsp, dims.np
+        cfg.delx, cfg.delt, cfg.c, cfg.gfac = delx, delt, c, gfac
+        for k in range(dims.nsp):
+            cfg.q[k] = float(q[k])
+            cfg.r[k] = float(r[k])
+        cfg.cg_err, cfg.cg_itemax = cg_err, cg_itemax
+        cfg.precision = PRECISIONS[precision]
+        cfg.capacity = capacity
+        self._h = ctypes.c_void_p()
+        check(lib().wm_sim_create(ctypes.byref(cfg), ctypes.byref(self._h)), "wm_sim_create")
+
+    # ------------------------------------------------------------------ state
+    def load(self, up: np.ndarray, uf: np.ndarray, np2: np.ndarray) -> None:
+        check(lib().wm_sim_load(self._h, up.ctypes.data, uf.ctypes.data, np2.ctypes.data), "wm_sim_load")
+
+    def store(self, up=None, uf=None, np2=None, cumcnt=None):
+        d = self.dims
+        up = d.alloc_up() if up is None else up
+        uf = d.alloc_uf() if uf is None else uf
+        np2 = d.alloc_np2() if np2 is None else np2
+        cumcnt = d.alloc_cumcnt() if cumcnt is None else cumcnt
+        check(lib().wm_sim_store(self._h, up.ctypes.data, uf.ctypes.data, np2.ctypes.data, cumcnt.ctypes.data),
+              "wm_sim_store")
+        return up, uf, np2, cumcnt
+
+    def step(self, nsteps: int = 1) -> None:
+        check(lib().wm_sim_step(self._h, int(nsteps)), "wm_sim_step")
+
+    def step_host(self, up, uf, np2, cumcnt, nsteps: int = 1) -> None:
+        """One call with host buffers: copy in, nsteps steps, copy out (the drop-in path)."""
+        check(lib().wm_sim_step_host(self._h, up.ctypes.data, uf.ctypes.data, np2.ctypes.data, cumcnt.ctypes.data,
+                                     int(nsteps)), "wm_sim_step_host")
+
+    def sync(self) -> None:
+        check(lib().wm_sim_sync(self._h), "wm_sim_sync")
+
+    # ------------------------------------------------------------ diagnostics
+    def energy(self) -> np.ndarray:
+        out = np.zeros(self.dims.nsp + 2)
+        check(lib().wm_sim_energy(self._h, out.ctypes.data), "wm_sim_energy")
+        return out
+
+    def moments(self) -> np.ndarray:
+        mom = self.dims.alloc_mom()
+        check(lib().wm_sim_moments(self._h, mom.ctypes.data), "wm_sim_moments")
+        return mom
+
+    def cg_iters(self) -> np.ndarray:
+        out = np.zeros(3, dtype=np.int32)
+        check(lib().wm_sim_cg_iters(self._h, out.ctypes.data), "wm_sim_cg_iters")
+        return out
+
+    def get_work(self):
+        d = self.dims
+        df = d.alloc_uf()
+        uj = d.alloc_uj()
+        check(lib().wm_sim_get_work(self._h, df.ctypes.data, uj.ctypes.data), "wm_sim_get_work")
+        return df, uj
+
+    def set_work(self, df: np.ndarray) -> None:
+        check(lib().wm_sim_set_work(self._h, df.ctypes.data), "wm_sim_set_work")
+
+    def set_timing(self, on: bool) -> None:
+        check(lib().wm_sim_set_timing(self._h, 1 if on else 0), "wm_sim_set_timing")
+
+    def kernel_times(self) -> dict:
+        n = ctypes.c_int(64)
+        names = (ctypes.c_char_p * 64)()
+        ms = (ctypes.c_double * 64)()
+        check(lib().wm_sim_kernel_times(self._h, names, ms, ctypes.byref(n)), "wm_sim_kernel_times")
+        return {names[i].decode(): ms[i] for i in range(n.value)}
+
+    def launches(self) -> int:
+        c = ctypes.c_int64()
+        check(lib().wm_sim_launches(self._h, ctypes.byref(c)), "wm_sim_launches")
+        return c.value
+
+    def info(self):
+        n, b = ctypes.c_int64(), ctypes.c_int64()
+        check(lib().wm_sim_info(self._h, ctypes.byref(n), ctypes.byref(b)), "wm_sim_info")
+        return n.value, b.value
+
+    def close(self) -> None:
+        if self._h:
+            lib().wm_sim_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def pin(a: np.ndarray) -> None:
+    """Page-lock a numpy array in place (cudaHostRegister)."""
+    check(lib().wm_host_register(a.ctypes.data, a.nbytes), "wm_host_register")
+
+
+def unpin(a: np.ndarray) -> None:
+    check(lib().wm_host_unregister(a.ctypes.data), "wm_host_unregister")
