@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Particle-updates per second of the WumingPIC2D time step on one GB300.
+
+Workload (default): the 2048 x 2048 periodic Weibel plasma, 64 particles per cell per
+species (5.37e8 particles), c dt/dx = 0.5, omega_pe dt = 0.05, mi/me = 25, electron beams
+at +/-0.3c with vth_e = 0.05c, vth_i = 0.01c, fields start at zero; seeded synthetic state.
+One step = push + Esirkepov deposit + implicit field solve (CG) + periodic particle
+boundaries + per-cell counting sort (proj/weibel/app.f90:102-107).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value    particle-updates/s with the state resident in HBM, K steps timed with CUDA events.
+e2e      the same metric through the host-buffer entry point (wm_sim_step_host): every step
+         copies the reference-layout state in from pinned host memory and back out.
+roofline the dominant particle kernel's algorithmic bytes per launch / its event time.
+cpu_baseline  the CPU restatement of the reference step (oracle/, OpenMP on every host core)
+         on a bounded sample of the same workload.
+--impl reference times that CPU restatement alone (the reference is Fortran + MPI and no
+Fortran compiler exists on this machine).
+Under torchrun (N > 1) each rank runs an independent replica on its own GPU (the path does
+not shard: replicas only); rank 0 prints the line, value = total over ranks / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-updates/s, full PIC step (Weibel 2048^2, 64 ppc/species)"
+UNIT = "particle-updates/s"
+L2_BYTES = 129e6
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--nx", type=int, default=2048)
+    p.add_argument("--ny", type=int, default=2048)
+    p.add_argument("--ppc", type=int, default=64)
+    p.add_argument("--seed", type=int, default=2024)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--cpu-rows", type=int, default=64, help="rows of the CPU sample strip")
+    p.add_argument("--cpu-steps", type=int, default=2)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ distributed
+class Dist:
+    def __init__(self, n):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ----------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per particle of the particle kernels from the committed ncu summary, if any."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_sample(args, steps: int):
+    """The CPU restatement (OpenMP, every host core) on a strip of the workload."""
+    from oracle import oracle as O
+    from wumingpic2d_gb300.weibel import WeibelConfig, weibel_particles
+
+    cfg = WeibelConfig(nx=args.nx, ny=args.cpu_rows, ppc=args.ppc, seed=args.seed + 7, slack=1.2)
+    d = cfg.dims()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    par = O.make_par(d, cfg.delt, cfg.charge, cfg.mass)
+    up0, np2 = weibel_particles(cfg)
+    up, cum = d.alloc_up(), d.alloc_cumcnt()
+    assert O.sort_bucket(par, d, up, up0, cum, np2) == 0
+    del up0
+    gp, uf, st = up.copy(order="F"), d.alloc_uf(), O.OracleState(d)
+    npart = int(np2.sum())
+    O.step(par, d, up, gp, uf, cum, np2, st)  # warm caches and thread pool
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s, _ = O.step(par, d, up, gp, uf, cum, np2, st)
+        assert s == 0
+    dt = time.perf_counter() - t0
+    sample = (f"{args.nx}x{args.cpu_rows}-cell periodic strip of the workload, {args.ppc} ppc/species "
+              f"({npart} particles), {steps} steps, OMP_NUM_THREADS={threads}")
+    return npart * steps / dt, threads, sample
+
+
+# ---------------------------------------------------------------------- GB300 arm
+def run_gpu(args, dist: Dist):
+    from wumingpic2d_gb300.sim import Simulation, pin, set_device, unpin
+    from wumingpic2d_gb300.weibel import WeibelConfig, weibel_particles
+
+    set_device(dist.local)
+    cfg = WeibelConfig(nx=args.nx, ny=args.ny, ppc=args.ppc, seed=args.seed + dist.rank, slack=1.1)
+    d = cfg.dims()
+    t_init = time.perf_counter()
+    up0, np2 = weibel_particles(cfg)
+    uf = d.alloc_uf()
+    sim = Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision=args.precision)
+    sim.load(up0, uf, np2)
+    t_init = time.perf_counter() - t_init
+    ntot, dev_bytes = sim.info()
+    sim.step(args.warmup)
+    sim.set_timing(True)
+
+    clocks = ClockSampler(dist.local)
+    dist.barrier()
+    clocks.start()
+    ms = sim.step_timed(args.steps)
+    clk = clocks.stop()
+    dist.barrier()
+    launches = sim.launches()
+    ktimes = sim.kernel_times()
+    iters = sim.cg_iters().tolist()
+    sim.set_timing(False)
+    ms_max = dist.max(ms)
+    total = dist.sum(float(ntot)) * args.steps
+    value = total / (ms_max / 1e3)
+
+    # e2e through the host-buffer entry point, pinned host state
+    e2e = None
+    if not args.no_e2e:
+        up_h, uf_h, np2_h, cc_h = sim.store(up=up0)
+        del up0
+        pin(up_h)
+        pin(uf_h)
+        maxc = int(np2_h.max())
+        h2d = 48 * maxc * d.nsp * d.ny + uf_h.nbytes + np2_h.nbytes + cc_h.nbytes
+        d2h = h2d
+        sim.step_host(up_h, uf_h, np2_h, cc_h, 1)  # warm-up of the copy path
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            sim.step_host(up_h, uf_h, np2_h, cc_h, 1)
+        dt = dist.max(time.perf_counter() - t0)
+        e2e = {"value": dist.sum(float(ntot)) * args.e2e_steps / dt, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "path": "wm_sim_step_host: reference-layout host arrays in and out every step (pinned)"}
+        unpin(up_h)
+        unpin(uf_h)
+    sim.close()
+    return dict(ntot=ntot, ms=ms_max, value=value, launches=launches, ktimes=ktimes, iters=iters, clocks=clk, e2e=e2e,
+                dev_bytes=dev_bytes, t_init=t_init, d=d, cfg=cfg)
+
+
+def roofline(res, args):
+    peaks, src = measured_peaks()
+    kt = res["ktimes"]
+    steps = args.steps
+    ntot = res["ntot"]
+    # algorithmic bytes per particle of the particle kernels (FP64 state: 8 B per component)
+    algo = {"push": 80, "deposit": 56, "sort_move": 96}
+    cand = {k: v for k, v in kt.items() if k in algo}
+    if not cand:
+        return None
+    name = max(cand, key=cand.get)
+    t = cand[name] / steps / 1e3
+    achieved = algo[name] * ntot / t / 1e9
+    tr = ncu_traffic().get(f"{args.precision}:{name}")
+    return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": (tr * ntot if tr else None), "bytes_per_particle_algorithmic": algo[name],
+            "ms_per_launch": round(t * 1e3, 3)}
+
+
+def main():
+    args = parse()
+    dist = Dist(args.gpus)
+    workload = (f"Weibel {args.nx}x{args.ny} periodic, {args.ppc} ppc/species, 2 species, cfl 0.5, "
+                f"omega_pe dt 0.05, mi/me 25, beams +/-0.3c")
+    if args.impl == "reference":
+        if dist.rank != 0:
+            dist.close()
+            return
+        v, cores, sample = cpu_sample(args, max(1, args.steps))
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
+                "config": {"workload": workload, "nx": args.nx, "ny": args.ny, "ppc": args.ppc},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                                 "note": "C restatement of the reference step (no Fortran compiler on this machine)"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        dist.close()
+        return
+
+    res = run_gpu(args, dist)
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu:
+        v, cores, sample = cpu_sample(args, args.cpu_steps)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    if dist.rank == 0:
+        d = res["d"]
+        kt = res["ktimes"]
+        line = {
+            "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "data": "synthetic (seeded Philox Weibel beams)",
+            "config": {"workload": workload, "nx": d.nx, "ny": d.ny, "ppc": args.ppc, "particles": res["ntot"],
+                       "precision": args.precision, "parallelism": f"replicas x{dist.world}",
+                       "l2": f"inputs larger than L2 ({res['ntot'] * 48 / 1e9:.1f} GB of particles vs 129 MB)",
+                       "cg_iters_last_step": res["iters"], "cg_tol": 1e-6},
+            "roofline": roofline(res, args),
+            "cpu_baseline": cpu,
+            "e2e": res["e2e"],
+            "gpu_launches": res["launches"],
+            "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in kt.items()},
+            "clocks": res["clocks"],
+            "device_bytes": res["dev_bytes"],
+            "setup_s": round(res["t_init"], 1),
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -161,6 +161,11 @@ int wm_sim_launches(wm_sim *s, int64_t *count);
 int wm_sim_info(wm_sim *s, int64_t *nparticles, int64_t *device_bytes);
 /* Block until every launched step has finished. */
 int wm_sim_sync(wm_sim *s);
+/* wm_sim_step bracketed by CUDA events on the simulation's stream: *ms = GPU time of the
+ * nsteps steps (host synchronisations inside the step loop included). */
+int wm_sim_step_timed(wm_sim *s, int nsteps, double *ms);
+/* Select the CUDA device used by the calling host thread (one process per GPU). */
+int wm_set_device(int device);
 
 /* The SAVE'd field work arrays of the resident simulation (see wm_field_get_work). */
 int wm_sim_get_work(wm_sim *s, double *df, double *uj);

@@ -550,22 +550,27 @@ int wmo_field_fdtd_i(const wmo_par *P, double *uf, const double *up, const doubl
  * the Fortran IEEE rules restore the caller's mode on return, which fesetround mirrors here. */
 void wmo_bc_particle_x(const wmo_par *P, double *up, const int *np2)
 {
-    const int save = fegetround();
-    fesetround(FE_DOWNWARD);
     const double delx = P->delx;
     for (int isp = 1; isp <= P->nsp; ++isp) {
-#pragma omp parallel for
-        for (int j = P->nys; j <= P->nye; ++j)
-            for (int ii = 1; ii <= NP2(j, isp); ++ii) {
-                volatile double x = UP(1, ii, j, isp);
-                const int ipos = (int)(x / delx);
-                if (ipos < P->nxgs)
-                    UP(1, ii, j, isp) = x + (P->nxge - P->nxgs + 1) * delx;
-                else if (ipos >= P->nxge + 1)
-                    UP(1, ii, j, isp) = x - (P->nxge - P->nxgs + 1) * delx;
-            }
+        /* The rounding mode is per thread: every OpenMP thread switches to downward rounding,
+         * which gives the single-thread semantics of the reference at any thread count. */
+#pragma omp parallel
+        {
+            const int save = fegetround();
+            fesetround(FE_DOWNWARD);
+#pragma omp for
+            for (int j = P->nys; j <= P->nye; ++j)
+                for (int ii = 1; ii <= NP2(j, isp); ++ii) {
+                    volatile double x = UP(1, ii, j, isp);
+                    const int ipos = (int)(x / delx);
+                    if (ipos < P->nxgs)
+                        UP(1, ii, j, isp) = x + (P->nxge - P->nxgs + 1) * delx;
+                    else if (ipos >= P->nxge + 1)
+                        UP(1, ii, j, isp) = x - (P->nxge - P->nxgs + 1) * delx;
+                }
+            fesetround(save);
+        }
     }
-    fesetround(save);
 }
 
 /* boundary_periodic.f90:99-248, single-thread semantics.  The reference sizes its exchange

@@ -75,6 +75,8 @@ SIGNATURES = {
     "wm_sim_sync": [_P],
     "wm_sim_get_work": [_P, _P, _P],
     "wm_sim_set_work": [_P, _P],
+    "wm_sim_step_timed": [_P, _I, ctypes.POINTER(_D)],
+    "wm_set_device": [_I],
     "wm_host_register": [_P, ctypes.c_size_t],
     "wm_host_unregister": [_P],
 }

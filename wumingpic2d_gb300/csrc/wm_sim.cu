@@ -575,6 +575,30 @@ int wm_sim_set_work(wm_sim *s, const double *df)
     return WM_OK;
 }
 
+int wm_sim_step_timed(wm_sim *s, int nsteps, double *ms)
+{
+    if (!s || !s->loaded || !ms) return WM_ERR_BAD_ARG;
+    cudaEvent_t e0, e1;
+    WM_CUDA(cudaEventCreate(&e0));
+    WM_CUDA(cudaEventCreate(&e1));
+    WM_CUDA(cudaEventRecord(e0, s->st));
+    const int st = wm_sim_step(s, nsteps);
+    WM_CUDA(cudaEventRecord(e1, s->st));
+    WM_CUDA(cudaEventSynchronize(e1));
+    float f = 0.f;
+    WM_CUDA(cudaEventElapsedTime(&f, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = f;
+    return st;
+}
+
+int wm_set_device(int device)
+{
+    WM_CUDA(cudaSetDevice(device));
+    return WM_OK;
+}
+
 int wm_host_register(void *ptr, size_t bytes)
 {
     WM_CUDA(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault));

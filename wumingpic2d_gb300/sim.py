@@ -57,6 +57,12 @@ class Simulation:
         check(lib().wm_sim_step_host(self._h, up.ctypes.data, uf.ctypes.data, np2.ctypes.data, cumcnt.ctypes.data,
                                      int(nsteps)), "wm_sim_step_host")
 
+    def step_timed(self, nsteps: int) -> float:
+        """Run nsteps steps; return their GPU time in ms (CUDA events on the simulation stream)."""
+        ms = ctypes.c_double()
+        check(lib().wm_sim_step_timed(self._h, int(nsteps), ctypes.byref(ms)), "wm_sim_step_timed")
+        return ms.value
+
     def sync(self) -> None:
         check(lib().wm_sim_sync(self._h), "wm_sim_sync")
 
@@ -122,6 +128,10 @@ class Simulation:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def set_device(device: int) -> None:
+    check(lib().wm_set_device(int(device)), "wm_set_device")
 
 
 def pin(a: np.ndarray) -> None:
