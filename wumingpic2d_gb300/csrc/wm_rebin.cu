@@ -53,6 +53,9 @@ __global__ void k_wrap_classify(WmGeom g, double delx, PV v, const int *__restri
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     const double xlen = __dmul_rd((double)(g.nxge - g.nxgs + 1), delx);
     const double ylen = __dmul_rd((double)(g.nyge - g.nygs + 1), delx);
+    // x / 1.0 is exact in every rounding mode, so with unit cells the FP64 division (a long
+    // software sequence on this GPU) is skipped without changing any result.
+    const bool unit = (delx == 1.0);
     unsigned bad = 0;
     for (int sb = warp_global * 32; sb < n; sb += nwarps * 32) {
         const int s = sb + lane;
@@ -62,7 +65,7 @@ __global__ void k_wrap_classify(WmGeom g, double delx, PV v, const int *__restri
             const long long p = v.idx(row, s);
             double x = v.X(p);
             if (mode & 1) {  // boundary_periodic.f90:82-88, rounding mode downward
-                const int ipos = (int)__ddiv_rd(x, delx);
+                const int ipos = unit ? (int)x : (int)__ddiv_rd(x, delx);
                 if (ipos < g.nxgs) {
                     x = __dadd_rd(x, xlen);
                     v.X(p) = x;
@@ -74,7 +77,7 @@ __global__ void k_wrap_classify(WmGeom g, double delx, PV v, const int *__restri
             int kr = jr;
             if (mode & 2) {  // boundary_periodic.f90:147-165
                 const double y = v.Y(p);
-                const int jpos = (int)__ddiv_rd(y, delx);
+                const int jpos = unit ? (int)y : (int)__ddiv_rd(y, delx);
                 unsigned char d = 0;
                 if (jpos != j) {
                     if (jpos <= g.nygs - 1) v.Y(p) = __dadd_rd(y, ylen);
