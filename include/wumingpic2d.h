@@ -171,6 +171,25 @@ int wm_set_device(int device);
 int wm_sim_get_work(wm_sim *s, double *df, double *uj);
 int wm_sim_set_work(wm_sim *s, const double *df);
 
+/* ------------------------------------------------- deposit without allocation
+ * No counterpart in the reference: an extra entry point for callers that cannot call cudaMalloc,
+ * such as an application that gives this library GPU memory from its own pool and allows no
+ * allocation (and the device synchronisation that comes with it) after start-up.
+ *
+ * The current deposit of field__fdtd_i -- ele_cur (common/field.f90:189-316) followed by the
+ * periodic current fold boundary_periodic__curre (common/boundary_periodic.f90:357-508) -- on
+ * caller-owned device buffers in the reference layout: up, gp (6, np, ny, nsp), cumcnt
+ * (nx+1, ny, nsp) in, uj (3, nx+4, ny+4) out; q (nsp values) is a host array.  Its scratch is a
+ * fixed static device array inside this library, so it allocates nothing: at most 65536 interior
+ * cells (nx*ny; more returns WM_ERR_BAD_ARG), 39.3 MB of device memory held by every GPU that
+ * loads the library until exit.  All calls share that scratch, so calls that overlap on the GPU
+ * race; the first call on a device looks the scratch up (cudaGetSymbolAddress) and should come
+ * before any stream capture.  stream: a cudaStream_t, or NULL for the default stream; the call
+ * returns after the work on it has finished. */
+int wm_deposit_current_noalloc(const double *up, const double *gp, const int *cumcnt, double *uj, int ndim, int np, int nsp,
+                               int nxgs, int nxge, int nygs, int nyge, double delx, double delt, double c, const double *q,
+                               void *stream);
+
 /* Page-lock (pin) a host buffer so that copies from and to it run at full link speed. */
 int wm_host_register(void *ptr, size_t bytes);
 int wm_host_unregister(void *ptr);

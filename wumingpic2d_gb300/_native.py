@@ -77,6 +77,7 @@ SIGNATURES = {
     "wm_sim_set_work": [_P, _P],
     "wm_sim_step_timed": [_P, _I, ctypes.POINTER(_D)],
     "wm_set_device": [_I],
+    "wm_deposit_current_noalloc": [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _P, _P],
     "wm_host_register": [_P, ctypes.c_size_t],
     "wm_host_unregister": [_P],
 }
