@@ -9,7 +9,9 @@ boundaries + per-cell counting sort (proj/weibel/app.f90:102-107).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-value    particle-updates/s with the state resident in HBM, K steps timed with CUDA events.
+value    particle-updates/s of the mixed-precision path (FP32 particles, FP64 fields and CG) with
+         the state resident in HBM, K steps timed with CUDA events; the FP64 path is timed the same
+         way and reported under "fp64_path".
 e2e      the same metric through the host-buffer entry point (wm_sim_step_host): every step
          copies the reference-layout state in from pinned host memory and back out.
 roofline the dominant particle kernel's algorithmic bytes per launch / its event time.
@@ -48,7 +50,8 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    p.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"],
+                   help="both: the mixed path is the headline value, the FP64 path is timed beside it")
     p.add_argument("--nx", type=int, default=2048)
     p.add_argument("--ny", type=int, default=2048)
     p.add_argument("--ppc", type=int, default=64)
@@ -196,19 +199,26 @@ def cpu_sample(args, steps: int):
 
 
 # ---------------------------------------------------------------------- GB300 arm
-def run_gpu(args, dist: Dist):
-    from wumingpic2d_gb300.sim import Simulation, pin, set_device, unpin
+def make_state(args, dist: Dist):
     from wumingpic2d_gb300.weibel import WeibelConfig, weibel_particles
 
-    set_device(dist.local)
     cfg = WeibelConfig(nx=args.nx, ny=args.ny, ppc=args.ppc, seed=args.seed + dist.rank, slack=1.1)
-    d = cfg.dims()
-    t_init = time.perf_counter()
+    t0 = time.perf_counter()
     up0, np2 = weibel_particles(cfg)
+    return cfg, up0, np2, time.perf_counter() - t0
+
+
+def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
+    from wumingpic2d_gb300.sim import Simulation, pin, set_device, unpin
+
+    set_device(dist.local)
+    cfg, up0, np2, t_init = state
+    d = cfg.dims()
     uf = d.alloc_uf()
-    sim = Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision=args.precision)
+    t0 = time.perf_counter()
+    sim = Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision=precision)
     sim.load(up0, uf, np2)
-    t_init = time.perf_counter() - t_init
+    t_init += time.perf_counter() - t0
     ntot, dev_bytes = sim.info()
     sim.step(args.warmup)
     sim.set_timing(True)
@@ -229,9 +239,8 @@ def run_gpu(args, dist: Dist):
 
     # e2e through the host-buffer entry point, pinned host state
     e2e = None
-    if not args.no_e2e:
-        up_h, uf_h, np2_h, cc_h = sim.store(up=up0)
-        del up0
+    if do_e2e:
+        up_h, uf_h, np2_h, cc_h = sim.store(up=d.alloc_up())
         pin(up_h)
         pin(uf_h)
         maxc = int(np2_h.max())
@@ -248,9 +257,18 @@ def run_gpu(args, dist: Dist):
                "path": "wm_sim_step_host: reference-layout host arrays in and out every step (pinned)"}
         unpin(up_h)
         unpin(uf_h)
+        del up_h
     sim.close()
     return dict(ntot=ntot, ms=ms_max, value=value, launches=launches, ktimes=ktimes, iters=iters, clocks=clk, e2e=e2e,
-                dev_bytes=dev_bytes, t_init=t_init, d=d, cfg=cfg)
+                dev_bytes=dev_bytes, t_init=t_init, d=d, cfg=cfg, precision=precision)
+
+
+# Algorithmic bytes per particle of the particle kernels.  FP64: 8 B per component (push reads and
+# writes x, y, u; the deposit reads old x, y and new x, y, u; the sort moves 6 components).  Mixed:
+# the fused push+deposit reads and writes 5 FP32 components and writes the 5-byte rebin key and
+# direction; the sort moves 5 FP32 components and the i64 pid.
+ALGO_BYTES = {"fp64": {"push": 80, "deposit": 56, "sort_move": 96},
+              "mixed": {"push_deposit": 45, "sort_move": 56}}
 
 
 def roofline(res, args):
@@ -258,15 +276,14 @@ def roofline(res, args):
     kt = res["ktimes"]
     steps = args.steps
     ntot = res["ntot"]
-    # algorithmic bytes per particle of the particle kernels (FP64 state: 8 B per component)
-    algo = {"push": 80, "deposit": 56, "sort_move": 96}
+    algo = ALGO_BYTES[res["precision"]]
     cand = {k: v for k, v in kt.items() if k in algo}
     if not cand:
         return None
     name = max(cand, key=cand.get)
     t = cand[name] / steps / 1e3
     achieved = algo[name] * ntot / t / 1e9
-    tr = ncu_traffic().get(f"{args.precision}:{name}")
+    tr = ncu_traffic().get(f"{res['precision']}:{name}")
     return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": (tr * ntot if tr else None), "bytes_per_particle_algorithmic": algo[name],
@@ -294,7 +311,12 @@ def main():
         dist.close()
         return
 
-    res = run_gpu(args, dist)
+    state = make_state(args, dist)
+    head = "mixed" if args.precision in ("both", "mixed") else "fp64"
+    res = run_gpu(args, dist, head, state, do_e2e=not args.no_e2e)
+    other = None
+    if args.precision == "both":
+        other = run_gpu(args, dist, "fp64", state, do_e2e=False)
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
         v, cores, sample = cpu_sample(args, args.cpu_steps)
@@ -305,10 +327,10 @@ def main():
         line = {
             "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+            "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32 particles + f64 fields",
             "data": "synthetic (seeded Philox Weibel beams)",
             "config": {"workload": workload, "nx": d.nx, "ny": d.ny, "ppc": args.ppc, "particles": res["ntot"],
-                       "precision": args.precision, "parallelism": f"replicas x{dist.world}",
+                       "precision": head, "parallelism": f"replicas x{dist.world}",
                        "l2": f"inputs larger than L2 ({res['ntot'] * 48 / 1e9:.1f} GB of particles vs 129 MB)",
                        "cg_iters_last_step": res["iters"], "cg_tol": 1e-6},
             "roofline": roofline(res, args),
@@ -320,6 +342,13 @@ def main():
             "device_bytes": res["dev_bytes"],
             "setup_s": round(res["t_init"], 1),
         }
+        if other is not None:
+            line["fp64_path"] = {"value": other["value"], "unit": UNIT, "ms_per_step": other["ms"] / args.steps,
+                                 "speedup_of_mixed": res["value"] / other["value"],
+                                 "cg_iters_last_step": other["iters"],
+                                 "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in other["ktimes"].items()},
+                                 "roofline": roofline(other, args), "gpu_launches": other["launches"],
+                                 "clocks": other["clocks"]}
         print(json.dumps(line), flush=True)
     dist.close()
 

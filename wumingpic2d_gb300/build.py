@@ -75,7 +75,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_verbose: bool = Fals
         raise RuntimeError("nvcc failed for: " + ", ".join(failed))
     if force or jobs or _stale(LIB, objs):
         tmp = LIB.with_suffix(f".so.tmp{os.getpid()}")
-        cmd = [cc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+        cmd = [cc, *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", str(tmp), *map(str, objs), "-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)

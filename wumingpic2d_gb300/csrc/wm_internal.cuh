@@ -59,6 +59,22 @@ struct AoSView {
     __device__ __forceinline__ void setpid(long long p, long long v) const { a[6 * p + 5] = __longlong_as_double(v); }
 };
 
+// Mixed-precision particles: FP32 offsets (dx, dy) in [0, 1) inside the particle's cell, FP32
+// momenta, i64 pid.  The cell itself is not stored: rows are cell-sorted and cumcnt gives it.
+struct MixedView {
+    float *x, *y, *ux, *uy, *uz;  // x, y hold the in-cell offsets
+    long long *pid;
+    const long long *rowbase;
+    __device__ __forceinline__ long long idx(int row, int s0) const { return rowbase[row] + s0; }
+    __device__ __forceinline__ float &X(long long p) const { return x[p]; }
+    __device__ __forceinline__ float &Y(long long p) const { return y[p]; }
+    __device__ __forceinline__ float &UX(long long p) const { return ux[p]; }
+    __device__ __forceinline__ float &UY(long long p) const { return uy[p]; }
+    __device__ __forceinline__ float &UZ(long long p) const { return uz[p]; }
+    __device__ __forceinline__ long long getpid(long long p) const { return pid[p]; }
+    __device__ __forceinline__ void setpid(long long p, long long v) const { pid[p] = v; }
+};
+
 template <class V>
 __device__ __forceinline__ void copy_particle(const V &dst, long long pd, const V &src, long long ps)
 {

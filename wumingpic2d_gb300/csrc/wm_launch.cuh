@@ -63,3 +63,13 @@ int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<
                    int *iters, int cg_batch, cudaStream_t st, wm_mark_fn mark, void *mctx, long long *launches);
 int wm_launch_energy_fields(const WmGeom &g, FView<6, false> uf, double *partial, int nblocks, cudaStream_t st);
 int wm_launch_sum_partials(const double *partial, int nparts, int nsets, double *out, cudaStream_t st);
+
+// wm_mixed.cu
+int wm_mixed_ntiles(const WmGeom &g);
+size_t wm_mixed_jtile_floats(const WmGeom &g);
+int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, FView<6, false> uf,
+                                 const int *cumcnt, const WmRebinScratch &sc, float *jtile, cudaStream_t st);
+int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> uj, cudaStream_t st);
+int wm_launch_mixed_unpack(const WmGeom &g, const double *stage, int pitch, const int *np2, MixedView dst, const WmRebinScratch &sc,
+                           cudaStream_t st);
+int wm_launch_mixed_pack(const WmGeom &g, MixedView src, const int *np2, const int *cumcnt, int pitch, double *stage, cudaStream_t st);

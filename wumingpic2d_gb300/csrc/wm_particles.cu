@@ -429,6 +429,8 @@ template int wm_launch_push<SoAView, FView<6, false>>(const WmGeom &, const WmCo
                                                      const int *, int, int, cudaStream_t);
 template int wm_launch_push<AoSView, FView<6, true>>(const WmGeom &, const WmConst &, AoSView, AoSView, FView<6, true>,
                                                     const int *, int, int, cudaStream_t);
+template int wm_launch_push<AoSView, FView<6, false>>(const WmGeom &, const WmConst &, AoSView, AoSView, FView<6, false>,
+                                                     const int *, int, int, cudaStream_t);
 template int wm_launch_deposit_cells<SoAView>(const WmGeom &, const WmConst &, SoAView, SoAView, const int *, double *,
                                               unsigned *, cudaStream_t);
 template int wm_launch_deposit_cells<AoSView>(const WmGeom &, const WmConst &, AoSView, AoSView, const int *, double *,
@@ -441,3 +443,5 @@ template int wm_launch_energy_particles<SoAView>(const WmGeom &, const WmConst &
                                                  cudaStream_t);
 template int wm_launch_energy_particles<AoSView>(const WmGeom &, const WmConst &, AoSView, const int *, double *, int,
                                                  cudaStream_t);
+template int wm_launch_energy_particles<MixedView>(const WmGeom &, const WmConst &, MixedView, const int *, double *, int,
+                                                   cudaStream_t);

@@ -568,4 +568,5 @@ int wm_launch_sort_move(const WmGeom &g, PV src, PV dst, const int *src_np2, int
                                          cudaStream_t);
 WM_INST(SoAView)
 WM_INST(AoSView)
+WM_INST(MixedView)
 #undef WM_INST

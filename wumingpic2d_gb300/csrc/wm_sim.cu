@@ -68,7 +68,7 @@ struct wm_sim {
     long long cap_req = 0, cap = 0, ntot = 0;
     cudaStream_t st = nullptr;
     DevBuf A[6], B[6];
-    DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out;
+    DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out, jtile, stage2;
     int cur = 0;  // index of the current rowbase/np2
     // field and rebin work
     DevBuf f_uf, f_uj, f_df, f_pj, f_b, f_r, f_p, f_ap, f_partial, f_ticket, f_scal;
@@ -94,6 +94,19 @@ struct wm_sim {
         v.ux = S[2].as<double>();
         v.uy = S[3].as<double>();
         v.uz = S[4].as<double>();
+        v.pid = S[5].as<long long>();
+        v.rowbase = rowbase[rb].as<long long>();
+        return v;
+    }
+    bool mixed() const { return precision == WM_PREC_MIXED; }
+    MixedView mview(DevBuf *S, int rb) const
+    {
+        MixedView v;
+        v.x = S[0].as<float>();
+        v.y = S[1].as<float>();
+        v.ux = S[2].as<float>();
+        v.uy = S[3].as<float>();
+        v.uz = S[4].as<float>();
         v.pid = S[5].as<long long>();
         v.rowbase = rowbase[rb].as<long long>();
         return v;
@@ -150,10 +163,12 @@ struct wm_sim {
     {
         const size_t nf = (size_t)g.nxw * g.nyw, nc = (size_t)g.nx * g.ny;
         cap = capacity;
-        for (int c = 0; c < 6; ++c) {
-            WM_TRY(A[c].ensure(8 * (size_t)cap));
-            WM_TRY(B[c].ensure(8 * (size_t)cap));
+        for (int c = 0; c < 6; ++c) {  // mixed: five FP32 components and the i64 pid
+            const size_t esz = (mixed() && c < 5) ? 4 : 8;
+            WM_TRY(A[c].ensure(esz * (size_t)cap));
+            WM_TRY(B[c].ensure(esz * (size_t)cap));
         }
+        if (mixed()) WM_TRY(jtile.ensure(sizeof(float) * wm_mixed_jtile_floats(g)));
         for (int c = 0; c < 2; ++c) {
             WM_TRY(rowbase[c].ensure(sizeof(long long) * (g.nrows + 1)));
             WM_TRY(np2[c].ensure(sizeof(int) * g.nrows));
@@ -190,7 +205,7 @@ struct wm_sim {
     {
         size_t t = 0;
         for (int c = 0; c < 6; ++c) t += A[c].bytes + B[c].bytes;
-        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &f_uf, &f_uj, &f_df, &f_pj,
+        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &f_uf, &f_uj, &f_df, &f_pj,
                                 &f_b, &f_r, &f_p, &f_ap, &f_partial, &rb_dir, &rb_ord, &rb_P, &rb_key, &rb_holes, &rb_nup,
                                 &rb_ndown, &rb_cellcnt, &rb_pairs})
             t += b->bytes;
@@ -204,7 +219,7 @@ struct wm_sim {
             A[c].release();
             B[c].release();
         }
-        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out,
+        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &stage2,
                           &f_uf, &f_uj, &f_df, &f_pj, &f_b, &f_r, &f_p, &f_ap, &f_partial, &f_ticket, &f_scal, &rb_dir, &rb_ord,
                           &rb_P, &rb_key, &rb_holes, &rb_nup, &rb_ndown, &rb_cellcnt, &rb_pairs, &rb_status})
             b->release();
@@ -238,9 +253,15 @@ struct wm_sim {
                                   g.nrows, cudaMemcpyHostToDevice, st));
         WM_CUDA(cudaMemcpyAsync(np2[cur].p, np2_h, sizeof(int) * g.nrows, cudaMemcpyHostToDevice, st));
         WM_TRY(wm_launch_rowbase(g.nrows, np2[cur].as<int>(), rowbase[cur].as<long long>(), st));
-        dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
-        k_unpack<<<grid, 256, 0, st>>>(g, stage.as<double>(), maxc, np2[cur].as<int>(), view(S, cur));
-        WM_TRY(wm_check_launch("k_unpack"));
+        if (mixed()) {  // offsets against int(x) and the row; also the load-sort keys and counts
+            WmRebinScratch sc = scratch();
+            WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
+            WM_TRY(wm_launch_mixed_unpack(g, stage.as<double>(), maxc, np2[cur].as<int>(), mview(S, cur), sc, st));
+        } else {
+            dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
+            k_unpack<<<grid, 256, 0, st>>>(g, stage.as<double>(), maxc, np2[cur].as<int>(), view(S, cur));
+            WM_TRY(wm_check_launch("k_unpack"));
+        }
         max_row = maxc;
         return WM_OK;
     }
@@ -257,6 +278,16 @@ struct wm_sim {
     int sort_B_into_A()
     {
         WmRebinScratch sc = scratch();
+        if (mixed()) {  // keys and counts came from the unpack
+            MixedView vb = mview(B, cur);
+            WM_TRY(wm_launch_slot_as_P(g, vb, np2[cur].as<int>(), max_row, sc, st));
+            WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
+            WM_TRY(check_status());
+            WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
+            WM_TRY(wm_launch_sort_move(g, vb, mview(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
+            cur = 1 - cur;
+            return WM_OK;
+        }
         WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
         SoAView vb = view(B, cur);
         WM_TRY(wm_launch_wrap_classify(g, k.delx, vb, np2[cur].as<int>(), max_row, 8, sc, st));
@@ -269,8 +300,40 @@ struct wm_sim {
         return WM_OK;
     }
 
+    // The mixed-precision step: FP32 push + deposit with the wrap, keys and counts fused in one
+    // kernel; FP64 current fold, field solve and the same particle_y / sort permutation.
+    int step_mixed()
+    {
+        WmRebinScratch sc = scratch();
+        long long nl = 0;
+        WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
+        mark("start");
+        MixedView va = mview(A, cur), vb = mview(B, cur);
+        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, uf(), cumcnt.as<int>(), sc, jtile.as<float>(), st));
+        ++nl;
+        mark("push_deposit");
+        WM_TRY(wm_launch_mixed_jfold(g, jtile.as<float>(), uj(), st));
+        ++nl;
+        mark("deposit");
+        WmFieldWork w = work();
+        const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl);
+        if (s != WM_OK) return s;
+        WM_TRY(wm_launch_place(g, vb, np2[cur].as<int>(), max_row, sc, nullptr, st));
+        WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
+        WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
+        nl += 4;
+        mark("place_scan");
+        WM_TRY(wm_launch_sort_move(g, vb, mview(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
+        nl += 2;
+        mark("sort_move");
+        cur = 1 - cur;
+        launches += nl;
+        return check_status();
+    }
+
     int step_once()
     {
+        if (mixed()) return step_mixed();
         WmRebinScratch sc = scratch();
         long long nl = 0;
         WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
@@ -310,7 +373,6 @@ int wm_sim_create(const wm_sim_config *cfg, wm_sim **out)
     if (!cfg || !out) return WM_ERR_BAD_ARG;
     *out = nullptr;
     if (cfg->precision != WM_PREC_FP64 && cfg->precision != WM_PREC_MIXED) return WM_ERR_BAD_ARG;
-    if (cfg->precision == WM_PREC_MIXED) return WM_ERR_UNSUPPORTED;
     if (cfg->nsp < 1 || cfg->nsp > WM_MAX_SP || cfg->nx < 4 || cfg->ny < 4 || cfg->np < 1) return WM_ERR_BAD_ARG;
     if (cfg->cg_itemax < 1 || !(cfg->cg_err > 0)) return WM_ERR_BAD_ARG;
     wm_sim *s = new wm_sim();
@@ -410,8 +472,13 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
     if (up) {
         WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
         dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
-        k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), maxc, s->stage.as<double>());
-        WM_TRY(wm_check_launch("k_pack"));
+        if (s->mixed()) {
+            WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), maxc,
+                                        s->stage.as<double>(), s->st));
+        } else {
+            k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), maxc, s->stage.as<double>());
+            WM_TRY(wm_check_launch("k_pack"));
+        }
         WM_CUDA(cudaMemcpy2DAsync(up, sizeof(double) * 6 * g.np, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * maxc,
                                   g.nrows, cudaMemcpyDeviceToHost, s->st));
     }
@@ -468,7 +535,10 @@ int wm_sim_energy(wm_sim *s, double *out)
     const WmGeom &g = s->g;
     const int nb = 304;
     double *part = s->energy_partial.as<double>();
-    WM_TRY(wm_launch_energy_particles(g, s->k, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), part, nb, s->st));
+    if (s->mixed())
+        WM_TRY(wm_launch_energy_particles(g, s->k, s->mview(s->A, s->cur), s->np2[s->cur].as<int>(), part, nb, s->st));
+    else
+        WM_TRY(wm_launch_energy_particles(g, s->k, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), part, nb, s->st));
     WM_TRY(wm_launch_energy_fields(g, s->uf(), part + (size_t)nb * g.nsp, nb, s->st));
     WM_TRY(wm_launch_sum_partials(part, nb, g.nsp + 2, s->energy_out.as<double>(), s->st));
     std::vector<double> tmp(g.nsp + 2);
@@ -485,9 +555,30 @@ int wm_sim_moments(wm_sim *s, double *mom)
 {
     if (!s || !s->loaded) return WM_ERR_NOT_INIT;
     const WmGeom &g = s->g;
+    const size_t nm = (size_t)7 * (g.nx + 2) * (g.ny + 2) * g.nsp;
+    if (s->mixed()) {
+        // moment steps are rare: expand the mixed state to FP64 rows (pitch = largest row) and run
+        // the FP64 half-step push and moment deposit on that copy
+        std::vector<int> cnt(g.nrows);
+        WM_CUDA(cudaMemcpyAsync(cnt.data(), s->np2[s->cur].p, sizeof(int) * g.nrows, cudaMemcpyDeviceToHost, s->st));
+        WM_CUDA(cudaStreamSynchronize(s->st));
+        const int pitch = std::max(1, *std::max_element(cnt.begin(), cnt.end()));
+        const size_t nstage = (size_t)6 * pitch * g.nrows;
+        WM_TRY(s->uf_aos.ensure(sizeof(double) * nm));
+        WM_TRY(s->stage.ensure(sizeof(double) * nstage));
+        WM_TRY(s->stage2.ensure(sizeof(double) * nstage));
+        WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), pitch,
+                                    s->stage.as<double>(), s->st));
+        AoSView va{s->stage.as<double>(), pitch}, vb{s->stage2.as<double>(), pitch};
+        WM_TRY(wm_launch_push(g, s->k, va, vb, s->uf(), s->cumcnt.as<int>(), 1, 0, s->st));
+        WM_TRY(wm_launch_mom_nvt(g, s->k, vb, s->np2[s->cur].as<int>(), s->uf_aos.as<double>(), pitch, s->st));
+        WM_TRY(wm_launch_mom_bc(g, s->uf_aos.as<double>(), s->st));
+        WM_CUDA(cudaMemcpyAsync(mom, s->uf_aos.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s->st));
+        WM_CUDA(cudaStreamSynchronize(s->st));
+        return WM_OK;
+    }
     SoAView va = s->view(s->A, s->cur), vb = s->view(s->B, s->cur);
     WM_TRY(wm_launch_push(g, s->k, va, vb, s->uf(), s->cumcnt.as<int>(), 1, 0, s->st));
-    const size_t nm = (size_t)7 * (g.nx + 2) * (g.ny + 2) * g.nsp;
     WM_TRY(s->stage.ensure(sizeof(double) * nm));
     WM_TRY(wm_launch_mom_nvt(g, s->k, vb, s->np2[s->cur].as<int>(), s->stage.as<double>(), s->max_row, s->st));
     WM_TRY(wm_launch_mom_bc(g, s->stage.as<double>(), s->st));
