@@ -295,7 +295,6 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
             b.ux[p] = S.buf[2][sidx];
             b.uy[p] = S.buf[3][sidx];
             b.uz[p] = S.buf[4][sidx];
-            b.pid[p] = a.pid[p];
             key[p] = S.keyb[sidx];
             dir[p] = S.dirb[sidx];
         }

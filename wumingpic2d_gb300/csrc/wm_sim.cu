@@ -99,7 +99,10 @@ struct wm_sim {
         return v;
     }
     bool mixed() const { return precision == WM_PREC_MIXED; }
-    MixedView mview(DevBuf *S, int rb) const
+    // Mixed path: the push does not touch the ids; the sort gathers them from the id buffer of the
+    // old order (pid_cur) into the other one, so the two id buffers alternate every step.
+    int pid_cur = 0;  // 0: A[5] holds the ids of the current order, 1: B[5]
+    MixedView mview(DevBuf *S, int rb, int pidw = -1) const
     {
         MixedView v;
         v.x = S[0].as<float>();
@@ -107,7 +110,7 @@ struct wm_sim {
         v.ux = S[2].as<float>();
         v.uy = S[3].as<float>();
         v.uz = S[4].as<float>();
-        v.pid = S[5].as<long long>();
+        v.pid = (pidw < 0 ? S[5] : (pidw == 0 ? A[5] : B[5])).as<long long>();
         v.rowbase = rowbase[rb].as<long long>();
         return v;
     }
@@ -286,6 +289,7 @@ struct wm_sim {
             WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
             WM_TRY(wm_launch_sort_move(g, vb, mview(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
             cur = 1 - cur;
+            pid_cur = 0;
             return WM_OK;
         }
         WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
@@ -323,10 +327,12 @@ struct wm_sim {
         WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
         nl += 4;
         mark("place_scan");
-        WM_TRY(wm_launch_sort_move(g, vb, mview(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
+        WM_TRY(wm_launch_sort_move(g, mview(B, cur, pid_cur), mview(A, 1 - cur, 1 - pid_cur), np2[cur].as<int>(), max_row,
+                                   cumcnt.as<int>(), sc, st));
         nl += 2;
         mark("sort_move");
         cur = 1 - cur;
+        pid_cur = 1 - pid_cur;
         launches += nl;
         return check_status();
     }
@@ -438,6 +444,7 @@ static int sim_load_common(wm_sim *s, const double *up, const double *uf, const 
     s->ntot = ntot;
     if (cumcnt_h) {  // already sorted: upload straight into A
         WM_TRY(s->upload_particles(up, np2_h, s->A));
+        s->pid_cur = 0;
         WM_CUDA(cudaMemcpyAsync(s->cumcnt.p, cumcnt_h, sizeof(int) * (size_t)(g.nx + 1) * g.nrows, cudaMemcpyHostToDevice, s->st));
     } else {
         WM_TRY(s->upload_particles(up, np2_h, s->B));
@@ -473,7 +480,7 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
         WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
         dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
         if (s->mixed()) {
-            WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), maxc,
+            WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur, s->pid_cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), maxc,
                                         s->stage.as<double>(), s->st));
         } else {
             k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), maxc, s->stage.as<double>());
@@ -567,7 +574,7 @@ int wm_sim_moments(wm_sim *s, double *mom)
         WM_TRY(s->uf_aos.ensure(sizeof(double) * nm));
         WM_TRY(s->stage.ensure(sizeof(double) * nstage));
         WM_TRY(s->stage2.ensure(sizeof(double) * nstage));
-        WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), pitch,
+        WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur, s->pid_cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), pitch,
                                     s->stage.as<double>(), s->st));
         AoSView va{s->stage.as<double>(), pitch}, vb{s->stage2.as<double>(), pitch};
         WM_TRY(wm_launch_push(g, s->k, va, vb, s->uf(), s->cumcnt.as<int>(), 1, 0, s->st));
