@@ -1,41 +1,32 @@
 // wm_mixed.cu -- the mixed-precision particle kernels (FP32 push and deposit) for sm_103a.
 //
 // Particles carry their position as (cell, FP32 offset in [0,1)) -- the cell is implicit in the
-// cell-sorted rows -- and FP32 momenta.  k_mixed_push_deposit does, for one (species, row, 64-cell
+// cell-sorted rows -- and FP32 momenta.  k_mixed_push_deposit does, for one (species, row, 32-cell
 // tile): the cell-centred fields of particle.f90:68-81 staged in shared memory as FP32, the
 // Buneman-Boris push of particle.f90:96-161 in FP32, the Esirkepov deposit of field.f90:224-298 in
 // FP32, the periodic wrap of boundary_periodic.f90:61-96 and :143-165 as integer cell arithmetic,
-// and the destination cell key and row direction the rebin needs.  Particles are staged through
-// shared memory in chunks so that global loads and stores are coalesced while each thread walks
-// 8 consecutive particles; a thread adds its particles' 5x5x3 currents into registers while they
-// stay in one cell and flushes them to the tile's FP32 current accumulator (shared-memory atomics)
-// when the cell changes.  Tile currents go to a per-tile buffer; k_mixed_jfold adds them into the
-// FP64 global J node by node in a fixed order, so the result is deterministic.
+// and the destination cell key and row direction the rebin needs.  Eight lanes share a cell and
+// read its particles in 32-byte runs straight from global memory; each lane keeps the cell's 5x5x3
+// partial currents in registers (the cell's particles all deposit on the same 5x5 nodes), the
+// eight lanes add theirs with shuffles, and the tile's node currents are summed from the per-cell
+// partials in a fixed order.  Tile currents go to a per-tile buffer; k_mixed_jfold adds them into
+// the FP64 global J node by node in a fixed order, so the result is deterministic and no atomics
+// touch the currents.
 #include <algorithm>
 
 #include "wm_launch.cuh"
 
 namespace {
 
-constexpr int MX_TW = 64;  // cells per tile
-constexpr int MX_THREADS = 256;
-constexpr int MX_PER = 8;  // consecutive particles per thread per chunk
-constexpr int MX_CHUNK = MX_THREADS * MX_PER;
-constexpr int MX_PAD = MX_PER + 1;  // padded stride: conflict-free shared-memory access
+constexpr int MX_TW = 32;   // cells per tile (one row, one species)
+constexpr int MX_LPC = 8;   // lanes per cell
+constexpr int MX_THREADS = MX_TW * MX_LPC;
 constexpr int MX_JW = MX_TW + 4;
+constexpr unsigned FULL = 0xffffffffu;
 
 struct MxConst {
     float fac1[WM_MAX_SP], txxx[WM_MAX_SP], fac2[WM_MAX_SP], mqdd[WM_MAX_SP], q[WM_MAX_SP];
     float dt_dx, inv_c2, c2;
-};
-
-struct MxSmem {
-    float tmp[6][3][MX_TW + 2];
-    float jacc[3][5][MX_JW];
-    int cc[MX_TW + 1];
-    float buf[5][MX_THREADS * MX_PAD];
-    int keyb[MX_THREADS * MX_PAD];
-    unsigned char dirb[MX_THREADS * MX_PAD];
 };
 
 __device__ __forceinline__ void shape3(float h, float &a0, float &a1, float &a2)
@@ -45,34 +36,47 @@ __device__ __forceinline__ void shape3(float h, float &a0, float &a1, float &a2)
     a2 = 0.5f * (0.5f + h) * (0.5f + h);
 }
 
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// One CTA per (tile of 32 cells, row, species); 8 lanes per cell read the cell's particles in
+// 32-byte runs straight from global memory.  Each lane keeps the cell's 5x5x3 partial currents in
+// registers; the 8 lanes of a cell add theirs with shuffles, and the tile's node currents are then
+// summed from the per-cell partials in a fixed order (no atomics on the currents).
 __global__ void __launch_bounds__(MX_THREADS, 2)
     k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, FView<6, false> uf, const int *__restrict__ cumcnt,
                          int *__restrict__ key, unsigned char *__restrict__ dir, int *__restrict__ cellcnt,
                          float *__restrict__ jtile, unsigned *status)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    MxSmem &S = *reinterpret_cast<MxSmem *>(smem_raw);
+    __shared__ float tmp[6][3][MX_TW + 2];
+    __shared__ float cellpj[65][MX_TW + 1];
+    __shared__ int cc[MX_TW + 1];
+    __shared__ float spc[5];
     const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
     const int row = isp * g.ny + jr;
-    const int c0 = tile * MX_TW;  // first interior cell of the tile
+    const int c0 = tile * MX_TW;
     const int ncell = min(MX_TW, g.nx - c0);
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, lane = tid & 31;
 
     // fields at cell centres (i+1/2, j+1/2) for cells c0-1 .. c0+ncell and rows jr-1 .. jr+1
     const int tw = ncell + 2;
     for (int e = tid; e < 3 * tw; e += MX_THREADS) {
         const int aa = e % tw, bb = e / tw;
         const int ix = c0 - 1 + aa + 2, iy = jr - 1 + bb + 2;
-        S.tmp[0][bb][aa] = (float)(0.5 * (uf(0, ix, iy) + uf(0, ix, iy + 1)));
-        S.tmp[1][bb][aa] = (float)(0.5 * (uf(1, ix, iy) + uf(1, ix + 1, iy)));
-        S.tmp[2][bb][aa] = (float)(0.25 * (uf(2, ix, iy) + uf(2, ix + 1, iy) + uf(2, ix, iy + 1) + uf(2, ix + 1, iy + 1)));
-        S.tmp[3][bb][aa] = (float)(0.5 * (uf(3, ix, iy) + uf(3, ix + 1, iy)));
-        S.tmp[4][bb][aa] = (float)(0.5 * (uf(4, ix, iy) + uf(4, ix, iy + 1)));
-        S.tmp[5][bb][aa] = (float)uf(5, ix, iy);
+        tmp[0][bb][aa] = (float)(0.5 * (uf(0, ix, iy) + uf(0, ix, iy + 1)));
+        tmp[1][bb][aa] = (float)(0.5 * (uf(1, ix, iy) + uf(1, ix + 1, iy)));
+        tmp[2][bb][aa] = (float)(0.25 * (uf(2, ix, iy) + uf(2, ix + 1, iy) + uf(2, ix, iy + 1) + uf(2, ix + 1, iy + 1)));
+        tmp[3][bb][aa] = (float)(0.5 * (uf(3, ix, iy) + uf(3, ix + 1, iy)));
+        tmp[4][bb][aa] = (float)(0.5 * (uf(4, ix, iy) + uf(4, ix, iy + 1)));
+        tmp[5][bb][aa] = (float)uf(5, ix, iy);
     }
-    for (int e = tid; e < 3 * 5 * MX_JW; e += MX_THREADS) (&S.jacc[0][0][0])[e] = 0.f;
-    __shared__ float spc[5];  // this species' constants (static indices: no local-memory copy)
-    if (tid == 0) {
+    const int *ccrow = cumcnt + (long long)(g.nx + 1) * row;
+    for (int e = tid; e <= ncell; e += MX_THREADS) cc[e] = ccrow[c0 + e];
+    if (tid == 0) {  // this species' constants (static indices: no local-memory copy)
 #pragma unroll
         for (int s = 0; s < WM_MAX_SP; ++s)
             if (s == isp) {
@@ -83,81 +87,43 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
                 spc[4] = kc.q[s];
             }
     }
-    const int *ccrow = cumcnt + (long long)(g.nx + 1) * row;
-    for (int e = tid; e <= ncell; e += MX_THREADS) S.cc[e] = ccrow[c0 + e];
     __syncthreads();
 
     const float fac1 = spc[0], txxx = spc[1], fac2 = spc[2], mqdd = spc[3], qs = spc[4];
-    const int start = S.cc[0], end = S.cc[ncell];
+    const int c = tid / MX_LPC, sub = tid % MX_LPC;
+    const bool has_cell = c < ncell;
+    const int s_beg = has_cell ? cc[c] : 0, s_end = has_cell ? cc[c + 1] : 0;
+    const int nmine = (s_end - s_beg > sub) ? (s_end - s_beg - sub + MX_LPC - 1) / MX_LPC : 0;
+    int nwarp = nmine;  // trip count of the warp: the largest over its lanes
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nwarp = max(nwarp, __shfl_xor_sync(FULL, nwarp, o));
     const long long rbase = a.rowbase[row];
-    unsigned bad = 0;
+    const int cl = has_cell ? c : 0;  // safe index for lanes without a cell
 
-    for (int cbeg = start; cbeg < end; cbeg += MX_CHUNK) {
-        const int nchunk = min(MX_CHUNK, end - cbeg);
-        // coalesced load into the padded per-thread layout
-        for (int e = tid; e < nchunk; e += MX_THREADS) {
-            const long long p = rbase + cbeg + e;
-            const int sidx = (e / MX_PER) * MX_PAD + (e % MX_PER);
-            S.buf[0][sidx] = a.x[p];
-            S.buf[1][sidx] = a.y[p];
-            S.buf[2][sidx] = a.ux[p];
-            S.buf[3][sidx] = a.uy[p];
-            S.buf[4][sidx] = a.uz[p];
+    float ax[5][4], ay[4][5], az[5][5];
+#pragma unroll
+    for (int jp = 0; jp < 5; ++jp)
+#pragma unroll
+        for (int ip = 0; ip < 5; ++ip) {
+            if (ip < 4) ax[jp][ip] = 0.f;
+            if (jp < 4) ay[jp][ip] = 0.f;
+            az[jp][ip] = 0.f;
         }
-        __syncthreads();
-
-        const int q0 = tid * MX_PER;
-        int c = -1;  // cell (within the tile) of the current run
-        float ax[5][4], ay[4][5], az[5][5];
-        int run_key = -1, run_cnt = 0;
-        for (int k = 0; k < MX_PER; ++k) {
-            const int q = q0 + k;
-            if (q >= nchunk) break;
-            const int slot = cbeg + q;
-            int cn = c;
-            if (cn < 0) {  // first particle of the chunk: last cell whose start is <= slot
-                int lo = 0, hi = ncell - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (S.cc[mid] <= slot) lo = mid;
-                    else hi = mid - 1;
-                }
-                cn = lo;
-            } else {
-                while (cn + 1 < ncell && S.cc[cn + 1] <= slot) ++cn;
-            }
-            if (cn != c) {
-                if (c >= 0) {  // flush the finished cell
-#pragma unroll
-                    for (int jp = 0; jp < 5; ++jp)
-#pragma unroll
-                        for (int ip = 0; ip < 5; ++ip) {
-                            if (ip > 0) atomicAdd(&S.jacc[0][jp][c + ip], ax[jp][ip - 1]);
-                            if (jp > 0) atomicAdd(&S.jacc[1][jp][c + ip], ay[jp - 1][ip]);
-                            atomicAdd(&S.jacc[2][jp][c + ip], az[jp][ip]);
-                        }
-                }
-                c = cn;
-#pragma unroll
-                for (int jp = 0; jp < 5; ++jp)
-#pragma unroll
-                    for (int ip = 0; ip < 5; ++ip) {
-                        if (ip < 4) ax[jp][ip] = 0.f;
-                        if (jp < 4) ay[jp][ip] = 0.f;
-                        az[jp][ip] = 0.f;
-                    }
-            }
-            const int sidx = tid * MX_PAD + k;
-            const float dx = S.buf[0][sidx], dy = S.buf[1][sidx];
-            float u1 = S.buf[2][sidx], u2 = S.buf[3][sidx], u3 = S.buf[4][sidx];
-            // gather (TSC weights about the cell centre)
+    unsigned bad = 0;
+    for (int it = 0; it < nwarp; ++it) {
+        const bool valid = it < nmine;
+        int kk = -1;
+        if (valid) {
+            const long long p = rbase + s_beg + sub + (long long)it * MX_LPC;
+            const float dx = a.x[p], dy = a.y[p];
+            float u1 = a.ux[p], u2 = a.uy[p], u3 = a.uz[p];
             float sx0, sx1, sx2, sy0, sy1, sy2;
             shape3(dx - 0.5f, sx0, sx1, sx2);
             shape3(dy - 0.5f, sy0, sy1, sy2);
             float f[6];
 #pragma unroll
             for (int m = 0; m < 6; ++m) {
-                const float *t0 = &S.tmp[m][0][c], *t1 = &S.tmp[m][1][c], *t2 = &S.tmp[m][2][c];
+                const float *t0 = &tmp[m][0][cl], *t1 = &tmp[m][1][cl], *t2 = &tmp[m][2][cl];
                 f[m] = (t0[0] * sx0 + t0[1] * sx1 + t0[2] * sx2) * sy0 + (t1[0] * sx0 + t1[1] * sx1 + t1[2] * sx2) * sy1
                        + (t2[0] * sx0 + t2[1] * sx1 + t2[2] * sx2) * sy2;
             }
@@ -193,42 +159,24 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
             }
             bad |= (incx < -1 || incx > 1 || incy < -1 || incy > 1);
             // Esirkepov: old shape about the old cell, new shape about the new cell shifted by inc
-            float s0x[5], s0y[5], dsx[5], dsy[5];
-            s0x[0] = 0.f;
-            s0x[4] = 0.f;
-            s0y[0] = 0.f;
-            s0y[4] = 0.f;
-            s0x[1] = sx0;
-            s0x[2] = sx1;
-            s0x[3] = sx2;
-            s0y[1] = sy0;
-            s0y[2] = sy1;
-            s0y[3] = sy2;
+            float dsx[5], dsy[5];
+            const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f}, s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
             {
                 float b0, b1, b2;
                 shape3(nx1 - 0.5f, b0, b1, b2);
 #pragma unroll
                 for (int m = 0; m < 5; ++m) {
                     const int o = m - 2 - incx;
-                    const float s1 = (o == -1) ? b0 : (o == 0) ? b1 : (o == 1) ? b2 : 0.f;
-                    dsx[m] = s1 - s0x[m];
+                    dsx[m] = ((o == -1) ? b0 : (o == 0) ? b1 : (o == 1) ? b2 : 0.f) - s0x[m];
                 }
                 shape3(ny1 - 0.5f, b0, b1, b2);
 #pragma unroll
                 for (int m = 0; m < 5; ++m) {
                     const int o = m - 2 - incy;
-                    const float s1 = (o == -1) ? b0 : (o == 0) ? b1 : (o == 1) ? b2 : 0.f;
-                    dsy[m] = s1 - s0y[m];
+                    dsy[m] = ((o == -1) ? b0 : (o == 0) ? b1 : (o == 1) ? b2 : 0.f) - s0y[m];
                 }
             }
             const float qg = qs * u3 * ig;
-            float wy[5], wx[5], z2[5];
-#pragma unroll
-            for (int m = 0; m < 5; ++m) {
-                wy[m] = s0y[m] + 0.5f * dsy[m];
-                wx[m] = s0x[m] + 0.5f * dsx[m];
-                z2[m] = qg * (0.5f * s0y[m] + (1.f / 3.f) * dsy[m]);
-            }
             float cx[4], cy[4];
             cx[0] = dsx[0];
             cy[0] = dsy[0];
@@ -239,73 +187,86 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
             }
 #pragma unroll
             for (int jp = 0; jp < 5; ++jp) {
-                const float fy = mqdd * wy[jp];
+                const float wy = s0y[jp] + 0.5f * dsy[jp];
+                const float fy = mqdd * wy;
 #pragma unroll
                 for (int m = 0; m < 4; ++m) ax[jp][m] = fmaf(fy, cx[m], ax[jp][m]);
+                const float z1 = qg * wy;
+                const float z2 = qg * (0.5f * s0y[jp] + (1.f / 3.f) * dsy[jp]);
+#pragma unroll
+                for (int ip = 0; ip < 5; ++ip) az[jp][ip] = fmaf(s0x[ip], z1, fmaf(dsx[ip], z2, az[jp][ip]));
             }
 #pragma unroll
             for (int ip = 0; ip < 5; ++ip) {
-                const float fx = mqdd * wx[ip];
+                const float fx = mqdd * (s0x[ip] + 0.5f * dsx[ip]);
 #pragma unroll
                 for (int m = 0; m < 4; ++m) ay[m][ip] = fmaf(fx, cy[m], ay[m][ip]);
             }
-#pragma unroll
-            for (int jp = 0; jp < 5; ++jp) {
-                const float z1 = qg * wy[jp];
-#pragma unroll
-                for (int ip = 0; ip < 5; ++ip) az[jp][ip] = fmaf(s0x[ip], z1, fmaf(dsx[ip], z2[jp], az[jp][ip]));
-            }
-            // new state, destination cell (periodic wrap as integer arithmetic) and row direction
-            S.buf[0][sidx] = nx1;
-            S.buf[1][sidx] = ny1;
-            S.buf[2][sidx] = u1;
-            S.buf[3][sidx] = u2;
-            S.buf[4][sidx] = u3;
+            b.x[p] = nx1;
+            b.y[p] = ny1;
+            b.ux[p] = u1;
+            b.uy[p] = u2;
+            b.uz[p] = u3;
             int ci = c0 + c + incx;
             ci = ci < 0 ? ci + g.nx : (ci >= g.nx ? ci - g.nx : ci);
             int kr = jr + incy;
             kr = kr < 0 ? kr + g.ny : (kr >= g.ny ? kr - g.ny : kr);
-            const int kk = (isp * g.ny + kr) * g.nx + ci;
-            S.keyb[sidx] = kk;
-            S.dirb[sidx] = (unsigned char)(incy == 1 ? 1 : (incy == -1 ? 2 : 0));
-            if (kk != run_key) {
-                if (run_cnt) atomicAdd(&cellcnt[run_key], run_cnt);
-                run_key = kk;
-                run_cnt = 0;
-            }
-            ++run_cnt;
+            kk = (isp * g.ny + kr) * g.nx + ci;
+            key[p] = kk;
+            dir[p] = (unsigned char)(incy == 1 ? 1 : (incy == -1 ? 2 : 0));
         }
-        if (run_cnt) atomicAdd(&cellcnt[run_key], run_cnt);
-        if (c >= 0) {
-#pragma unroll
-            for (int jp = 0; jp < 5; ++jp)
-#pragma unroll
-                for (int ip = 0; ip < 5; ++ip) {
-                    if (ip > 0) atomicAdd(&S.jacc[0][jp][c + ip], ax[jp][ip - 1]);
-                    if (jp > 0) atomicAdd(&S.jacc[1][jp][c + ip], ay[jp - 1][ip]);
-                    atomicAdd(&S.jacc[2][jp][c + ip], az[jp][ip]);
-                }
+        // cell counts for the sort, aggregated over the lanes that share a destination
+        const unsigned m = __ballot_sync(FULL, valid);
+        if (valid) {
+            const unsigned peers = __match_any_sync(m, kk);
+            if ((peers & lanemask_lt()) == 0) atomicAdd(&cellcnt[kk], __popc(peers));
         }
-        __syncthreads();
-        for (int e = tid; e < nchunk; e += MX_THREADS) {
-            const long long p = rbase + cbeg + e;
-            const int sidx = (e / MX_PER) * MX_PAD + (e % MX_PER);
-            b.x[p] = S.buf[0][sidx];
-            b.y[p] = S.buf[1][sidx];
-            b.ux[p] = S.buf[2][sidx];
-            b.uy[p] = S.buf[3][sidx];
-            b.uz[p] = S.buf[4][sidx];
-            key[p] = S.keyb[sidx];
-            dir[p] = S.dirb[sidx];
-        }
-        __syncthreads();
     }
     if (bad) atomicOr(status, (unsigned)WMDEV_CELL);
-    // tile currents -> per-tile buffer [isp][jr][tile][3][5][MX_JW]
-    const int ntiles = gridDim.x;
-    float *out = jtile + ((((long long)isp * g.ny + jr) * ntiles + tile) * 3) * 5 * MX_JW;
-    for (int e = tid; e < 3 * 5 * MX_JW; e += MX_THREADS) out[e] = (&S.jacc[0][0][0])[e];
+
+    // the 8 lanes of a cell add their partial currents; lane 0 of the cell keeps the sum
+#pragma unroll
+    for (int jp = 0; jp < 5; ++jp)
+#pragma unroll
+        for (int ip = 0; ip < 5; ++ip) {
+#pragma unroll
+            for (int o = 1; o < MX_LPC; o <<= 1) {
+                if (ip < 4) ax[jp][ip] += __shfl_xor_sync(FULL, ax[jp][ip], o);
+                if (jp < 4) ay[jp][ip] += __shfl_xor_sync(FULL, ay[jp][ip], o);
+                az[jp][ip] += __shfl_xor_sync(FULL, az[jp][ip], o);
+            }
+        }
+    if (sub == 0 && has_cell) {
+#pragma unroll
+        for (int jp = 0; jp < 5; ++jp)
+#pragma unroll
+            for (int ip = 0; ip < 5; ++ip) {
+                if (ip < 4) cellpj[jp * 4 + ip][c] = ax[jp][ip];
+                if (jp < 4) cellpj[20 + jp * 5 + ip][c] = ay[jp][ip];
+                cellpj[40 + jp * 5 + ip][c] = az[jp][ip];
+            }
+    }
+    __syncthreads();
+    // node currents of the tile footprint (5 rows x (32+4) columns), cells in ascending order;
+    // per-tile buffer [isp][jr][tile][3][5][MX_JW]
+    float *out = jtile + ((((long long)isp * g.ny + jr) * gridDim.x + tile) * 3) * 5 * MX_JW;
+    for (int e = tid; e < 3 * 5 * MX_JW; e += MX_THREADS) {
+        const int k = e / (5 * MX_JW), ly = (e / MX_JW) % 5, lx = e % MX_JW;
+        float sum = 0.f;
+        for (int cc2 = max(0, lx - 4); cc2 <= min(ncell - 1, lx); ++cc2) {
+            const int ip = lx - cc2;
+            if (k == 0) {
+                if (ip >= 1) sum += cellpj[ly * 4 + ip - 1][cc2];
+            } else if (k == 1) {
+                if (ly >= 1) sum += cellpj[20 + (ly - 1) * 5 + ip][cc2];
+            } else {
+                sum += cellpj[40 + ly * 5 + ip][cc2];
+            }
+        }
+        out[e] = sum;
+    }
 }
+
 
 // uj(k, ix, iy) over the ghosted grid = sum of the tile currents that cover the node, in the
 // order (species, cell row, tile), accumulated in FP64.
@@ -406,12 +367,6 @@ size_t wm_mixed_jtile_floats(const WmGeom &g) { return (size_t)g.nsp * g.ny * wm
 int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, FView<6, false> uf,
                                  const int *cumcnt, const WmRebinScratch &sc, float *jtile, cudaStream_t st)
 {
-    static bool attr_set = false;
-    const size_t smem = sizeof(MxSmem);
-    if (!attr_set) {
-        WM_CUDA(cudaFuncSetAttribute(k_mixed_push_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr_set = true;
-    }
     MxConst kc;
     for (int s = 0; s < WM_MAX_SP; ++s) {
         const double qm = k.q[s] / k.r[s];
@@ -426,7 +381,7 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
     kc.c2 = (float)(k.c * k.c);
     WM_CUDA(cudaMemsetAsync(sc.cellcnt, 0, sizeof(int) * (size_t)g.nrows * g.nx, st));
     dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
-    k_mixed_push_deposit<<<grid, MX_THREADS, smem, st>>>(g, kc, a, b, uf, cumcnt, sc.key, sc.dir, sc.cellcnt, jtile, sc.status);
+    k_mixed_push_deposit<<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, uf, cumcnt, sc.key, sc.dir, sc.cellcnt, jtile, sc.status);
     return wm_check_launch("k_mixed_push_deposit");
 }
 
