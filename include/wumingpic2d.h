@@ -164,6 +164,16 @@ int wm_sim_sync(wm_sim *s);
 /* wm_sim_step bracketed by CUDA events on the simulation's stream: *ms = GPU time of the
  * nsteps steps (host synchronisations inside the step loop included). */
 int wm_sim_step_timed(wm_sim *s, int nsteps, double *ms);
+/* Learned initial guess for the CG (no reference counterpart; see wm_cnn_* below): params =
+ * the network's FP32 parameters on the HOST, per layer w[9][cout][cin] then b[cout] for the
+ * padded (cin, cout) = (16,48), (48,48) x 4, (48,8): 93560 values.  From the next step on, each
+ * field component's CG starts from the network's dB or the previous step's dB, whichever has the
+ * smaller residual, and runs to the usual tolerance.  params = NULL switches it off.  Needs nx a
+ * multiple of 16 and ny a multiple of 8. */
+int wm_sim_set_guess(wm_sim *s, const float *params, long long nparams);
+/* For the last step with the guess on: stats[0..2] = |b - A dB_net|^2, stats[3..5] =
+ * |b - A dB_prev|^2 per component, stats[6..8] = 1.0 where the network's guess was taken. */
+int wm_sim_guess_stats(wm_sim *s, double *stats);
 /* Select the CUDA device used by the calling host thread (one process per GPU). */
 int wm_set_device(int device);
 
@@ -193,6 +203,38 @@ int wm_deposit_current_noalloc(const double *up, const double *gp, const int *cu
 /* Page-lock (pin) a host buffer so that copies from and to it run at full link speed. */
 int wm_host_register(void *ptr, size_t bytes);
 int wm_host_unregister(void *ptr);
+
+/* ------------------------------------------------- learned initial guess for the implicit solve
+ * No reference counterpart: the reference starts its CG (common/field.f90:319-461) from the
+ * previous step's dB only.  A six-layer 3x3 convolutional network on the periodic cell grid maps
+ * (E, B at time n; J at n+1/2) to dB.  All pointers below are DEVICE pointers; activations are
+ * BF16 NHWC [nimg][h][w][c] (periodic in h and w, h a multiple of 8, w a multiple of 16), weights
+ * BF16 [9][cout][cin] (tap = (dy+1)*3 + dx+1), biases FP32.  stream: a cudaStream_t or NULL.  The
+ * calls are asynchronous on the stream. */
+enum { WM_CNN_FWD_TRAIN = 0, WM_CNN_FWD_INFER = 1, WM_CNN_FWD_LINEAR = 2, WM_CNN_BWD = 3 };
+
+/* One 3x3 convolution, (cin, cout) in {(16, 48), (48, 48), (48, 8)}.  Modes:
+ *   FWD_TRAIN  out = GELU(conv + bias) BF16 and zout = conv + bias BF16;
+ *   FWD_INFER  out = GELU(conv + bias) BF16;
+ *   FWD_LINEAR out = conv + bias FP32 [.][cout] (cin 48, cout 8 only);
+ *   BWD        out = conv (no bias) * GELU'(zprev) BF16, zprev [.][cout]: with the flipped,
+ *              transposed weights of the next layer this is the pre-activation gradient. */
+int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, int cout, int mode, int nimg, int h, int wd, void *out,
+                   void *zout, const void *zprev, void *stream);
+/* Weight and bias gradients dw[9][cout][cin] (FP32), db[cout] from the layer input x [.][cin] and
+ * the pre-activation gradient dz [.][coutp], (cin, coutp) in {(16, 48), (48, 48), (48, 16)},
+ * cout <= coutp.  scratch: at least 9*coutp*cin + coutp floats per CTA used (up to 304 CTAs). */
+int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int cout, int nimg, int h, int wd, float *dw, float *db,
+                         float *scratch, long long scratch_floats, void *stream);
+/* *loss = sum over pixels and the 3 outputs of 0.5 (pred - target)^2 / (3 npix); dz = its gradient
+ * as BF16 [npix][16].  pred FP32 [npix][8], target FP32 [npix][3]; partial holds nblocks doubles. */
+int wm_cnn_mse(const float *pred, const float *target, long long npix, void *dz, double *partial, int nblocks, double *loss, void *stream);
+/* One Adam step (step = 1, 2, ...) on n FP32 parameters. */
+int wm_cnn_adam(float *p, const float *grad, float *m, float *v, long long n, float lr, float beta1, float beta2, float eps, int step,
+                void *stream);
+/* BF16 layer weights from FP32 w[9][cout][cin]: wf = the same layout; wt (optional) = the flipped
+ * transpose [9][cin][coutb], wt(tap, ci, co) = w(8 - tap, co, ci) for co < cout, else 0. */
+int wm_cnn_prep_weights(const float *w, int cin, int cout, int coutb, void *wf, void *wt, void *stream);
 
 #ifdef __cplusplus
 }

@@ -76,10 +76,17 @@ SIGNATURES = {
     "wm_sim_get_work": [_P, _P, _P],
     "wm_sim_set_work": [_P, _P],
     "wm_sim_step_timed": [_P, _I, ctypes.POINTER(_D)],
+    "wm_sim_set_guess": [_P, _P, ctypes.c_longlong],
+    "wm_sim_guess_stats": [_P, _P],
     "wm_set_device": [_I],
     "wm_deposit_current_noalloc": [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _P, _P],
     "wm_host_register": [_P, ctypes.c_size_t],
     "wm_host_unregister": [_P],
+    "wm_cnn_conv3x3": [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P, _P],
+    "wm_cnn_conv3x3_wgrad": [_P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P, ctypes.c_int64, _P],
+    "wm_cnn_mse": [_P, _P, ctypes.c_int64, _P, _P, _I, _P, _P],
+    "wm_cnn_adam": [_P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _I, _P],
+    "wm_cnn_prep_weights": [_P, _I, _I, _I, _P, _P, _P],
 }
 _RESTYPE = {"wm_status_string": ctypes.c_char_p, "wm_build_info": ctypes.c_char_p}
 

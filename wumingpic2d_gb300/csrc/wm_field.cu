@@ -289,6 +289,55 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_resid(WmGeom g, FieldK fk, FV
     }
 }
 
+// Candidate guess stored as [3][nx*ny] (x fastest), read through ghosted indices like df.
+struct PlaneView {
+    const double *p;
+    int nx, ny;
+    __device__ __forceinline__ double operator()(int l, int ix, int iy) const
+    {
+        return p[((long long)l * ny + (iy - 2)) * nx + (ix - 2)];
+    }
+};
+
+// |b - A x|^2 per component for a candidate initial guess x (the residual of k_cg_resid).
+template <class V>
+__global__ void __launch_bounds__(CG_THREADS) k_guess_resid(WmGeom g, FieldK fk, V x, const double *__restrict__ b, double *partial,
+                                                            unsigned *ticket, double *out3)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+        const int xm = wrapm(ci - 1, g.nx) + 2, xp = wrapm(ci + 1, g.nx) + 2, ym = wrapm(cj - 1, g.ny) + 2,
+                  yp = wrapm(cj + 1, g.ny) + 2, xx = ci + 2, yy = cj + 2;
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+            const double rv = b[l * ncell + e] + x(l, xx, ym) + x(l, xm, yy) - fk.f4 * x(l, xx, yy) + x(l, xp, yy) + x(l, xx, yp);
+            acc[l] += rv * rv;
+        }
+    }
+    double tot[3];
+    if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot))
+        for (int l = 0; l < 3; ++l) out3[l] = tot[l];
+}
+
+// Start each component from the candidate where its residual is the smaller one.
+template <class FV6>
+__global__ void k_guess_pick(WmGeom g, FV6 df, const double *__restrict__ cand, double *stats)
+{
+    const long long ncell = (long long)g.nx * g.ny;
+    bool take[3];
+#pragma unroll
+    for (int l = 0; l < 3; ++l) take[l] = stats[l] < stats[3 + l];
+    if (blockIdx.x == 0 && threadIdx.x < 3) stats[6 + threadIdx.x] = take[threadIdx.x] ? 1.0 : 0.0;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
+        const int ix = (int)(e % g.nx) + 2, iy = (int)(e / g.nx) + 2;
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+            if (take[l]) df(l, ix, iy) = cand[l * ncell + e];
+    }
+}
+
 // ap = A p and p.ap (:395-415).
 __global__ void __launch_bounds__(CG_THREADS) k_cg_ap(WmGeom g, FieldK fk, const double *__restrict__ p, double *__restrict__ ap,
                                                       double *partial, unsigned *ticket, CgScal *scal)
@@ -515,7 +564,7 @@ static FieldK make_fk(const WmConst &k)
 // iters[3] and the status are read back at the end.  cg_batch = CG iterations enqueued between
 // host checks of the "still iterating" flags.
 int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<3, false> uj, FView<6, false> df, WmFieldWork &w,
-                   int *iters, int cg_batch, cudaStream_t st, wm_mark_fn mark, void *mctx, long long *launches)
+                   int *iters, int cg_batch, cudaStream_t st, wm_mark_fn mark, void *mctx, long long *launches, const WmGuess *guess)
 {
     const FieldK fk = make_fk(k);
     long long nl = 0;
@@ -527,6 +576,17 @@ int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<
     M("curre_bc");
     k_cg_rhs<FView<6, false>, FView<3, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, uf, uj, w.b, w.partial, w.ticket, w.scal);
     WM_TRY(wm_check_launch("k_cg_rhs"));
+    if (guess) {
+        M("cg_setup");
+        WM_TRY(guess->run(guess->ctx, st));
+        M("guess_net");
+        const PlaneView cv{guess->cand, g.nx, g.ny};
+        k_guess_resid<PlaneView><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, cv, w.b, w.partial, w.ticket, guess->stats);
+        k_guess_resid<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.b, w.partial, w.ticket, guess->stats + 3);
+        k_guess_pick<FView<6, false>><<<grid_for((long long)g.nx * g.ny, 256), 256, 0, st>>>(g, df, guess->cand, guess->stats);
+        WM_TRY(wm_check_launch("k_guess_pick"));
+        nl += 3;
+    }
     k_cg_resid<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.b, w.r, w.p, w.partial, w.ticket, w.scal);
     WM_TRY(wm_check_launch("k_cg_resid"));
     nl += 2;

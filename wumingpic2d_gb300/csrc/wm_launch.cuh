@@ -36,6 +36,9 @@ int wm_launch_slot_as_P(const WmGeom &g, PV v, const int *np2, int max_row_count
 int wm_launch_scan_cells(const WmGeom &g, const WmRebinScratch &sc, int *cumcnt, int *np2_out, cudaStream_t st);
 int wm_launch_rowbase(int nrows, const int *np2, long long *rowbase, cudaStream_t st);
 template <class PV>
+int wm_launch_place_sort(const WmGeom &g, PV src, PV dst, const int *np2, int max_row_count, const int *cumcnt,
+                         const WmRebinScratch &sc, cudaStream_t st);
+template <class PV>
 int wm_launch_sort_move(const WmGeom &g, PV src, PV dst, const int *src_np2, int max_row_count, const int *cumcnt,
                         const WmRebinScratch &sc, cudaStream_t st);
 
@@ -59,17 +62,51 @@ int wm_launch_phi_bc(int nx, int ny, double *phi, cudaStream_t st);
 int wm_launch_mom_bc(const WmGeom &g, double *mom, cudaStream_t st);
 int wm_launch_aos_to_soa(int nc, long long npts, const double *a, double *s, cudaStream_t st);
 int wm_launch_soa_to_aos(int nc, long long npts, const double *s, double *a, cudaStream_t st);
+// Optional initial guess for the CG: run() writes cand ([3][nx*ny], x fastest) from uf and the
+// folded uj; the solve then starts each component from whichever of cand and the previous dB has
+// the smaller residual.  stats (device, 9 doubles): |b - A cand|^2 [3], |b - A dB_prev|^2 [3],
+// 1.0 where cand was taken [3].
+struct WmGuess {
+    int (*run)(void *ctx, cudaStream_t st);
+    void *ctx;
+    double *cand;
+    double *stats;
+};
 int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<3, false> uj, FView<6, false> df, WmFieldWork &w,
-                   int *iters, int cg_batch, cudaStream_t st, wm_mark_fn mark, void *mctx, long long *launches);
+                   int *iters, int cg_batch, cudaStream_t st, wm_mark_fn mark, void *mctx, long long *launches,
+                   const WmGuess *guess = nullptr);
 int wm_launch_energy_fields(const WmGeom &g, FView<6, false> uf, double *partial, int nblocks, cudaStream_t st);
 int wm_launch_sum_partials(const double *partial, int nparts, int nsets, double *out, cudaStream_t st);
 
 // wm_mixed.cu
 int wm_mixed_ntiles(const WmGeom &g);
 size_t wm_mixed_jtile_floats(const WmGeom &g);
-int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, FView<6, false> uf,
+size_t wm_mixed_fcc_floats(const WmGeom &g);
+int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cudaStream_t st);
+int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const float *fcc,
                                  const int *cumcnt, const WmRebinScratch &sc, float *jtile, cudaStream_t st);
 int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> uj, cudaStream_t st);
 int wm_launch_mixed_unpack(const WmGeom &g, const double *stage, int pitch, const int *np2, MixedView dst, const WmRebinScratch &sc,
                            cudaStream_t st);
 int wm_launch_mixed_pack(const WmGeom &g, MixedView src, const int *np2, const int *cumcnt, int pitch, double *stage, cudaStream_t st);
+
+// wm_cnn.cu: the learned-guess network inside the solve (layer shapes are padded channel counts)
+constexpr int WM_CNN_LAYERS = 6;
+constexpr int wm_cnn_cin[WM_CNN_LAYERS] = {16, 48, 48, 48, 48, 48};
+constexpr int wm_cnn_cout[WM_CNN_LAYERS] = {48, 48, 48, 48, 48, 8};
+constexpr int WM_CNN_RED_BLOCKS = 1024;
+struct WmCnnNet {
+    float *params;  // FP32, per layer w[9][cout][cin] then b[cout]
+    void *wf[WM_CNN_LAYERS];
+    const float *bias[WM_CNN_LAYERS];
+};
+struct WmCnnWork {
+    void *x, *a0, *a1;  // BF16 [ny][nx][16], [ny][nx][48] x 2
+    float *pred;        // FP32 [ny][nx][8]
+    double *partial;    // WM_CNN_RED_BLOCKS
+    double *scale;      // 2
+};
+size_t wm_cnn_param_count();
+int wm_cnn_net_prepare(WmCnnNet &net, cudaStream_t st);
+int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf, FView<3, false> uj, const WmCnnWork &w, double *cand,
+                       cudaStream_t st);

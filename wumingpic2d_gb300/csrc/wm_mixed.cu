@@ -1,27 +1,30 @@
 // wm_mixed.cu -- the mixed-precision particle kernels (FP32 push and deposit) for sm_103a.
 //
 // Particles carry their position as (cell, FP32 offset in [0,1)) -- the cell is implicit in the
-// cell-sorted rows -- and FP32 momenta.  k_mixed_push_deposit does, for one (species, row, 32-cell
-// tile): the cell-centred fields of particle.f90:68-81 staged in shared memory as FP32, the
-// Buneman-Boris push of particle.f90:96-161 in FP32, the Esirkepov deposit of field.f90:224-298 in
-// FP32, the periodic wrap of boundary_periodic.f90:61-96 and :143-165 as integer cell arithmetic,
-// and the destination cell key and row direction the rebin needs.  Eight lanes share a cell and
-// read its particles in 32-byte runs straight from global memory; each lane keeps the cell's 5x5x3
-// partial currents in registers (the cell's particles all deposit on the same 5x5 nodes), the
-// eight lanes add theirs with shuffles, and the tile's node currents are summed from the per-cell
-// partials in a fixed order.  Tile currents go to a per-tile buffer; k_mixed_jfold adds them into
-// the FP64 global J node by node in a fixed order, so the result is deterministic and no atomics
-// touch the currents.
+// cell-sorted rows -- and FP32 momenta.  k_mixed_fields turns the FP64 Yee fields into the
+// cell-centred fields of particle.f90:68-81 once per step, as FP32.  k_mixed_push_deposit then
+// does, for one (species, row, 64-cell tile): the Buneman-Boris push of particle.f90:96-161 in
+// FP32, the Esirkepov deposit of field.f90:224-298 in FP32, the periodic wrap of
+// boundary_periodic.f90:61-96 and :143-165 as integer cell arithmetic, and the destination cell key
+// and row direction the rebin needs.  Four lanes share a cell and read its particles in 16-byte
+// runs straight from global memory; each lane reads the cell's 3x3x6 field stencil with 128-bit
+// shared loads and keeps the cell's 5x5x3 partial currents in registers (the cell's particles all
+// deposit on the same 5x5 nodes); the four lanes add theirs with shuffles, and the tile's node
+// currents are summed from the per-cell partials in a fixed order.  Tile currents go to a per-tile
+// buffer; k_mixed_jfold adds them into the FP64 global J node by node in a fixed order, so the
+// result is deterministic and no atomics touch the currents.
 #include <algorithm>
 
 #include "wm_launch.cuh"
 
 namespace {
 
-constexpr int MX_TW = 32;   // cells per tile (one row, one species)
-constexpr int MX_LPC = 8;   // lanes per cell
-constexpr int MX_THREADS = MX_TW * MX_LPC;
-constexpr int MX_JW = MX_TW + 4;
+constexpr int MX_THREADS = 256;
+constexpr int MX_LPC = 4;                   // lanes per cell
+constexpr int MX_TW = MX_THREADS / MX_LPC;  // cells per tile (one row, one species)
+constexpr int MX_JW = MX_TW + 4;            // node columns a tile deposits on
+constexpr int MX_FS = 60;                   // floats per cell of staged stencil: 9 x 6 used; 60 keeps 128-bit reads conflict-free
+constexpr int MX_PW = MX_TW + 8;            // per-cell partial rows: 4 zero cells on each side
 constexpr unsigned FULL = 0xffffffffu;
 
 struct MxConst {
@@ -43,36 +46,75 @@ __device__ __forceinline__ unsigned lanemask_lt()
     return m;
 }
 
-// One CTA per (tile of 32 cells, row, species); 8 lanes per cell read the cell's particles in
-// 32-byte runs straight from global memory.  Each lane keeps the cell's 5x5x3 partial currents in
-// registers; the 8 lanes of a cell add theirs with shuffles, and the tile's node currents are then
-// summed from the per-cell partials in a fixed order (no atomics on the currents).
+// Predicated global access: the loop body stays free of branches, and lanes past the end of their
+// cell neither read nor write.
+__device__ __forceinline__ float ld_if(const float *ptr, bool pred, float dflt)
+{
+    float v = dflt;
+    asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.global.nc.f32 %0, [%1];\n\t}" : "+f"(v) : "l"(ptr), "r"((unsigned)pred));
+    return v;
+}
+__device__ __forceinline__ void st_if(float *ptr, float v, bool pred)
+{
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.f32 [%0], %1;\n\t}" ::"l"(ptr), "f"(v), "r"((unsigned)pred)
+                 : "memory");
+}
+__device__ __forceinline__ void st_if(int *ptr, int v, bool pred)
+{
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.s32 [%0], %1;\n\t}" ::"l"(ptr), "r"(v), "r"((unsigned)pred)
+                 : "memory");
+}
+__device__ __forceinline__ void st_if(unsigned char *ptr, unsigned v, bool pred)
+{
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.u8 [%0], %1;\n\t}" ::"l"(ptr), "r"(v), "r"((unsigned)pred)
+                 : "memory");
+}
+
+// Cell-centred fields (i+1/2, j+1/2) of particle.f90:68-81 for cells -1..nx and rows -1..ny,
+// averaged in FP64 and rounded once to FP32: fcc[m][(jy+1)*(nx+2) + ix+1].
+__global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__ fcc)
+{
+    const int W = g.nx + 2;
+    const long long n = (long long)W * (g.ny + 2);
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int ix = (int)(e % W) + 1, iy = (int)(e / W) + 1;  // ghosted index of cell ix-2, row iy-2
+        fcc[e] = (float)(0.5 * (uf(0, ix, iy) + uf(0, ix, iy + 1)));
+        fcc[n + e] = (float)(0.5 * (uf(1, ix, iy) + uf(1, ix + 1, iy)));
+        fcc[2 * n + e] = (float)(0.25 * (uf(2, ix, iy) + uf(2, ix + 1, iy) + uf(2, ix, iy + 1) + uf(2, ix + 1, iy + 1)));
+        fcc[3 * n + e] = (float)(0.5 * (uf(3, ix, iy) + uf(3, ix + 1, iy)));
+        fcc[4 * n + e] = (float)(0.5 * (uf(4, ix, iy) + uf(4, ix, iy + 1)));
+        fcc[5 * n + e] = (float)uf(5, ix, iy);
+    }
+}
+
+// One CTA per (tile of 64 cells, row, species); 4 lanes per cell.  The loop body has no branches:
+// a lane past the end of its cell runs on a dummy particle with zero deposit weights and its loads
+// and stores switched off.
 __global__ void __launch_bounds__(MX_THREADS, 2)
-    k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, FView<6, false> uf, const int *__restrict__ cumcnt,
+    k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const float *__restrict__ fcc, const int *__restrict__ cumcnt,
                          int *__restrict__ key, unsigned char *__restrict__ dir, int *__restrict__ cellcnt,
                          float *__restrict__ jtile, unsigned *status)
 {
-    __shared__ float tmp[6][3][MX_TW + 2];
-    __shared__ float cellpj[65][MX_TW + 1];
+    __shared__ __align__(16) float fcell[MX_TW][MX_FS];  // [cell][(b*3 + a)*6 + m]
+    __shared__ float cellpj[65][MX_PW];                   // per-cell partials; first holds the node rows
     __shared__ int cc[MX_TW + 1];
     __shared__ float spc[5];
+    float(*tmp)[3][MX_TW + 2] = reinterpret_cast<float(*)[3][MX_TW + 2]>(&cellpj[0][0]);
+    static_assert(6 * 3 * (MX_TW + 2) <= 65 * MX_PW, "node rows fit in the partials buffer");
     const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
     const int row = isp * g.ny + jr;
     const int c0 = tile * MX_TW;
     const int ncell = min(MX_TW, g.nx - c0);
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int tid = threadIdx.x;
 
-    // fields at cell centres (i+1/2, j+1/2) for cells c0-1 .. c0+ncell and rows jr-1 .. jr+1
-    const int tw = ncell + 2;
-    for (int e = tid; e < 3 * tw; e += MX_THREADS) {
-        const int aa = e % tw, bb = e / tw;
-        const int ix = c0 - 1 + aa + 2, iy = jr - 1 + bb + 2;
-        tmp[0][bb][aa] = (float)(0.5 * (uf(0, ix, iy) + uf(0, ix, iy + 1)));
-        tmp[1][bb][aa] = (float)(0.5 * (uf(1, ix, iy) + uf(1, ix + 1, iy)));
-        tmp[2][bb][aa] = (float)(0.25 * (uf(2, ix, iy) + uf(2, ix + 1, iy) + uf(2, ix, iy + 1) + uf(2, ix + 1, iy + 1)));
-        tmp[3][bb][aa] = (float)(0.5 * (uf(3, ix, iy) + uf(3, ix + 1, iy)));
-        tmp[4][bb][aa] = (float)(0.5 * (uf(4, ix, iy) + uf(4, ix, iy + 1)));
-        tmp[5][bb][aa] = (float)uf(5, ix, iy);
+    // cell-centred fields of cells c0-1 .. c0+ncell, rows jr-1 .. jr+1
+    {
+        const int W = g.nx + 2, tw = ncell + 2;
+        const long long n = (long long)W * (g.ny + 2);
+        for (int e = tid; e < 18 * tw; e += MX_THREADS) {
+            const int aa = e % tw, mb = e / tw, bb = mb % 3, m = mb / 3;
+            tmp[m][bb][aa] = fcc[m * n + (long long)(jr + bb) * W + c0 + aa];
+        }
     }
     const int *ccrow = cumcnt + (long long)(g.nx + 1) * row;
     for (int e = tid; e <= ncell; e += MX_THREADS) cc[e] = ccrow[c0 + e];
@@ -88,6 +130,17 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
             }
     }
     __syncthreads();
+    // each cell's 3x3 stencil of the six fields, stencil position major
+    for (int e = tid; e < MX_TW * 54; e += MX_THREADS) {
+        const int c = e / 54, k = e % 54, r = k / 6, m = k % 6;
+        fcell[c][k] = c < ncell ? tmp[m][r / 3][c + r % 3] : 0.f;
+    }
+    __syncthreads();
+    // the node rows are consumed: zero the pad columns of the partials buffer
+    for (int e = tid; e < 65 * 8; e += MX_THREADS) {
+        const int r = e >> 3, q = e & 7;
+        cellpj[r][q < 4 ? q : MX_TW + q] = 0.f;
+    }
 
     const float fac1 = spc[0], txxx = spc[1], fac2 = spc[2], mqdd = spc[3], qs = spc[4];
     const int c = tid / MX_LPC, sub = tid % MX_LPC;
@@ -98,7 +151,8 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nwarp = max(nwarp, __shfl_xor_sync(FULL, nwarp, o));
     const long long rbase = a.rowbase[row];
-    const int cl = has_cell ? c : 0;  // safe index for lanes without a cell
+    const float4 *stencil = reinterpret_cast<const float4 *>(&fcell[has_cell ? c : 0][0]);
+    const int cg = c0 + c;
 
     float ax[5][4], ay[4][5], az[5][5];
 #pragma unroll
@@ -112,119 +166,129 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
     unsigned bad = 0;
     for (int it = 0; it < nwarp; ++it) {
         const bool valid = it < nmine;
-        int kk = -1;
-        if (valid) {
-            const long long p = rbase + s_beg + sub + (long long)it * MX_LPC;
-            const float dx = a.x[p], dy = a.y[p];
-            float u1 = a.ux[p], u2 = a.uy[p], u3 = a.uz[p];
-            float sx0, sx1, sx2, sy0, sy1, sy2;
-            shape3(dx - 0.5f, sx0, sx1, sx2);
-            shape3(dy - 0.5f, sy0, sy1, sy2);
-            float f[6];
+        const long long p = rbase + s_beg + sub + (long long)it * MX_LPC;
+        const float dx = ld_if(a.x + p, valid, 0.5f), dy = ld_if(a.y + p, valid, 0.5f);
+        float u1 = ld_if(a.ux + p, valid, 0.f), u2 = ld_if(a.uy + p, valid, 0.f), u3 = ld_if(a.uz + p, valid, 0.f);
+        float sx0, sx1, sx2, sy0, sy1, sy2;
+        shape3(dx - 0.5f, sx0, sx1, sx2);
+        shape3(dy - 0.5f, sy0, sy1, sy2);
+        float f[6];
+        {
+            const float w[9] = {sy0 * sx0, sy0 * sx1, sy0 * sx2, sy1 * sx0, sy1 * sx1, sy1 * sx2, sy2 * sx0, sy2 * sx1, sy2 * sx2};
+            float v[56];
 #pragma unroll
-            for (int m = 0; m < 6; ++m) {
-                const float *t0 = &tmp[m][0][cl], *t1 = &tmp[m][1][cl], *t2 = &tmp[m][2][cl];
-                f[m] = (t0[0] * sx0 + t0[1] * sx1 + t0[2] * sx2) * sy0 + (t1[0] * sx0 + t1[1] * sx1 + t1[2] * sx2) * sy1
-                       + (t2[0] * sx0 + t2[1] * sx1 + t2[2] * sx2) * sy2;
-            }
-            // Buneman-Boris
-            float v1 = u1 + fac1 * f[3], v2 = u2 + fac1 * f[4], v3 = u3 + fac1 * f[5];
-            const float g2 = kc.c2 + v1 * v1 + v2 * v2 + v3 * v3;
-            const float igam = rsqrtf(g2);
-            const float gam = g2 * igam;
-            const float fac1r = fac1 * igam;
-            const float fac2r = fac2 / (gam + txxx * (f[0] * f[0] + f[1] * f[1] + f[2] * f[2]) * igam);
-            const float w4 = v1 + fac1r * (v2 * f[2] - v3 * f[1]);
-            const float w5 = v2 + fac1r * (v3 * f[0] - v1 * f[2]);
-            const float w6 = v3 + fac1r * (v1 * f[1] - v2 * f[0]);
-            v1 = v1 + fac2r * (w5 * f[2] - w6 * f[1]);
-            v2 = v2 + fac2r * (w6 * f[0] - w4 * f[2]);
-            v3 = v3 + fac2r * (w4 * f[1] - w5 * f[0]);
-            u1 = v1 + fac1 * f[3];
-            u2 = v2 + fac1 * f[4];
-            u3 = v3 + fac1 * f[5];
-            const float ig = rsqrtf(1.f + (u1 * u1 + u2 * u2 + u3 * u3) * kc.inv_c2);
-            // move in cell units; a step crosses at most one cell (c dt < dx)
-            float nx1 = dx + u1 * kc.dt_dx * ig, ny1 = dy + u2 * kc.dt_dx * ig;
-            int incx = (int)floorf(nx1), incy = (int)floorf(ny1);
-            nx1 -= (float)incx;
-            ny1 -= (float)incy;
-            if (nx1 >= 1.f) {
-                nx1 -= 1.f;
-                ++incx;
-            }
-            if (ny1 >= 1.f) {
-                ny1 -= 1.f;
-                ++incy;
-            }
-            bad |= (incx < -1 || incx > 1 || incy < -1 || incy > 1);
-            // Esirkepov: old shape about the old cell, new shape about the new cell shifted by inc
-            float dsx[5], dsy[5];
-            const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f}, s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
-            {
-                float b0, b1, b2;
-                shape3(nx1 - 0.5f, b0, b1, b2);
-#pragma unroll
-                for (int m = 0; m < 5; ++m) {
-                    const int o = m - 2 - incx;
-                    dsx[m] = ((o == -1) ? b0 : (o == 0) ? b1 : (o == 1) ? b2 : 0.f) - s0x[m];
-                }
-                shape3(ny1 - 0.5f, b0, b1, b2);
-#pragma unroll
-                for (int m = 0; m < 5; ++m) {
-                    const int o = m - 2 - incy;
-                    dsy[m] = ((o == -1) ? b0 : (o == 0) ? b1 : (o == 1) ? b2 : 0.f) - s0y[m];
-                }
-            }
-            const float qg = qs * u3 * ig;
-            float cx[4], cy[4];
-            cx[0] = dsx[0];
-            cy[0] = dsy[0];
-#pragma unroll
-            for (int m = 1; m < 4; ++m) {
-                cx[m] = cx[m - 1] + dsx[m];
-                cy[m] = cy[m - 1] + dsy[m];
+            for (int q4 = 0; q4 < 14; ++q4) {
+                const float4 t = stencil[q4];
+                v[4 * q4] = t.x;
+                v[4 * q4 + 1] = t.y;
+                v[4 * q4 + 2] = t.z;
+                v[4 * q4 + 3] = t.w;
             }
 #pragma unroll
-            for (int jp = 0; jp < 5; ++jp) {
-                const float wy = s0y[jp] + 0.5f * dsy[jp];
-                const float fy = mqdd * wy;
+            for (int m = 0; m < 6; ++m) f[m] = w[0] * v[m];
 #pragma unroll
-                for (int m = 0; m < 4; ++m) ax[jp][m] = fmaf(fy, cx[m], ax[jp][m]);
-                const float z1 = qg * wy;
-                const float z2 = qg * (0.5f * s0y[jp] + (1.f / 3.f) * dsy[jp]);
+            for (int r = 1; r < 9; ++r)
 #pragma unroll
-                for (int ip = 0; ip < 5; ++ip) az[jp][ip] = fmaf(s0x[ip], z1, fmaf(dsx[ip], z2, az[jp][ip]));
-            }
+                for (int m = 0; m < 6; ++m) f[m] = fmaf(w[r], v[6 * r + m], f[m]);
+        }
+        // Buneman-Boris
+        float v1 = u1 + fac1 * f[3], v2 = u2 + fac1 * f[4], v3 = u3 + fac1 * f[5];
+        const float g2 = kc.c2 + v1 * v1 + v2 * v2 + v3 * v3;
+        const float igam = rsqrtf(g2);
+        const float gam = g2 * igam;
+        const float fac1r = fac1 * igam;
+        const float fac2r = __fdividef(fac2, gam + txxx * (f[0] * f[0] + f[1] * f[1] + f[2] * f[2]) * igam);
+        const float w4 = v1 + fac1r * (v2 * f[2] - v3 * f[1]);
+        const float w5 = v2 + fac1r * (v3 * f[0] - v1 * f[2]);
+        const float w6 = v3 + fac1r * (v1 * f[1] - v2 * f[0]);
+        v1 = v1 + fac2r * (w5 * f[2] - w6 * f[1]);
+        v2 = v2 + fac2r * (w6 * f[0] - w4 * f[2]);
+        v3 = v3 + fac2r * (w4 * f[1] - w5 * f[0]);
+        u1 = v1 + fac1 * f[3];
+        u2 = v2 + fac1 * f[4];
+        u3 = v3 + fac1 * f[5];
+        const float ig = rsqrtf(1.f + (u1 * u1 + u2 * u2 + u3 * u3) * kc.inv_c2);
+        // move in cell units; a step crosses at most one cell (c dt < dx)
+        float nx1 = dx + u1 * kc.dt_dx * ig, ny1 = dy + u2 * kc.dt_dx * ig;
+        int incx = (int)floorf(nx1), incy = (int)floorf(ny1);
+        nx1 -= (float)incx;
+        ny1 -= (float)incy;
+        const bool ox = nx1 >= 1.f, oy = ny1 >= 1.f;
+        nx1 = ox ? nx1 - 1.f : nx1;
+        ny1 = oy ? ny1 - 1.f : ny1;
+        incx += ox;
+        incy += oy;
+        bad |= valid & (incx < -1 || incx > 1 || incy < -1 || incy > 1);
+        // Esirkepov: old shape on nodes 1..3 about the old cell, new shape on 1+inc..3+inc
+        float dsx[5], dsy[5];
+        {
+            float b0, b1, b2;
+            shape3(nx1 - 0.5f, b0, b1, b2);
+            const bool lo = incx < 0, mid = incx == 0, hi = incx > 0;
+            dsx[0] = lo ? b0 : 0.f;
+            dsx[1] = (lo ? b1 : mid ? b0 : 0.f) - sx0;
+            dsx[2] = (lo ? b2 : mid ? b1 : b0) - sx1;
+            dsx[3] = (hi ? b1 : mid ? b2 : 0.f) - sx2;
+            dsx[4] = hi ? b2 : 0.f;
+            shape3(ny1 - 0.5f, b0, b1, b2);
+            const bool ylo = incy < 0, ymid = incy == 0, yhi = incy > 0;
+            dsy[0] = ylo ? b0 : 0.f;
+            dsy[1] = (ylo ? b1 : ymid ? b0 : 0.f) - sy0;
+            dsy[2] = (ylo ? b2 : ymid ? b1 : b0) - sy1;
+            dsy[3] = (yhi ? b1 : ymid ? b2 : 0.f) - sy2;
+            dsy[4] = yhi ? b2 : 0.f;
+        }
+        const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f}, s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
+        const float mq = valid ? mqdd : 0.f;           // zero weights for a lane past its cell
+        const float qg = valid ? qs * u3 * ig : 0.f;
+        float cx[4], cy[4];
+        cx[0] = dsx[0];
+        cy[0] = dsy[0];
+#pragma unroll
+        for (int m = 1; m < 4; ++m) {
+            cx[m] = cx[m - 1] + dsx[m];
+            cy[m] = cy[m - 1] + dsy[m];
+        }
+#pragma unroll
+        for (int jp = 0; jp < 5; ++jp) {
+            const bool inner = jp >= 1 && jp <= 3;
+            const float wy = inner ? s0y[jp] + 0.5f * dsy[jp] : 0.5f * dsy[jp];
+            const float fy = mq * wy;
+#pragma unroll
+            for (int m = 0; m < 4; ++m) ax[jp][m] = fmaf(fy, cx[m], ax[jp][m]);
+            const float z1 = qg * wy;
+            const float z2 = qg * (inner ? 0.5f * s0y[jp] + (1.f / 3.f) * dsy[jp] : (1.f / 3.f) * dsy[jp]);
 #pragma unroll
             for (int ip = 0; ip < 5; ++ip) {
-                const float fx = mqdd * (s0x[ip] + 0.5f * dsx[ip]);
-#pragma unroll
-                for (int m = 0; m < 4; ++m) ay[m][ip] = fmaf(fx, cy[m], ay[m][ip]);
+                az[jp][ip] = fmaf(dsx[ip], z2, az[jp][ip]);
+                if (ip >= 1 && ip <= 3) az[jp][ip] = fmaf(s0x[ip], z1, az[jp][ip]);
             }
-            b.x[p] = nx1;
-            b.y[p] = ny1;
-            b.ux[p] = u1;
-            b.uy[p] = u2;
-            b.uz[p] = u3;
-            int ci = c0 + c + incx;
-            ci = ci < 0 ? ci + g.nx : (ci >= g.nx ? ci - g.nx : ci);
-            int kr = jr + incy;
-            kr = kr < 0 ? kr + g.ny : (kr >= g.ny ? kr - g.ny : kr);
-            kk = (isp * g.ny + kr) * g.nx + ci;
-            key[p] = kk;
-            dir[p] = (unsigned char)(incy == 1 ? 1 : (incy == -1 ? 2 : 0));
         }
+#pragma unroll
+        for (int ip = 0; ip < 5; ++ip) {
+            const float fx = mq * ((ip >= 1 && ip <= 3) ? s0x[ip] + 0.5f * dsx[ip] : 0.5f * dsx[ip]);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) ay[m][ip] = fmaf(fx, cy[m], ay[m][ip]);
+        }
+        st_if(b.x + p, nx1, valid);
+        st_if(b.y + p, ny1, valid);
+        st_if(b.ux + p, u1, valid);
+        st_if(b.uy + p, u2, valid);
+        st_if(b.uz + p, u3, valid);
+        int ci = cg + incx;
+        ci = ci < 0 ? ci + g.nx : (ci >= g.nx ? ci - g.nx : ci);
+        int kr = jr + incy;
+        kr = kr < 0 ? kr + g.ny : (kr >= g.ny ? kr - g.ny : kr);
+        const int kk = valid ? (isp * g.ny + kr) * g.nx + ci : -1;
+        st_if(key + p, kk, valid);
+        st_if(dir + p, incy == 1 ? 1u : (incy == -1 ? 2u : 0u), valid);
         // cell counts for the sort, aggregated over the lanes that share a destination
-        const unsigned m = __ballot_sync(FULL, valid);
-        if (valid) {
-            const unsigned peers = __match_any_sync(m, kk);
-            if ((peers & lanemask_lt()) == 0) atomicAdd(&cellcnt[kk], __popc(peers));
-        }
+        const unsigned peers = __match_any_sync(FULL, kk);
+        if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&cellcnt[kk], __popc(peers));
     }
     if (bad) atomicOr(status, (unsigned)WMDEV_CELL);
 
-    // the 8 lanes of a cell add their partial currents; lane 0 of the cell keeps the sum
+    // the 4 lanes of a cell add their partial currents; lane 0 of the cell keeps the sum
 #pragma unroll
     for (int jp = 0; jp < 5; ++jp)
 #pragma unroll
@@ -236,34 +300,37 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
                 az[jp][ip] += __shfl_xor_sync(FULL, az[jp][ip], o);
             }
         }
-    if (sub == 0 && has_cell) {
+    if (sub == 0) {
+        const int col = c + 4;
 #pragma unroll
         for (int jp = 0; jp < 5; ++jp)
 #pragma unroll
             for (int ip = 0; ip < 5; ++ip) {
-                if (ip < 4) cellpj[jp * 4 + ip][c] = ax[jp][ip];
-                if (jp < 4) cellpj[20 + jp * 5 + ip][c] = ay[jp][ip];
-                cellpj[40 + jp * 5 + ip][c] = az[jp][ip];
+                if (ip < 4) cellpj[jp * 4 + ip][col] = has_cell ? ax[jp][ip] : 0.f;
+                if (jp < 4) cellpj[20 + jp * 5 + ip][col] = has_cell ? ay[jp][ip] : 0.f;
+                cellpj[40 + jp * 5 + ip][col] = has_cell ? az[jp][ip] : 0.f;
             }
     }
     __syncthreads();
-    // node currents of the tile footprint (5 rows x (32+4) columns), cells in ascending order;
-    // per-tile buffer [isp][jr][tile][3][5][MX_JW]
+    // node currents of the tile footprint (5 rows x (64+4) columns): node lx takes cell lx-ip's
+    // entry ip, cells ascending; pad cells are zero.  Per-tile buffer [isp][jr][tile][3][5][MX_JW].
     float *out = jtile + ((((long long)isp * g.ny + jr) * gridDim.x + tile) * 3) * 5 * MX_JW;
-    for (int e = tid; e < 3 * 5 * MX_JW; e += MX_THREADS) {
-        const int k = e / (5 * MX_JW), ly = (e / MX_JW) % 5, lx = e % MX_JW;
-        float sum = 0.f;
-        for (int cc2 = max(0, lx - 4); cc2 <= min(ncell - 1, lx); ++cc2) {
-            const int ip = lx - cc2;
-            if (k == 0) {
-                if (ip >= 1) sum += cellpj[ly * 4 + ip - 1][cc2];
-            } else if (k == 1) {
-                if (ly >= 1) sum += cellpj[20 + (ly - 1) * 5 + ip][cc2];
-            } else {
-                sum += cellpj[40 + ly * 5 + ip][cc2];
-            }
+    for (int e = tid; e < 5 * MX_JW; e += MX_THREADS) {
+        const int ly = e / MX_JW, lx = e % MX_JW;
+        float sx = 0.f, sy = 0.f, sz = 0.f;
+#pragma unroll
+        for (int ip = 4; ip >= 0; --ip) {
+            const int col = lx - ip + 4;
+            if (ip >= 1) sx += cellpj[ly * 4 + ip - 1][col];
+            sz += cellpj[40 + ly * 5 + ip][col];
         }
-        out[e] = sum;
+        if (ly >= 1) {
+#pragma unroll
+            for (int ip = 4; ip >= 0; --ip) sy += cellpj[20 + (ly - 1) * 5 + ip][lx - ip + 4];
+        }
+        out[e] = sx;
+        out[5 * MX_JW + e] = sy;
+        out[10 * MX_JW + e] = sz;
     }
 }
 
@@ -363,8 +430,17 @@ __global__ void k_mixed_pack(WmGeom g, MixedView src, const int *__restrict__ np
 
 int wm_mixed_ntiles(const WmGeom &g) { return (g.nx + MX_TW - 1) / MX_TW; }
 size_t wm_mixed_jtile_floats(const WmGeom &g) { return (size_t)g.nsp * g.ny * wm_mixed_ntiles(g) * 3 * 5 * MX_JW; }
+size_t wm_mixed_fcc_floats(const WmGeom &g) { return (size_t)6 * (g.nx + 2) * (g.ny + 2); }
 
-int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, FView<6, false> uf,
+int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cudaStream_t st)
+{
+    const long long n = (long long)(g.nx + 2) * (g.ny + 2);
+    const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16);
+    k_mixed_fields<<<blocks, 256, 0, st>>>(g, uf, fcc);
+    return wm_check_launch("k_mixed_fields");
+}
+
+int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const float *fcc,
                                  const int *cumcnt, const WmRebinScratch &sc, float *jtile, cudaStream_t st)
 {
     MxConst kc;
@@ -381,7 +457,7 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
     kc.c2 = (float)(k.c * k.c);
     WM_CUDA(cudaMemsetAsync(sc.cellcnt, 0, sizeof(int) * (size_t)g.nrows * g.nx, st));
     dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
-    k_mixed_push_deposit<<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, uf, cumcnt, sc.key, sc.dir, sc.cellcnt, jtile, sc.status);
+    k_mixed_push_deposit<<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, sc.key, sc.dir, sc.cellcnt, jtile, sc.status);
     return wm_check_launch("k_mixed_push_deposit");
 }
 

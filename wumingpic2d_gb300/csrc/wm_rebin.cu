@@ -219,6 +219,92 @@ __device__ __forceinline__ int incoming(const int *nup, const int *ndown, int ba
     return kin;
 }
 
+// Slot after particle_y (1-based, Pv) and destination row (kr, 0-based in the species block) of
+// the particle at slot s of row (isp, jr).
+template <class PV>
+__device__ __forceinline__ void place_one(const WmGeom &g, const PV &v, int row, int jr, int base, int s, unsigned char d, int o,
+                                          const int *__restrict__ np2, const int *__restrict__ holes,
+                                          const int *__restrict__ nup, const int *__restrict__ ndown, int &kr, int &Pv)
+{
+    if (d == 0) {
+        kr = jr;
+        const int N = np2[row], m = nup[row] + ndown[row];
+        const int kin = incoming(nup, ndown, base, kr, g.ny);
+        Pv = s + 1;
+        if (kin < m) {
+            const int Np = N + kin - m;
+            if (Pv > Np) {
+                const int rr = (N - Pv) - (m - o) + 1;
+                Pv = holes[v.idx(row, kin + rr - 1)];
+            }
+        }
+    } else {
+        int off;
+        if (d == 1) {
+            if (jr < g.ny - 1) {
+                kr = jr + 1;
+                off = 0;
+            } else {
+                kr = 0;
+                off = (g.ny > 1) ? ndown[base + 1] : ndown[base + 0];
+            }
+        } else {
+            if (jr > 0) {
+                kr = jr - 1;
+                off = (kr > 0) ? nup[base + kr - 1] : 0;
+            } else {
+                kr = g.ny - 1;
+                off = (g.ny > 1) ? nup[base + g.ny - 2] : 0;
+            }
+        }
+        const int krow = base + kr;
+        const int t = off + o + 1;
+        const int m = nup[krow] + ndown[krow];
+        Pv = (t <= m) ? holes[v.idx(krow, t - 1)] : np2[krow] + t - m;
+    }
+}
+
+// particle_y slot fused with the sort's scatter: with the new cumcnt already built from the
+// destination cell counts, every particle drops its (P, index) pair into its destination cell's
+// range right away (cursor atomics aggregated over the lanes that share a cell).
+template <class PV>
+__global__ void k_place_scatter(WmGeom g, PV v, PV dst, const int *__restrict__ np2, const unsigned char *__restrict__ dir,
+                                const int *__restrict__ ord, const int *__restrict__ holes, const int *__restrict__ nup,
+                                const int *__restrict__ ndown, const int *__restrict__ key, const int *__restrict__ cumcnt,
+                                int *__restrict__ cursor, unsigned long long *__restrict__ pairs)
+{
+    const int row = blockIdx.y;
+    const int jr = row % g.ny, base = (row / g.ny) * g.ny;
+    const int n = np2[row];
+    const int lane = threadIdx.x & 31;
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int sb = warp_global * 32; sb < n; sb += nwarps * 32) {
+        const int s = sb + lane;
+        const bool valid = s < n;
+        long long p = 0;
+        int k = -1, Pv = 0;
+        if (valid) {
+            p = v.idx(row, s);
+            int kr;
+            place_one(g, v, row, jr, base, s, dir[p], ord[p], np2, holes, nup, ndown, kr, Pv);
+            k = key[p];
+        }
+        const unsigned m = __ballot_sync(FULL, valid && k >= 0);
+        if (valid && k >= 0) {
+            const unsigned peers = __match_any_sync(m, k);
+            const int leader = __ffs(peers) - 1;
+            int basev = 0;
+            if (lane == leader) basev = atomicAdd(&cursor[k], __popc(peers));
+            basev = __shfl_sync(peers, basev, leader);
+            const int slot = basev + __popc(peers & lanemask_lt());
+            const int krow = k / g.nx, ci = k - krow * g.nx;
+            const int cstart = cumcnt[(long long)krow * (g.nx + 1) + ci];
+            pairs[dst.idx(krow, cstart + slot)] = ((unsigned long long)(unsigned)Pv << 32) | (unsigned long long)(unsigned)p;
+        }
+    }
+}
+
 // P (1-based slot after particle_y) of every particle.
 template <class PV>
 __global__ void k_place(WmGeom g, PV v, const int *__restrict__ np2, const unsigned char *__restrict__ dir,
@@ -509,6 +595,23 @@ int wm_launch_place(const WmGeom &g, PV v, const int *np2, int max_row_count, co
     return wm_check_launch("k_place");
 }
 
+// The fused step's rebin once the destination cumcnt and row bases exist: row prefix counts,
+// particle_y slots with the pair scatter, then the per-cell ranking and gather src -> dst.
+template <class PV>
+int wm_launch_place_sort(const WmGeom &g, PV src, PV dst, const int *np2, int max_row_count, const int *cumcnt,
+                         const WmRebinScratch &sc, cudaStream_t st)
+{
+    k_rowscan<PV><<<g.nrows, SCAN_THREADS, 0, st>>>(g, src, np2, sc.dir, sc.ord, sc.holes, sc.nup, sc.ndown);
+    WM_TRY(wm_check_launch("k_rowscan"));
+    k_place_scatter<PV><<<row_grid(g, max_row_count, 256), 256, 0, st>>>(g, src, dst, np2, sc.dir, sc.ord, sc.holes, sc.nup,
+                                                                        sc.ndown, sc.key, cumcnt, sc.cellcnt, sc.pairs);
+    WM_TRY(wm_check_launch("k_place_scatter"));
+    const long long ncells = (long long)g.nrows * g.nx;
+    const unsigned blocks = (unsigned)std::min<long long>((ncells + CS_WARPS - 1) / CS_WARPS, 152LL * 64);
+    k_cellsort_gather<PV><<<blocks, CS_WARPS * 32, 0, st>>>(g, src, dst, cumcnt, sc.pairs);
+    return wm_check_launch("k_cellsort_gather");
+}
+
 int wm_launch_np2_after_y(const WmGeom &g, const int *np2, const WmRebinScratch &sc, int *np2_new, int np_limit,
                           cudaStream_t st)
 {
@@ -565,7 +668,9 @@ int wm_launch_sort_move(const WmGeom &g, PV src, PV dst, const int *src_np2, int
                                             int, cudaStream_t);                                                        \
     template int wm_launch_slot_as_P<PV>(const WmGeom &, PV, const int *, int, const WmRebinScratch &, cudaStream_t);    \
     template int wm_launch_sort_move<PV>(const WmGeom &, PV, PV, const int *, int, const int *, const WmRebinScratch &,  \
-                                         cudaStream_t);
+                                         cudaStream_t);                                                                \
+    template int wm_launch_place_sort<PV>(const WmGeom &, PV, PV, const int *, int, const int *, const WmRebinScratch &, \
+                                          cudaStream_t);
 WM_INST(SoAView)
 WM_INST(AoSView)
 WM_INST(MixedView)

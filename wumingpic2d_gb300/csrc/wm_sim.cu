@@ -68,7 +68,12 @@ struct wm_sim {
     long long cap_req = 0, cap = 0, ntot = 0;
     cudaStream_t st = nullptr;
     DevBuf A[6], B[6];
-    DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out, jtile, stage2;
+    DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out, jtile, fcc, stage2;
+    // learned CG guess (off until wm_sim_set_guess)
+    DevBuf cnn_params, cnn_wf[WM_CNN_LAYERS], cnn_x, cnn_a0, cnn_a1, cnn_pred, cnn_partial, cnn_scale, guess_cand, guess_stats;
+    WmCnnNet net{};
+    WmGuess gdesc{};
+    bool guess_on = false;
     int cur = 0;  // index of the current rowbase/np2
     // field and rebin work
     DevBuf f_uf, f_uj, f_df, f_pj, f_b, f_r, f_p, f_ap, f_partial, f_ticket, f_scal;
@@ -147,6 +152,13 @@ struct wm_sim {
     FView<6, false> uf() const { return FView<6, false>{f_uf.as<double>(), g.nxw, g.nyw}; }
     FView<6, false> df() const { return FView<6, false>{f_df.as<double>(), g.nxw, g.nyw}; }
     FView<3, false> uj() const { return FView<3, false>{f_uj.as<double>(), g.nxw, g.nyw}; }
+    const WmGuess *guess() const { return guess_on ? &gdesc : nullptr; }
+    static int guess_run(void *ctx, cudaStream_t stream)
+    {
+        wm_sim *s = static_cast<wm_sim *>(ctx);
+        const WmCnnWork w{s->cnn_x.p, s->cnn_a0.p, s->cnn_a1.p, s->cnn_pred.as<float>(), s->cnn_partial.as<double>(), s->cnn_scale.as<double>()};
+        return wm_cnn_infer_guess(s->g, s->net, s->uf(), s->uj(), w, s->guess_cand.as<double>(), stream);
+    }
 
     void mark(const char *name)
     {
@@ -171,7 +183,10 @@ struct wm_sim {
             WM_TRY(A[c].ensure(esz * (size_t)cap));
             WM_TRY(B[c].ensure(esz * (size_t)cap));
         }
-        if (mixed()) WM_TRY(jtile.ensure(sizeof(float) * wm_mixed_jtile_floats(g)));
+        if (mixed()) {
+            WM_TRY(jtile.ensure(sizeof(float) * wm_mixed_jtile_floats(g)));
+            WM_TRY(fcc.ensure(sizeof(float) * wm_mixed_fcc_floats(g)));
+        }
         for (int c = 0; c < 2; ++c) {
             WM_TRY(rowbase[c].ensure(sizeof(long long) * (g.nrows + 1)));
             WM_TRY(np2[c].ensure(sizeof(int) * g.nrows));
@@ -208,7 +223,7 @@ struct wm_sim {
     {
         size_t t = 0;
         for (int c = 0; c < 6; ++c) t += A[c].bytes + B[c].bytes;
-        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &f_uf, &f_uj, &f_df, &f_pj,
+        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &fcc, &f_uf, &f_uj, &f_df, &f_pj,
                                 &f_b, &f_r, &f_p, &f_ap, &f_partial, &rb_dir, &rb_ord, &rb_P, &rb_key, &rb_holes, &rb_nup,
                                 &rb_ndown, &rb_cellcnt, &rb_pairs})
             t += b->bytes;
@@ -222,10 +237,14 @@ struct wm_sim {
             A[c].release();
             B[c].release();
         }
-        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &stage2,
+        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &stage2,
                           &f_uf, &f_uj, &f_df, &f_pj, &f_b, &f_r, &f_p, &f_ap, &f_partial, &f_ticket, &f_scal, &rb_dir, &rb_ord,
                           &rb_P, &rb_key, &rb_holes, &rb_nup, &rb_ndown, &rb_cellcnt, &rb_pairs, &rb_status})
             b->release();
+        for (DevBuf *b : {&cnn_params, &cnn_x, &cnn_a0, &cnn_a1, &cnn_pred, &cnn_partial, &cnn_scale, &guess_cand, &guess_stats})
+            b->release();
+        for (DevBuf &b : cnn_wf) b.release();
+        guess_on = false;
         for (Mark &m : marks) cudaEventDestroy(m.ev);
         marks.clear();
         if (scal_host) cudaFreeHost(scal_host);
@@ -313,23 +332,27 @@ struct wm_sim {
         WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
         mark("start");
         MixedView va = mview(A, cur), vb = mview(B, cur);
-        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, uf(), cumcnt.as<int>(), sc, jtile.as<float>(), st));
+        WM_TRY(wm_launch_mixed_fields(g, uf(), fcc.as<float>(), st));
+        ++nl;
+        mark("fields");
+        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, fcc.as<float>(), cumcnt.as<int>(), sc, jtile.as<float>(), st));
         ++nl;
         mark("push_deposit");
         WM_TRY(wm_launch_mixed_jfold(g, jtile.as<float>(), uj(), st));
         ++nl;
         mark("deposit");
         WmFieldWork w = work();
-        const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl);
+        const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl, guess());
         if (s != WM_OK) return s;
-        WM_TRY(wm_launch_place(g, vb, np2[cur].as<int>(), max_row, sc, nullptr, st));
+        // destination counts came from the push: the new cumcnt and row bases first, then the
+        // particle_y slots scatter straight into the destination cells
         WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
         WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
-        nl += 4;
-        mark("place_scan");
-        WM_TRY(wm_launch_sort_move(g, mview(B, cur, pid_cur), mview(A, 1 - cur, 1 - pid_cur), np2[cur].as<int>(), max_row,
-                                   cumcnt.as<int>(), sc, st));
         nl += 2;
+        mark("scan");
+        WM_TRY(wm_launch_place_sort(g, mview(B, cur, pid_cur), mview(A, 1 - cur, 1 - pid_cur), np2[cur].as<int>(), max_row,
+                                    cumcnt.as<int>(), sc, st));
+        nl += 3;
         mark("sort_move");
         cur = 1 - cur;
         pid_cur = 1 - pid_cur;
@@ -353,18 +376,17 @@ struct wm_sim {
         nl += 2;
         mark("deposit");
         WmFieldWork w = work();
-        const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl);
+        const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl, guess());
         if (s != WM_OK) return s;
         WM_TRY(wm_launch_wrap_classify(g, k.delx, vb, np2[cur].as<int>(), max_row, 1 | 2 | 4, sc, st));
         nl += 1;
         mark("classify");
-        WM_TRY(wm_launch_place(g, vb, np2[cur].as<int>(), max_row, sc, nullptr, st));
         WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
         WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
-        nl += 4;
-        mark("place_scan");
-        WM_TRY(wm_launch_sort_move(g, vb, view(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
         nl += 2;
+        mark("scan");
+        WM_TRY(wm_launch_place_sort(g, vb, view(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
+        nl += 3;
         mark("sort_move");
         cur = 1 - cur;
         launches += nl;
@@ -669,6 +691,48 @@ int wm_sim_set_work(wm_sim *s, const double *df)
     WM_TRY(s->uf_aos.ensure(sizeof(double) * 6 * npts));
     WM_CUDA(cudaMemcpyAsync(s->uf_aos.p, df, sizeof(double) * 6 * npts, cudaMemcpyHostToDevice, s->st));
     WM_TRY(wm_launch_aos_to_soa(6, npts, s->uf_aos.as<double>(), s->f_df.as<double>(), s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    return WM_OK;
+}
+
+int wm_sim_set_guess(wm_sim *s, const float *params, long long nparams)
+{
+    if (!s) return WM_ERR_BAD_ARG;
+    if (!params) {
+        s->guess_on = false;
+        return WM_OK;
+    }
+    const WmGeom &g = s->g;
+    if (nparams != (long long)wm_cnn_param_count() || g.nx % 16 != 0 || g.ny % 8 != 0) return WM_ERR_BAD_ARG;
+    const size_t ncell = (size_t)g.nx * g.ny;
+    WM_TRY(s->cnn_params.ensure(sizeof(float) * nparams));
+    for (int l = 0; l < WM_CNN_LAYERS; ++l) {
+        WM_TRY(s->cnn_wf[l].ensure(2 * 9 * (size_t)wm_cnn_cin[l] * wm_cnn_cout[l]));
+        s->net.wf[l] = s->cnn_wf[l].p;
+    }
+    WM_TRY(s->cnn_x.ensure(2 * 16 * ncell));
+    WM_TRY(s->cnn_a0.ensure(2 * 48 * ncell));
+    WM_TRY(s->cnn_a1.ensure(2 * 48 * ncell));
+    WM_TRY(s->cnn_pred.ensure(sizeof(float) * 8 * ncell));
+    WM_TRY(s->cnn_partial.ensure(sizeof(double) * WM_CNN_RED_BLOCKS));
+    WM_TRY(s->cnn_scale.ensure(sizeof(double) * 2));
+    WM_TRY(s->guess_cand.ensure(sizeof(double) * 3 * ncell));
+    WM_TRY(s->guess_stats.ensure(sizeof(double) * 9));
+    WM_CUDA(cudaMemsetAsync(s->guess_stats.p, 0, sizeof(double) * 9, s->st));
+    WM_CUDA(cudaMemcpyAsync(s->cnn_params.p, params, sizeof(float) * nparams, cudaMemcpyHostToDevice, s->st));
+    s->net.params = s->cnn_params.as<float>();
+    WM_TRY(wm_cnn_net_prepare(s->net, s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    s->gdesc = WmGuess{&wm_sim::guess_run, s, s->guess_cand.as<double>(), s->guess_stats.as<double>()};
+    s->guess_on = true;
+    return WM_OK;
+}
+
+int wm_sim_guess_stats(wm_sim *s, double *stats9)
+{
+    if (!s || !stats9) return WM_ERR_BAD_ARG;
+    if (!s->guess_on) return WM_ERR_NOT_INIT;
+    WM_CUDA(cudaMemcpyAsync(stats9, s->guess_stats.p, sizeof(double) * 9, cudaMemcpyDeviceToHost, s->st));
     WM_CUDA(cudaStreamSynchronize(s->st));
     return WM_OK;
 }
