@@ -172,7 +172,8 @@ int wm_sim_step_timed(wm_sim *s, int nsteps, double *ms);
  * multiple of 16 and ny a multiple of 8. */
 int wm_sim_set_guess(wm_sim *s, const float *params, long long nparams);
 /* For the last step with the guess on: stats[0..2] = |b - A dB_net|^2, stats[3..5] =
- * |b - A dB_prev|^2 per component, stats[6..8] = 1.0 where the network's guess was taken. */
+ * |b - A dB_prev|^2 per component, stats[6..8] = 1.0 where the network's guess was taken,
+ * stats[9..11] = |b|^2 (12 values). */
 int wm_sim_guess_stats(wm_sim *s, double *stats);
 /* Select the CUDA device used by the calling host thread (one process per GPU). */
 int wm_set_device(int device);
@@ -229,9 +230,10 @@ int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int 
 /* *loss = sum over pixels and the 3 outputs of 0.5 (pred - target)^2 / (3 npix); dz = its gradient
  * as BF16 [npix][16].  pred FP32 [npix][8], target FP32 [npix][3]; partial holds nblocks doubles. */
 int wm_cnn_mse(const float *pred, const float *target, long long npix, void *dz, double *partial, int nblocks, double *loss, void *stream);
-/* One Adam step (step = 1, 2, ...) on n FP32 parameters. */
-int wm_cnn_adam(float *p, const float *grad, float *m, float *v, long long n, float lr, float beta1, float beta2, float eps, int step,
-                void *stream);
+/* One Adam step (step = 1, 2, ...) on n FP32 parameters; mask (optional, n values) multiplies the
+ * gradient, so parameters with mask 0 keep their value. */
+int wm_cnn_adam(float *p, const float *grad, const float *mask, float *m, float *v, long long n, float lr, float beta1, float beta2,
+                float eps, int step, void *stream);
 /* BF16 layer weights from FP32 w[9][cout][cin]: wf = the same layout; wt (optional) = the flipped
  * transpose [9][cin][coutb], wt(tap, ci, co) = w(8 - tap, co, ci) for co < cout, else 0. */
 int wm_cnn_prep_weights(const float *w, int cin, int cout, int coutb, void *wf, void *wt, void *stream);

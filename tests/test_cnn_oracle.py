@@ -79,3 +79,32 @@ def test_flatten_roundtrip_and_size():
         assert np.array_equal(w, w2) and np.array_equal(b, b2)
     # padding stays zero: layer 0 inputs 9..15 and layer 5 outputs 3..7
     assert not params[0][0][:, :, 9:].any() and not params[5][0][:, 3:, :].any()
+
+
+def test_network_mask_is_block_diagonal_and_scales_are_per_group():
+    from wumingpic2d_gb300 import cnn
+
+    mask = cnn.param_mask()
+    assert mask.size == cnn.NPARAMS
+    P = C.unflatten(cnn.init_params(1))
+    M = C.unflatten(mask)
+    for (w, b), (mw, mb) in zip(P, M):
+        assert not (w * (1 - mw)).any()  # weights outside the blocks start (and stay) at zero
+    # layer 0: input group -> hidden block; layer 5: hidden block k -> output k only
+    w0 = M[0][0]
+    assert w0[0, 0:16, 0:3].all() and not w0[0, 0:16, 3:].any()
+    assert w0[4, 32:48, 6:11].all() and not w0[4, 32:48, :6].any() and not w0[4, :, 11:].any()
+    w5 = M[5][0]
+    assert w5[8, 2, 32:48].all() and not w5[8, 2, :32].any() and not w5[:, 3:, :].any()
+    # the normalisation divides each group by its own scale: scaling one group's raw inputs
+    # leaves every packed channel unchanged
+    rng = np.random.default_rng(0)
+    xs = rng.standard_normal((2, 8, 16, 9))
+    ys = rng.standard_normal((2, 8, 16, 3))
+    x1, y1 = cnn.normalise(xs, ys)
+    xs2 = xs.copy()
+    xs2[..., [5, 0, 1, 6, 7]] *= 1e3  # the dBz group
+    ys2 = ys.copy()
+    ys2[..., 2] *= 1e3
+    x2, y2 = cnn.normalise(xs2, ys2)
+    assert np.allclose(x1, x2) and np.allclose(y1, y2)

@@ -1,0 +1,130 @@
+"""The learned CG guess on the GPU: the BF16 tensor-core forward and backward kernels against the
+CPU network (oracle/cnn_ref.py, which emulates the same BF16 roundings), training on pairs the
+FP64 solver produced, and the iteration count it saves inside the resident step.
+
+Stated bounds (normwise relative): forward output 2e-2, stored activations 2e-2, parameter
+gradients 5e-2 per layer.  The differences come from FP32 accumulation order against exact sums,
+which moves a few BF16 roundings by one unit.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import cnn_ref as C
+from tests.helpers import rel_err
+from wumingpic2d_gb300 import cnn
+from wumingpic2d_gb300.sim import Simulation
+from wumingpic2d_gb300.weibel import WeibelConfig, weibel_particles
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(seed, n=2, H=16, W=32):
+    rng = np.random.default_rng(seed)
+    params = cnn.init_params(seed)
+    P = C.unflatten(params)
+    for l, (w, b) in enumerate(P):  # non-zero biases on the real channels
+        rout = 3 if l == 5 else w.shape[1]
+        b[:rout] = (0.1 * rng.standard_normal(rout)).astype(np.float32)
+    params = C.flatten(P)
+    x = np.zeros((n, H, W, 16))
+    x[..., :9] = C.bf16(rng.standard_normal((n, H, W, 9)))
+    target = rng.standard_normal((n, H, W, 3)).astype(np.float32)
+    return params, C.unflatten(params), x, target
+
+
+def _dev_x(x):
+    return torch.tensor(x, dtype=torch.float32).to("cuda", torch.bfloat16)
+
+
+def test_forward_matches_oracle(gpu):
+    params, P, x, _ = _case(1)
+    net = cnn.GuessNet(params)
+    pred_i, _ = net.forward(_dev_x(x), train=False)
+    pred_t, (acts, zs) = net.forward(_dev_x(x), train=True)
+    torch.cuda.synchronize()
+    ref, (racts, rzs) = C.forward(x, P, bf=True)
+    e_inf = rel_err(pred_i.cpu().numpy()[..., :3], ref[..., :3])
+    e_tr = rel_err(pred_t.cpu().numpy()[..., :3], ref[..., :3])
+    e_act = max(rel_err(a.float().cpu().numpy(), r) for a, r in zip(acts[1:], racts[1:]))
+    e_z = max(rel_err(z.float().cpu().numpy(), r) for z, r in zip(zs, rzs))
+    print(f"\nforward vs oracle: infer {e_inf:.2e} train {e_tr:.2e} activations {e_act:.2e} pre-activations {e_z:.2e}")
+    assert e_inf <= 2e-2 and e_tr <= 2e-2 and e_act <= 2e-2 and e_z <= 2e-2
+    assert np.array_equal(pred_i.cpu().numpy(), pred_t.cpu().numpy())  # same arithmetic in both modes
+    assert not pred_i.cpu().numpy()[..., 3:].any()  # padded outputs stay zero
+
+
+def test_gradients_match_oracle(gpu):
+    params, P, x, target = _case(2)
+    net = cnn.GuessNet(params)
+    tr = cnn.Trainer(net)
+    loss = tr.loss_and_grad(_dev_x(x), torch.tensor(target, device="cuda"))
+    torch.cuda.synchronize()
+    pred, cache = C.forward(x, P, bf=True)
+    rloss, g = C.loss_and_grad(pred, target)
+    grads = C.backward(cache, g, P, bf=True)
+    gflat = C.unflatten(tr.grad.cpu().numpy())
+    errs = []
+    for l, ((dw, db), (rdw, rdb)) in enumerate(zip(gflat, grads)):
+        errs.append((rel_err(dw, rdw), rel_err(db[:rdb.size], rdb)))
+    print("\ngradients vs oracle (dW, db) per layer: " + ", ".join(f"({a:.1e}, {b:.1e})" for a, b in errs)
+          + f"; loss {float(loss.item()):.6e} vs {rloss:.6e}")
+    assert abs(float(loss.item()) - rloss) <= 1e-2 * rloss
+    for a, b in errs:
+        assert a <= 5e-2 and b <= 5e-2
+
+
+def _weibel_sim(seed, nx=128, ny=128, ppc=16):
+    cfg = WeibelConfig(nx=nx, ny=ny, ppc=ppc, seed=seed)
+    d = cfg.dims()
+    up, np2 = weibel_particles(cfg)
+    sim = Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision="fp64")
+    sim.load(up, d.alloc_uf(), np2)
+    return sim
+
+
+@pytest.fixture(scope="module")
+def trained():
+    with _weibel_sim(11) as sim:
+        xs, ys = cnn.capture_pairs(sim, 160, every=1)
+    xn, yn = cnn.normalise(xs, ys)
+    x, y = cnn.to_device(xn, yn)
+    net = cnn.GuessNet(seed=3)
+    hist = cnn.train(net, x, y, steps=1500, batch=8, lr=2e-3, seed=4, log_every=250)
+    return net, hist
+
+
+def test_training_reduces_the_loss(gpu, trained):
+    _, hist = trained
+    print("\ntraining loss: " + ", ".join(f"{it}:{l:.3e}" for it, l in hist))
+    assert hist[-1][1] < 0.05 * hist[0][1]
+
+
+def test_learned_guess_saves_cg_iterations(gpu, trained):
+    net, _ = trained
+    params = net.host_params()
+    runs = {}
+    for mode in ("prev", "net"):
+        with _weibel_sim(12) as sim:
+            sim.step(20)  # leave the first steps, where both guesses are trivial
+            if mode == "net":
+                sim.set_guess(params)
+            its, taken, rel = [], 0, []
+            for _ in range(40):
+                sim.step(1)
+                its.append(sim.cg_iters().sum())
+                if mode == "net":
+                    st = sim.guess_stats()
+                    taken += int(st[6:9].sum())
+                    rel.append(np.sqrt(st[0:6] / np.concatenate([st[9:12], st[9:12]])))
+            runs[mode] = (np.array(its), taken, sim.energy(), np.array(rel))
+    it_prev, it_net = runs["prev"][0], runs["net"][0]
+    rel = runs["net"][3]
+    print(f"\nCG iterations per step (3 components): previous-step guess {it_prev.mean():.2f}, "
+          f"learned guess {it_net.mean():.2f}; network guess taken {runs['net'][1]} of {3 * len(it_net)} solves; "
+          f"median initial relative residual per component: network {np.median(rel[:, :3], axis=0)}, "
+          f"previous step {np.median(rel[:, 3:], axis=0)}")
+    assert it_net.mean() < it_prev.mean()
+    # the answer does not depend on the guess beyond the solver tolerance
+    e_prev, e_net = runs["prev"][2], runs["net"][2]
+    assert abs(e_net.sum() - e_prev.sum()) <= 1e-6 * e_prev.sum()

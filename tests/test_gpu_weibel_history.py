@@ -25,7 +25,7 @@ NSTEPS, EVERY = 2000, 20
 
 
 def _run(precision):
-    cfg = WeibelConfig(nx=256, ny=256, ppc=16, seed=2024)
+    cfg = WeibelConfig(nx=256, ny=256, ppc=16, seed=2024, slack=2.5)  # rows bunch up in the filaments
     d = cfg.dims()
     up, np2 = weibel_particles(cfg)
     uf = d.alloc_uf()

@@ -85,7 +85,7 @@ SIGNATURES = {
     "wm_cnn_conv3x3": [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P, _P],
     "wm_cnn_conv3x3_wgrad": [_P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P, ctypes.c_int64, _P],
     "wm_cnn_mse": [_P, _P, ctypes.c_int64, _P, _P, _I, _P, _P],
-    "wm_cnn_adam": [_P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _I, _P],
+    "wm_cnn_adam": [_P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _I, _P],
     "wm_cnn_prep_weights": [_P, _I, _I, _I, _P, _P, _P],
 }
 _RESTYPE = {"wm_status_string": ctypes.c_char_p, "wm_build_info": ctypes.c_char_p}

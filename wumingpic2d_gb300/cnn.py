@@ -1,0 +1,286 @@
+"""Learned initial guess for the implicit field solve: the network's parameters, training on the
+GPU with the library's own BF16 tensor-core kernels (wm_cnn_*), and capture of (input, converged
+dB) pairs from runs.
+
+The reference starts the CG of common/field.f90:319-461 from the previous step's dB (:355); the
+network predicts dB from E, B at time n and the new J instead.  The solve keeps the previous-step
+guess as its fallback per component and runs to the same tolerance either way
+(Simulation.set_guess), so the network changes the iteration count, never the answer.
+
+Network: six periodic 3x3 convolutions with channels (padded to the tensor-core tile)
+16 -> 48 -> 48 -> 48 -> 48 -> 48 -> 8, GELU between layers.  The three CG unknowns decouple --
+dBx depends on (Bx, Ez, Jz) only, dBy on (By, Ez, Jz), dBz on (Bz, Ex, Ey, Jx, Jy) (the right-hand
+side of field.f90:125-146, with one diagonal operator per component) -- so the network is three
+16-channel sub-networks side by side: its weights are block-diagonal over the groups (the other
+weights are held at zero by a gradient mask), and each group's inputs are divided by their own
+root mean square s_k, the prediction being scaled back by s_k.  That makes the guess exactly
+scale-equivariant per component, as the linear solve it replaces.  Input channels: 0-2 (Bx, Ez,
+Jz)/s_x, 3-5 (By, Ez, Jz)/s_y, 6-10 (Bz, Ex, Ey, Jx, Jy)/s_z, 11-15 zero; the device-side packing of
+the resident step (wm_cnn.cu) is the same.
+PyTorch provides device memory and the stream here; every layer runs in the library's kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from ._native import check, lib
+from .layout import Dims
+
+LAYERS = ((16, 48), (48, 48), (48, 48), (48, 48), (48, 48), (48, 8))  # padded (cin, cout)
+NOUT, GRAD_CH, GROUP_CH = 3, 16, 16
+# raw inputs: 0-2 Ex, Ey, Ez; 3-5 Bx, By, Bz; 6-8 Jx, Jy, Jz
+PACKED_SOURCE = (3, 2, 8, 4, 2, 8, 5, 0, 1, 6, 7)
+PACKED_GROUP = (0, 0, 0, 1, 1, 1, 2, 2, 2, 2, 2)
+FWD_TRAIN, FWD_INFER, FWD_LINEAR, BWD = 0, 1, 2, 3
+WGRAD_SCRATCH = 304 * (9 * 48 * 48 + 48)  # floats: per-CTA partial gradients, 304 CTAs at most
+
+
+def _offsets():
+    out, o = [], 0
+    for cin, cout in LAYERS:
+        out.append((o, o + 9 * cin * cout, cin, cout))
+        o += 9 * cin * cout + cout
+    return out, o
+
+
+OFFSETS, NPARAMS = _offsets()
+
+
+def _groups_in(l, cin):
+    """Group of each input channel of layer l (-1: padding)."""
+    if l == 0:
+        return np.array([PACKED_GROUP[c] if c < len(PACKED_GROUP) else -1 for c in range(cin)])
+    return np.arange(cin) // GROUP_CH
+
+
+def _groups_out(l, cout):
+    if l == len(LAYERS) - 1:
+        return np.array([c if c < NOUT else -1 for c in range(cout)])
+    return np.arange(cout) // GROUP_CH
+
+
+def param_mask() -> np.ndarray:
+    """1 for the parameters the block-diagonal network uses, 0 for the rest (flat, FP32)."""
+    mask = np.zeros(NPARAMS, dtype=np.float32)
+    for l, (wo, bo, cin, cout) in enumerate(OFFSETS):
+        gi, go = _groups_in(l, cin), _groups_out(l, cout)
+        m = (go[:, None] == gi[None, :]) & (go[:, None] >= 0)
+        mask[wo:bo] = np.broadcast_to(m, (9, cout, cin)).ravel()
+        mask[bo:bo + cout] = go >= 0
+    return mask
+
+
+def init_params(seed: int = 0) -> np.ndarray:
+    """He-style initial weights on the used (block-diagonal) entries, zero biases; FP32, flat."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    flat = np.zeros(NPARAMS, dtype=np.float32)
+    mask = param_mask()
+    for l, (wo, bo, cin, cout) in enumerate(OFFSETS):
+        m = mask[wo:bo].reshape(9, cout, cin)
+        fan_in = np.maximum(m.sum(axis=(0, 2)), 1)  # per output channel
+        w = rng.standard_normal((9, cout, cin)) * np.sqrt(2.0 / fan_in)[None, :, None]
+        flat[wo:bo] = (w * m).astype(np.float32).ravel()
+    return flat
+
+
+def _p(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _pf(t, offset):
+    return ctypes.c_void_p(t.data_ptr() + 4 * offset)
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class GuessNet:
+    """Parameters (FP32 master copy on the device) and the BF16 layer weights the kernels read."""
+
+    def __init__(self, params: np.ndarray | None = None, seed: int = 0, device: str = "cuda"):
+        flat = init_params(seed) if params is None else np.asarray(params, dtype=np.float32)
+        if flat.size != NPARAMS:
+            raise ValueError(f"expected {NPARAMS} parameters, got {flat.size}")
+        self.device = torch.device(device)
+        self.params = torch.tensor(flat, device=self.device)
+        self.wf = [torch.empty(9 * ci * co, dtype=torch.bfloat16, device=self.device) for ci, co in LAYERS]
+        self.wt = [None] + [torch.empty(9 * ci * (GRAD_CH if l == len(LAYERS) - 1 else co), dtype=torch.bfloat16, device=self.device)
+                            for l, (ci, co) in enumerate(LAYERS) if l > 0]
+        self.prep()
+
+    def prep(self) -> None:
+        """Refresh the BF16 forward weights and the flipped transposes used by the input gradient."""
+        for l, (wo, _, cin, cout) in enumerate(OFFSETS):
+            coutb = GRAD_CH if l == len(LAYERS) - 1 else cout
+            check(lib().wm_cnn_prep_weights(_pf(self.params, wo), cin, cout, coutb, _p(self.wf[l]), _p(self.wt[l]), _stream()),
+                  "wm_cnn_prep_weights")
+
+    def host_params(self) -> np.ndarray:
+        return self.params.detach().cpu().numpy().copy()
+
+    def load_params(self, flat: np.ndarray) -> None:
+        self.params.copy_(torch.from_numpy(np.asarray(flat, dtype=np.float32)))
+        self.prep()
+
+    def forward(self, x: torch.Tensor, train: bool = False):
+        """x: BF16 [n][H][W][16] on the device.  Returns (pred FP32 [n][H][W][8], cache)."""
+        n, H, W, c = x.shape
+        if c != LAYERS[0][0] or x.dtype != torch.bfloat16:
+            raise ValueError("input must be BF16 [n][H][W][16]")
+        acts, zs, a = [x], [], x
+        for l in range(len(LAYERS) - 1):
+            wo, bo, cin, cout = OFFSETS[l]
+            out = torch.empty((n, H, W, cout), dtype=torch.bfloat16, device=self.device)
+            z = torch.empty_like(out) if train else None
+            check(lib().wm_cnn_conv3x3(_p(a), _p(self.wf[l]), _pf(self.params, bo), cin, cout, FWD_TRAIN if train else FWD_INFER,
+                                       n, H, W, _p(out), _p(z), None, _stream()), "wm_cnn_conv3x3")
+            acts.append(out)
+            zs.append(z)
+            a = out
+        wo, bo, cin, cout = OFFSETS[-1]
+        pred = torch.empty((n, H, W, cout), dtype=torch.float32, device=self.device)
+        check(lib().wm_cnn_conv3x3(_p(a), _p(self.wf[-1]), _pf(self.params, bo), cin, cout, FWD_LINEAR, n, H, W, _p(pred), None, None,
+                                   _stream()), "wm_cnn_conv3x3")
+        return pred, (acts, zs)
+
+    def backward(self, cache, dpred: torch.Tensor, grad: torch.Tensor, scratch: torch.Tensor) -> None:
+        """Parameter gradients into grad (flat FP32) for the output gradient dpred (BF16 [..][16])."""
+        acts, zs = cache
+        n, H, W, _ = dpred.shape
+        dz = dpred
+        for l in range(len(LAYERS) - 1, -1, -1):
+            wo, bo, cin, cout = OFFSETS[l]
+            coutp = GRAD_CH if l == len(LAYERS) - 1 else cout
+            check(lib().wm_cnn_conv3x3_wgrad(_p(acts[l]), _p(dz), cin, coutp, cout, n, H, W, _pf(grad, wo), _pf(grad, bo), _p(scratch),
+                                             scratch.numel(), _stream()), "wm_cnn_conv3x3_wgrad")
+            if l == 0:
+                break
+            dprev = torch.empty((n, H, W, cin), dtype=torch.bfloat16, device=self.device)
+            check(lib().wm_cnn_conv3x3(_p(dz), _p(self.wt[l]), None, coutp, cin, BWD, n, H, W, _p(dprev), None, _p(zs[l - 1]),
+                                       _stream()), "wm_cnn_conv3x3")
+            dz = dprev
+
+
+class Trainer:
+    """Adam on the mean squared error, all steps on the device; the gradient mask keeps the
+    network block-diagonal."""
+
+    def __init__(self, net: GuessNet, lr: float = 1e-3, betas=(0.9, 0.999), eps: float = 1e-8, masked: bool = True):
+        self.net, self.lr, self.betas, self.eps = net, lr, betas, eps
+        dev = net.device
+        self.m = torch.zeros_like(net.params)
+        self.v = torch.zeros_like(net.params)
+        self.grad = torch.zeros_like(net.params)
+        self.mask = torch.tensor(param_mask(), device=dev) if masked else None
+        self.scratch = torch.empty(WGRAD_SCRATCH, dtype=torch.float32, device=dev)
+        self.nblocks = 512
+        self.partial = torch.empty(self.nblocks, dtype=torch.float64, device=dev)
+        self.loss = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.t = 0
+
+    def loss_and_grad(self, x: torch.Tensor, target: torch.Tensor) -> torch.Tensor:
+        """Forward, loss and parameter gradients (into self.grad); returns the loss (device)."""
+        pred, cache = self.net.forward(x, train=True)
+        n, H, W, _ = x.shape
+        dz = torch.empty((n, H, W, GRAD_CH), dtype=torch.bfloat16, device=self.net.device)
+        check(lib().wm_cnn_mse(_p(pred), _p(target), n * H * W, _p(dz), _p(self.partial), self.nblocks, _p(self.loss), _stream()),
+              "wm_cnn_mse")
+        self.net.backward(cache, dz, self.grad, self.scratch)
+        return self.loss
+
+    def step(self, x: torch.Tensor, target: torch.Tensor, lr: float | None = None) -> torch.Tensor:
+        loss = self.loss_and_grad(x, target)
+        self.t += 1
+        check(lib().wm_cnn_adam(_p(self.net.params), _p(self.grad), _p(self.mask), _p(self.m), _p(self.v), self.net.params.numel(),
+                                self.lr if lr is None else lr, self.betas[0], self.betas[1], self.eps, self.t, _stream()),
+              "wm_cnn_adam")
+        self.net.prep()
+        return loss
+
+
+# ----------------------------------------------------------------------------- data
+def field_inputs(d: Dims, uf: np.ndarray, uj: np.ndarray) -> np.ndarray:
+    """Raw inputs [ny][nx][9] = (Ex, Ey, Ez, Bx, By, Bz, Jx, Jy, Jz) at each cell's stored index,
+    from reference-layout uf (6, nx+4, ny+4) and uj (3, nx+4, ny+4)."""
+    sl = (slice(None), slice(2, d.nx + 2), slice(2, d.ny + 2))
+    stack = np.concatenate([uf[3:6][sl], uf[0:3][sl], uj[0:3][sl]])
+    return np.ascontiguousarray(np.transpose(stack, (2, 1, 0)))
+
+
+def solve_target(d: Dims, df: np.ndarray) -> np.ndarray:
+    """The converged dB [ny][nx][3] from a reference-layout df (6, nx+4, ny+4)."""
+    return np.ascontiguousarray(np.transpose(df[0:3, 2:d.nx + 2, 2:d.ny + 2], (2, 1, 0)))
+
+
+def capture_pairs(sim, nsteps: int, every: int = 1):
+    """Step a resident Simulation nsteps times; every `every` steps keep (raw inputs, converged dB)."""
+    d = sim.dims
+    xs, ys = [], []
+    for k in range(nsteps):
+        uf = sim.fields()
+        sim.step(1)
+        if k % every == 0:
+            df, uj = sim.get_work()
+            xs.append(field_inputs(d, uf, uj))
+            ys.append(solve_target(d, df))
+    return np.stack(xs), np.stack(ys)
+
+
+def group_scales(xs: np.ndarray) -> np.ndarray:
+    """Per sample, the root mean square of each group's raw inputs: [n][3]."""
+    xs = np.asarray(xs, dtype=np.float64)
+    out = np.zeros((xs.shape[0], 3))
+    for g in range(3):
+        src = [PACKED_SOURCE[k] for k in range(len(PACKED_SOURCE)) if PACKED_GROUP[k] == g]
+        out[:, g] = np.sqrt(np.mean(xs[..., src] ** 2, axis=(1, 2, 3)))
+    return out
+
+
+def normalise(xs: np.ndarray, ys: np.ndarray):
+    """Raw samples -> packed network inputs [n][H][W][11] and targets [n][H][W][3], each group
+    divided by its own root mean square."""
+    s = group_scales(xs)
+    inv = np.where(s > 0, 1.0 / np.where(s > 0, s, 1.0), 0.0)
+    x = np.stack([xs[..., PACKED_SOURCE[k]] * inv[:, PACKED_GROUP[k], None, None] for k in range(len(PACKED_SOURCE))], axis=-1)
+    y = ys * inv[:, None, None, :]
+    return x, y
+
+
+def to_device(xs: np.ndarray, ys: np.ndarray, device: str = "cuda"):
+    """Packed samples -> BF16 inputs [n][H][W][16] and FP32 targets [n][H][W][3] on the device."""
+    n, H, W, c = xs.shape
+    x = torch.zeros((n, H, W, LAYERS[0][0]), dtype=torch.float32)
+    x[..., :c] = torch.from_numpy(xs.astype(np.float32))
+    return x.to(device=device, dtype=torch.bfloat16), torch.from_numpy(ys.astype(np.float32)).to(device)
+
+
+def train(net: GuessNet, x: torch.Tensor, y: torch.Tensor, steps: int, batch: int = 8, lr: float = 2e-3, seed: int = 0,
+          log_every: int = 0):
+    """Adam with a cosine learning-rate decay over random mini-batches.  The targets are divided by
+    their per-component root mean square over the samples while training, and that factor is then
+    folded into the last layer.  Returns the loss history [(step, loss)] on the scaled targets."""
+    sigma = torch.sqrt(torch.mean(y.double() ** 2, dim=(0, 1, 2))).clamp_min(1e-300)
+    ys = (y / sigma.float()).contiguous()
+    tr = Trainer(net, lr=lr)
+    rng = np.random.Generator(np.random.Philox(seed))
+    hist = []
+    n = x.shape[0]
+    for it in range(steps):
+        idx = torch.from_numpy(rng.choice(n, size=min(batch, n), replace=False)).to(x.device)
+        lr_t = 0.5 * lr * (1.0 + math.cos(math.pi * it / steps))
+        loss = tr.step(x.index_select(0, idx).contiguous(), ys.index_select(0, idx).contiguous(), lr=lr_t)
+        if log_every and (it % log_every == 0 or it == steps - 1):
+            hist.append((it, float(loss.item())))
+    flat = net.host_params()
+    wo, bo, cin, cout = OFFSETS[-1]
+    s = sigma.cpu().numpy()
+    w = flat[wo:bo].reshape(9, cout, cin)
+    w[:, :NOUT, :] *= s[None, :, None]
+    flat[bo:bo + NOUT] *= s
+    net.load_params(flat)
+    return hist

@@ -302,11 +302,11 @@ __global__ void k_sum_in_order(const double *__restrict__ partial, int n, double
 }
 
 // Adam on the FP32 master parameters (bias-corrected step size precomputed on the host).
-__global__ void k_adam(float *__restrict__ p, const float *__restrict__ gr, float *__restrict__ m, float *__restrict__ v, long long n,
-                       float lr_t, float b1, float b2, float eps)
+__global__ void k_adam(float *__restrict__ p, const float *__restrict__ gr, const float *__restrict__ mask, float *__restrict__ m,
+                       float *__restrict__ v, long long n, float lr_t, float b1, float b2, float eps)
 {
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const float gg = gr[e];
+        const float gg = mask ? gr[e] * mask[e] : gr[e];
         const float mm = b1 * m[e] + (1.f - b1) * gg;
         const float vv = b2 * v[e] + (1.f - b2) * gg * gg;
         m[e] = mm;
@@ -369,47 +369,62 @@ int launch_wgrad(const void *x, const void *dz, int nimg, int H, int W, int cout
 bool shape_ok(int nimg, int H, int W) { return nimg > 0 && H >= TH && W >= TWD && H % TH == 0 && W % TWD == 0; }
 
 // ---------------------------------------------------------------- inference inside the solve
-// Network input at cell (i, j): the Yee values (Ex, Ey, Ez, Bx, By, Bz, Jx, Jy, Jz) stored at
-// ghosted index (i+2, j+2), divided by their root mean square s over the grid.  The problem is
-// linear in these inputs, so the guess is s * net(input / s).
-__device__ __forceinline__ double guess_input(const FView<6, false> &uf, const FView<3, false> &uj, int c, int ix, int iy)
+// The CG unknowns decouple: dBx depends on (Bx, Ez, Jz) only, dBy on (By, Ez, Jz), dBz on (Bz, Ex,
+// Ey, Jx, Jy) (the right-hand side of field.f90:125-146 and a diagonal operator per component).
+// Input channels, each group divided by its own root mean square s_k over the grid:
+//   0-2 (Bx, Ez, Jz)/s_x, 3-5 (By, Ez, Jz)/s_y, 6-10 (Bz, Ex, Ey, Jx, Jy)/s_z, 11-15 zero,
+// read at each cell's stored Yee index (i+2, j+2).  The network's weights are block-diagonal over
+// the three groups, so the guess is (s_x, s_y, s_z) * net(input), exact in scale per component.
+constexpr int GUESS_NIN = 11;
+__device__ __forceinline__ double raw_input(const FView<6, false> &uf, const FView<3, false> &uj, int c, int ix, int iy)
 {
+    // c: 0-2 Ex, Ey, Ez; 3-5 Bx, By, Bz; 6-8 Jx, Jy, Jz
     if (c < 3) return uf(3 + c, ix, iy);
     if (c < 6) return uf(c - 3, ix, iy);
     return uj(c - 6, ix, iy);
 }
+__device__ __forceinline__ int packed_source(int k)
+{
+    constexpr int src[GUESS_NIN] = {3, 2, 8, 4, 2, 8, 5, 0, 1, 6, 7};
+    return src[k];
+}
+__device__ __forceinline__ int packed_group(int k) { return k < 3 ? 0 : (k < 6 ? 1 : 2); }
 
 __global__ void k_guess_sumsq(WmGeom g, FView<6, false> uf, FView<3, false> uj, double *__restrict__ partial)
 {
-    __shared__ double red[256];
+    __shared__ double red[3][256];
     const long long ncell = (long long)g.nx * g.ny;
-    double s = 0.0;
+    double s[3] = {0.0, 0.0, 0.0};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
         const int ix = (int)(e % g.nx) + 2, iy = (int)(e / g.nx) + 2;
 #pragma unroll
-        for (int c = 0; c < 9; ++c) {
-            const double v = guess_input(uf, uj, c, ix, iy);
-            s += v * v;
+        for (int k = 0; k < GUESS_NIN; ++k) {
+            const double v = raw_input(uf, uj, packed_source(k), ix, iy);
+            s[packed_group(k)] += v * v;
         }
     }
-    red[threadIdx.x] = s;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) red[q][threadIdx.x] = s[q];
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        if (threadIdx.x < w)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
         __syncthreads();
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+    if (threadIdx.x < 3) partial[3 * blockIdx.x + threadIdx.x] = red[threadIdx.x][0];
 }
 
-// scale[0] = s (root mean square), scale[1] = 1/s (0 for an all-zero input)
-__global__ void k_guess_scale(const double *__restrict__ partial, int n, double count, double *__restrict__ scale)
+// scale[k] = s_k (root mean square of group k), scale[3+k] = 1/s_k (0 for an all-zero group)
+__global__ void k_guess_scale(const double *__restrict__ partial, int n, long long ncell, double *__restrict__ scale)
 {
-    if (threadIdx.x == 0 && blockIdx.x == 0) {
+    if (blockIdx.x == 0 && threadIdx.x < 3) {
+        const int q = threadIdx.x;
         double t = 0.0;
-        for (int k = 0; k < n; ++k) t += partial[k];
-        const double s = sqrt(t / count);
-        scale[0] = s;
-        scale[1] = s > 0.0 ? 1.0 / s : 0.0;
+        for (int k = 0; k < n; ++k) t += partial[3 * k + q];
+        const double s = sqrt(t / ((q == 2 ? 5.0 : 3.0) * (double)ncell));
+        scale[q] = s;
+        scale[3 + q] = s > 0.0 ? 1.0 / s : 0.0;
     }
 }
 
@@ -417,14 +432,15 @@ __global__ void k_guess_pack(WmGeom g, FView<6, false> uf, FView<3, false> uj, c
                              __nv_bfloat16 *__restrict__ x)
 {
     const long long ncell = (long long)g.nx * g.ny;
-    const double inv = scale[1];
+    const double inv[3] = {scale[3], scale[4], scale[5]};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
         const int ix = (int)(e % g.nx) + 2, iy = (int)(e / g.nx) + 2;
         unsigned w[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const float lo = 2 * k < 9 ? (float)(guess_input(uf, uj, 2 * k, ix, iy) * inv) : 0.f;
-            const float hi = 2 * k + 1 < 9 ? (float)(guess_input(uf, uj, 2 * k + 1, ix, iy) * inv) : 0.f;
+            const int c0 = 2 * k, c1 = 2 * k + 1;
+            const float lo = c0 < GUESS_NIN ? (float)(raw_input(uf, uj, packed_source(c0), ix, iy) * inv[packed_group(c0)]) : 0.f;
+            const float hi = c1 < GUESS_NIN ? (float)(raw_input(uf, uj, packed_source(c1), ix, iy) * inv[packed_group(c1)]) : 0.f;
             const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
             w[k] = *reinterpret_cast<const unsigned *>(&v);
         }
@@ -434,14 +450,14 @@ __global__ void k_guess_pack(WmGeom g, FView<6, false> uf, FView<3, false> uj, c
     }
 }
 
-// cand[l][j*nx + i] = s * pred(j, i, l), l = dBx, dBy, dBz
+// cand[l][j*nx + i] = s_l * pred(j, i, l), l = dBx, dBy, dBz
 __global__ void k_guess_unpack(WmGeom g, const float *__restrict__ pred, const double *__restrict__ scale, double *__restrict__ cand)
 {
     const long long ncell = (long long)g.nx * g.ny;
-    const double s = scale[0];
+    const double s[3] = {scale[0], scale[1], scale[2]};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
 #pragma unroll
-        for (int l = 0; l < 3; ++l) cand[l * ncell + e] = s * (double)pred[e * 8 + l];
+        for (int l = 0; l < 3; ++l) cand[l * ncell + e] = s[l] * (double)pred[e * 8 + l];
     }
 }
 
@@ -474,7 +490,7 @@ int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf,
     const int blocks = (int)std::min<long long>((ncell + 255) / 256, WM_CNN_RED_BLOCKS);
     k_guess_sumsq<<<blocks, 256, 0, st>>>(g, uf, uj, w.partial);
     WM_TRY(wm_check_launch("k_guess_sumsq"));
-    k_guess_scale<<<1, 32, 0, st>>>(w.partial, blocks, 9.0 * (double)ncell, w.scale);
+    k_guess_scale<<<1, 32, 0, st>>>(w.partial, blocks, ncell, w.scale);
     WM_TRY(wm_check_launch("k_guess_scale"));
     k_guess_pack<<<blocks, 256, 0, st>>>(g, uf, uj, w.scale, static_cast<__nv_bfloat16 *>(w.x));
     WM_TRY(wm_check_launch("k_guess_pack"));
@@ -538,15 +554,15 @@ int wm_cnn_mse(const float *pred, const float *target, long long npix, void *dz,
     return wm_check_launch("k_sum_in_order");
 }
 
-int wm_cnn_adam(float *p, const float *grad, float *m, float *v, long long n, float lr, float beta1, float beta2, float eps, int step,
-                void *stream)
+int wm_cnn_adam(float *p, const float *grad, const float *mask, float *m, float *v, long long n, float lr, float beta1, float beta2,
+                float eps, int step, void *stream)
 {
     if (!p || !grad || !m || !v || n <= 0 || step < 1) return WM_ERR_BAD_ARG;
     const double bc1 = 1.0 - std::pow((double)beta1, step), bc2 = 1.0 - std::pow((double)beta2, step);
     const float lr_t = (float)(lr * std::sqrt(bc2) / bc1);
     const float eps_t = (float)(eps * std::sqrt(bc2));
     const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 8);
-    k_adam<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(p, grad, m, v, n, lr_t, beta1, beta2, eps_t);
+    k_adam<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(p, grad, mask, m, v, n, lr_t, beta1, beta2, eps_t);
     return wm_check_launch("k_adam");
 }
 

@@ -323,13 +323,16 @@ __global__ void __launch_bounds__(CG_THREADS) k_guess_resid(WmGeom g, FieldK fk,
 
 // Start each component from the candidate where its residual is the smaller one.
 template <class FV6>
-__global__ void k_guess_pick(WmGeom g, FV6 df, const double *__restrict__ cand, double *stats)
+__global__ void k_guess_pick(WmGeom g, FV6 df, const double *__restrict__ cand, const CgScal *scal, double *stats)
 {
     const long long ncell = (long long)g.nx * g.ny;
     bool take[3];
 #pragma unroll
     for (int l = 0; l < 3; ++l) take[l] = stats[l] < stats[3 + l];
-    if (blockIdx.x == 0 && threadIdx.x < 3) stats[6 + threadIdx.x] = take[threadIdx.x] ? 1.0 : 0.0;
+    if (blockIdx.x == 0 && threadIdx.x < 3) {
+        stats[6 + threadIdx.x] = take[threadIdx.x] ? 1.0 : 0.0;
+        stats[9 + threadIdx.x] = scal[threadIdx.x].sum_g;
+    }
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
         const int ix = (int)(e % g.nx) + 2, iy = (int)(e / g.nx) + 2;
 #pragma unroll
@@ -583,7 +586,7 @@ int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<
         const PlaneView cv{guess->cand, g.nx, g.ny};
         k_guess_resid<PlaneView><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, cv, w.b, w.partial, w.ticket, guess->stats);
         k_guess_resid<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.b, w.partial, w.ticket, guess->stats + 3);
-        k_guess_pick<FView<6, false>><<<grid_for((long long)g.nx * g.ny, 256), 256, 0, st>>>(g, df, guess->cand, guess->stats);
+        k_guess_pick<FView<6, false>><<<grid_for((long long)g.nx * g.ny, 256), 256, 0, st>>>(g, df, guess->cand, w.scal, guess->stats);
         WM_TRY(wm_check_launch("k_guess_pick"));
         nl += 3;
     }

@@ -64,8 +64,8 @@ int wm_launch_aos_to_soa(int nc, long long npts, const double *a, double *s, cud
 int wm_launch_soa_to_aos(int nc, long long npts, const double *s, double *a, cudaStream_t st);
 // Optional initial guess for the CG: run() writes cand ([3][nx*ny], x fastest) from uf and the
 // folded uj; the solve then starts each component from whichever of cand and the previous dB has
-// the smaller residual.  stats (device, 9 doubles): |b - A cand|^2 [3], |b - A dB_prev|^2 [3],
-// 1.0 where cand was taken [3].
+// the smaller residual.  stats (device, 12 doubles): |b - A cand|^2 [3], |b - A dB_prev|^2 [3],
+// 1.0 where cand was taken [3], |b|^2 [3].
 struct WmGuess {
     int (*run)(void *ctx, cudaStream_t st);
     void *ctx;
@@ -103,8 +103,8 @@ struct WmCnnNet {
 struct WmCnnWork {
     void *x, *a0, *a1;  // BF16 [ny][nx][16], [ny][nx][48] x 2
     float *pred;        // FP32 [ny][nx][8]
-    double *partial;    // WM_CNN_RED_BLOCKS
-    double *scale;      // 2
+    double *partial;    // 3 * WM_CNN_RED_BLOCKS
+    double *scale;      // 6
 };
 size_t wm_cnn_param_count();
 int wm_cnn_net_prepare(WmCnnNet &net, cudaStream_t st);

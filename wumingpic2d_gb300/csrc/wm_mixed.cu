@@ -46,27 +46,26 @@ __device__ __forceinline__ unsigned lanemask_lt()
     return m;
 }
 
-// Predicated global access: the loop body stays free of branches, and lanes past the end of their
-// cell neither read nor write.
-__device__ __forceinline__ float ld_if(const float *ptr, bool pred, float dflt)
+// Asynchronous copy of one float into shared memory; nbytes = 0 writes a zero and reads nothing.
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, unsigned nbytes)
 {
-    float v = dflt;
-    asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.global.nc.f32 %0, [%1];\n\t}" : "+f"(v) : "l"(ptr), "r"((unsigned)pred));
-    return v;
-}
-__device__ __forceinline__ void st_if(float *ptr, float v, bool pred)
-{
-    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.f32 [%0], %1;\n\t}" ::"l"(ptr), "f"(v), "r"((unsigned)pred)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src), "r"(nbytes)
                  : "memory");
 }
-__device__ __forceinline__ void st_if(int *ptr, int v, bool pred)
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// The pushed particle's five components, its destination key and row direction, stored only by
+// lanes that hold a particle (one predicate for the seven stores: the loop body has no branches).
+__device__ __forceinline__ void store_particle(const MixedView &b, long long p, float x, float y, float ux, float uy, float uz, int *key,
+                                               int kk, unsigned char *dir, unsigned dv, bool pred)
 {
-    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.s32 [%0], %1;\n\t}" ::"l"(ptr), "r"(v), "r"((unsigned)pred)
-                 : "memory");
-}
-__device__ __forceinline__ void st_if(unsigned char *ptr, unsigned v, bool pred)
-{
-    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.u8 [%0], %1;\n\t}" ::"l"(ptr), "r"(v), "r"((unsigned)pred)
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t"
+                 "@q st.global.f32 [%1], %2;\n\t@q st.global.f32 [%3], %4;\n\t@q st.global.f32 [%5], %6;\n\t"
+                 "@q st.global.f32 [%7], %8;\n\t@q st.global.f32 [%9], %10;\n\t@q st.global.s32 [%11], %12;\n\t"
+                 "@q st.global.u8 [%13], %14;\n\t}"
+                 ::"r"((unsigned)pred), "l"(b.x + p), "f"(x), "l"(b.y + p), "f"(y), "l"(b.ux + p), "f"(ux), "l"(b.uy + p), "f"(uy),
+                 "l"(b.uz + p), "f"(uz), "l"(key + p), "r"(kk), "l"(dir + p), "r"(dv)
                  : "memory");
 }
 
@@ -88,8 +87,9 @@ __global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__
 }
 
 // One CTA per (tile of 64 cells, row, species); 4 lanes per cell.  The loop body has no branches:
-// a lane past the end of its cell runs on a dummy particle with zero deposit weights and its loads
-// and stores switched off.
+// a lane past the end of its cell runs on a zero particle with zero deposit weights and its stores
+// switched off.  Each lane's next particle is copied into shared memory (cp.async) while the
+// current one is pushed.
 __global__ void __launch_bounds__(MX_THREADS, 2)
     k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const float *__restrict__ fcc, const int *__restrict__ cumcnt,
                          int *__restrict__ key, unsigned char *__restrict__ dir, int *__restrict__ cellcnt,
@@ -99,6 +99,7 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
     __shared__ float cellpj[65][MX_PW];                   // per-cell partials; first holds the node rows
     __shared__ int cc[MX_TW + 1];
     __shared__ float spc[5];
+    __shared__ float pbuf[2][5][MX_THREADS];  // each lane's next particle, double-buffered
     float(*tmp)[3][MX_TW + 2] = reinterpret_cast<float(*)[3][MX_TW + 2]>(&cellpj[0][0]);
     static_assert(6 * 3 * (MX_TW + 2) <= 65 * MX_PW, "node rows fit in the partials buffer");
     const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
@@ -164,11 +165,29 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
             az[jp][ip] = 0.f;
         }
     unsigned bad = 0;
+    // lane's particle of iteration it -> pbuf[it & 1]; a lane past its cell copies zeros
+    auto prefetch = [&](int it) {
+        const bool v = it < nmine;
+        const long long q = v ? rbase + s_beg + sub + (long long)it * MX_LPC : 0;
+        const unsigned nb = v ? 4u : 0u;
+        float(*dst)[MX_THREADS] = pbuf[it & 1];
+        cp_async4(&dst[0][tid], a.x + q, nb);
+        cp_async4(&dst[1][tid], a.y + q, nb);
+        cp_async4(&dst[2][tid], a.ux + q, nb);
+        cp_async4(&dst[3][tid], a.uy + q, nb);
+        cp_async4(&dst[4][tid], a.uz + q, nb);
+        cp_async_commit();
+    };
+    if (nwarp > 0) prefetch(0);
     for (int it = 0; it < nwarp; ++it) {
         const bool valid = it < nmine;
         const long long p = rbase + s_beg + sub + (long long)it * MX_LPC;
-        const float dx = ld_if(a.x + p, valid, 0.5f), dy = ld_if(a.y + p, valid, 0.5f);
-        float u1 = ld_if(a.ux + p, valid, 0.f), u2 = ld_if(a.uy + p, valid, 0.f), u3 = ld_if(a.uz + p, valid, 0.f);
+        if (it + 1 < nwarp) prefetch(it + 1);
+        else cp_async_commit();  // an empty group keeps the wait count uniform
+        cp_async_wait1();
+        const float(*src)[MX_THREADS] = pbuf[it & 1];
+        const float dx = src[0][tid], dy = src[1][tid];
+        float u1 = src[2][tid], u2 = src[3][tid], u3 = src[4][tid];
         float sx0, sx1, sx2, sy0, sy1, sy2;
         shape3(dx - 0.5f, sx0, sx1, sx2);
         shape3(dy - 0.5f, sy0, sy1, sy2);
@@ -270,18 +289,12 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
 #pragma unroll
             for (int m = 0; m < 4; ++m) ay[m][ip] = fmaf(fx, cy[m], ay[m][ip]);
         }
-        st_if(b.x + p, nx1, valid);
-        st_if(b.y + p, ny1, valid);
-        st_if(b.ux + p, u1, valid);
-        st_if(b.uy + p, u2, valid);
-        st_if(b.uz + p, u3, valid);
         int ci = cg + incx;
         ci = ci < 0 ? ci + g.nx : (ci >= g.nx ? ci - g.nx : ci);
         int kr = jr + incy;
         kr = kr < 0 ? kr + g.ny : (kr >= g.ny ? kr - g.ny : kr);
         const int kk = valid ? (isp * g.ny + kr) * g.nx + ci : -1;
-        st_if(key + p, kk, valid);
-        st_if(dir + p, incy == 1 ? 1u : (incy == -1 ? 2u : 0u), valid);
+        store_particle(b, p, nx1, ny1, u1, u2, u3, key, kk, dir, incy == 1 ? 1u : (incy == -1 ? 2u : 0u), valid);
         // cell counts for the sort, aggregated over the lanes that share a destination
         const unsigned peers = __match_any_sync(FULL, kk);
         if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&cellcnt[kk], __popc(peers));

@@ -714,11 +714,11 @@ int wm_sim_set_guess(wm_sim *s, const float *params, long long nparams)
     WM_TRY(s->cnn_a0.ensure(2 * 48 * ncell));
     WM_TRY(s->cnn_a1.ensure(2 * 48 * ncell));
     WM_TRY(s->cnn_pred.ensure(sizeof(float) * 8 * ncell));
-    WM_TRY(s->cnn_partial.ensure(sizeof(double) * WM_CNN_RED_BLOCKS));
-    WM_TRY(s->cnn_scale.ensure(sizeof(double) * 2));
+    WM_TRY(s->cnn_partial.ensure(sizeof(double) * 3 * WM_CNN_RED_BLOCKS));
+    WM_TRY(s->cnn_scale.ensure(sizeof(double) * 6));
     WM_TRY(s->guess_cand.ensure(sizeof(double) * 3 * ncell));
-    WM_TRY(s->guess_stats.ensure(sizeof(double) * 9));
-    WM_CUDA(cudaMemsetAsync(s->guess_stats.p, 0, sizeof(double) * 9, s->st));
+    WM_TRY(s->guess_stats.ensure(sizeof(double) * 12));
+    WM_CUDA(cudaMemsetAsync(s->guess_stats.p, 0, sizeof(double) * 12, s->st));
     WM_CUDA(cudaMemcpyAsync(s->cnn_params.p, params, sizeof(float) * nparams, cudaMemcpyHostToDevice, s->st));
     s->net.params = s->cnn_params.as<float>();
     WM_TRY(wm_cnn_net_prepare(s->net, s->st));
@@ -728,11 +728,11 @@ int wm_sim_set_guess(wm_sim *s, const float *params, long long nparams)
     return WM_OK;
 }
 
-int wm_sim_guess_stats(wm_sim *s, double *stats9)
+int wm_sim_guess_stats(wm_sim *s, double *stats)
 {
-    if (!s || !stats9) return WM_ERR_BAD_ARG;
+    if (!s || !stats) return WM_ERR_BAD_ARG;
     if (!s->guess_on) return WM_ERR_NOT_INIT;
-    WM_CUDA(cudaMemcpyAsync(stats9, s->guess_stats.p, sizeof(double) * 9, cudaMemcpyDeviceToHost, s->st));
+    WM_CUDA(cudaMemcpyAsync(stats, s->guess_stats.p, sizeof(double) * 12, cudaMemcpyDeviceToHost, s->st));
     WM_CUDA(cudaStreamSynchronize(s->st));
     return WM_OK;
 }

@@ -49,6 +49,27 @@ class Simulation:
               "wm_sim_store")
         return up, uf, np2, cumcnt
 
+    def fields(self) -> np.ndarray:
+        """The current fields uf in the reference layout (6, nx+4, ny+4)."""
+        uf = self.dims.alloc_uf()
+        check(lib().wm_sim_store(self._h, None, uf.ctypes.data, None, None), "wm_sim_store")
+        return uf
+
+    def set_guess(self, params) -> None:
+        """Start each step's CG from the learned network's dB where it beats the previous step's
+        (params: the network's flat FP32 parameters), or switch that off (None)."""
+        if params is None:
+            check(lib().wm_sim_set_guess(self._h, None, 0), "wm_sim_set_guess")
+            return
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        check(lib().wm_sim_set_guess(self._h, p.ctypes.data, p.size), "wm_sim_set_guess")
+
+    def guess_stats(self) -> np.ndarray:
+        """Last step: |b - A dB_net|^2 (3), |b - A dB_prev|^2 (3), network guess taken (3), |b|^2 (3)."""
+        out = np.zeros(12)
+        check(lib().wm_sim_guess_stats(self._h, out.ctypes.data), "wm_sim_guess_stats")
+        return out
+
     def step(self, nsteps: int = 1) -> None:
         check(lib().wm_sim_step(self._h, int(nsteps)), "wm_sim_step")
 
