@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--cpu-rows", type=int, default=64, help="rows of the CPU sample strip")
+    p.add_argument("--guess", default=os.path.join(ROOT, "wumingpic2d_gb300", "guess_weibel.npz"),
+                   help="trained CG-guess network (wumingpic2d_gb300.train_guess); 'none' skips the learned-guess leg")
     p.add_argument("--cpu-steps", type=int, default=2)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -258,20 +260,53 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
         unpin(up_h)
         unpin(uf_h)
         del up_h
+
+    # the same loop with the learned CG initial guess (each component starts from the better of the
+    # network's dB and the previous step's; same tolerance)
+    guess = None
+    if precision == "mixed" and args.guess != "none" and os.path.exists(args.guess):
+        sim.set_guess(np.load(args.guess)["params"])
+        sim.step(2)
+        sim.set_timing(True)
+        dist.barrier()
+        ms_g = dist.max(sim.step_timed(args.steps))
+        kt_g = sim.kernel_times()
+        st = sim.guess_stats()
+        sim.set_timing(False)
+        guess = {"value": dist.sum(float(ntot)) * args.steps / (ms_g / 1e3), "unit": UNIT, "ms_per_step": ms_g / args.steps,
+                 "cg_iters_last_step": sim.cg_iters().tolist(), "cg_iters_previous_step_guess": iters,
+                 "initial_relative_residual": {"network": np.sqrt(st[0:3] / st[9:12]).round(4).tolist(),
+                                               "previous_step": np.sqrt(st[3:6] / st[9:12]).round(4).tolist()},
+                 "guess_net_ms_per_step": round(kt_g.get("guess_net", 0.0) / args.steps, 3),
+                 "cg_iterate_ms_per_step": round(kt_g.get("cg_iterate", 0.0) / args.steps, 3),
+                 "weights": os.path.relpath(args.guess, ROOT)}
     sim.close()
     return dict(ntot=ntot, ms=ms_max, value=value, launches=launches, ktimes=ktimes, iters=iters, clocks=clk, e2e=e2e,
-                dev_bytes=dev_bytes, t_init=t_init, d=d, cfg=cfg, precision=precision)
+                dev_bytes=dev_bytes, t_init=t_init, d=d, cfg=cfg, precision=precision, guess=guess)
 
 
 # Algorithmic bytes per particle of the particle kernels.  FP64: 8 B per component (push reads and
 # writes x, y, u; the deposit reads old x, y and new x, y, u; the sort moves 6 components).  Mixed:
-# the fused push+deposit reads and writes 5 FP32 components and writes the 5-byte rebin key and
-# direction; the sort moves 5 FP32 components and the i64 pid.
+# the fused push+deposit reads and writes 5 FP32 components and writes the 4-byte move code; the
+# move reads the code and moves 5 FP32 components and the i64 pid.
 ALGO_BYTES = {"fp64": {"push": 80, "deposit": 56, "sort_move": 96},
-              "mixed": {"push_deposit": 45, "sort_move": 56}}
+              "mixed": {"push_deposit": 44, "sort_move": 60}}
 
 
-def roofline(res, args):
+def all_rooflines(res, args):
+    """achieved GB/s and fraction of the measured HBM peak for every particle kernel"""
+    peaks, _ = measured_peaks()
+    out = {}
+    for name, b in ALGO_BYTES[res["precision"]].items():
+        t = res["ktimes"].get(name)
+        if t:
+            gbs = b * res["ntot"] / (t / args.steps / 1e3) / 1e9
+            out[name] = {"achieved": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4), "bytes_per_particle": b,
+                         "ms_per_launch": round(t / args.steps, 3)}
+    return out
+
+
+def roofline(res, args, name=None):
     peaks, src = measured_peaks()
     kt = res["ktimes"]
     steps = args.steps
@@ -280,7 +315,7 @@ def roofline(res, args):
     cand = {k: v for k, v in kt.items() if k in algo}
     if not cand:
         return None
-    name = max(cand, key=cand.get)
+    name = name or max(cand, key=cand.get)
     t = cand[name] / steps / 1e3
     achieved = algo[name] * ntot / t / 1e9
     tr = ncu_traffic().get(f"{res['precision']}:{name}")
@@ -341,7 +376,10 @@ def main():
             "clocks": res["clocks"],
             "device_bytes": res["dev_bytes"],
             "setup_s": round(res["t_init"], 1),
+            "rooflines": all_rooflines(res, args),
         }
+        if res.get("guess") is not None:
+            line["learned_guess"] = res["guess"]
         if other is not None:
             line["fp64_path"] = {"value": other["value"], "unit": UNIT, "ms_per_step": other["ms"] / args.steps,
                                  "speedup_of_mixed": res["value"] / other["value"],

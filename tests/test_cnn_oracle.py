@@ -108,3 +108,18 @@ def test_network_mask_is_block_diagonal_and_scales_are_per_group():
     ys2[..., 2] *= 1e3
     x2, y2 = cnn.normalise(xs2, ys2)
     assert np.allclose(x1, x2) and np.allclose(y1, y2)
+
+
+def test_shipped_guess_weights_are_block_diagonal():
+    import json
+    from pathlib import Path
+
+    from wumingpic2d_gb300 import cnn
+
+    z = np.load(Path(cnn.__file__).with_name("guess_weibel.npz"))
+    params = z["params"]
+    assert params.shape == (cnn.NPARAMS,) and params.dtype == np.float32 and np.all(np.isfinite(params))
+    assert not (params * (1 - cnn.param_mask())).any()
+    meta = json.loads(str(z["meta"]))
+    held = meta["cg_iterations_held_out"]
+    assert held["1e-06"]["learned"] < held["1e-06"]["previous_step"]

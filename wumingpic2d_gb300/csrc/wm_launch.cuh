@@ -83,8 +83,14 @@ int wm_mixed_ntiles(const WmGeom &g);
 size_t wm_mixed_jtile_floats(const WmGeom &g);
 size_t wm_mixed_fcc_floats(const WmGeom &g);
 int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cudaStream_t st);
+// sc.key receives each particle's move code (rank << 4 | direction), cnt9 [cells][9] the per-cell
+// direction counts; k_mixed_incoming turns them into destination counts (sc.cellcnt) and offsets
+// off9 [cells][9]; k_mixed_move writes the new cell-sorted order.
 int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const float *fcc,
-                                 const int *cumcnt, const WmRebinScratch &sc, float *jtile, cudaStream_t st);
+                                 const int *cumcnt, const WmRebinScratch &sc, int *cnt9, float *jtile, cudaStream_t st);
+int wm_launch_mixed_incoming(const WmGeom &g, const int *cnt9, int *off9, const WmRebinScratch &sc, cudaStream_t st);
+int wm_launch_mixed_move(const WmGeom &g, MixedView src, MixedView dst, const int *cumcnt_old, const int *cumcnt_new, const int *off9,
+                         const WmRebinScratch &sc, cudaStream_t st);
 int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> uj, cudaStream_t st);
 int wm_launch_mixed_unpack(const WmGeom &g, const double *stage, int pitch, const int *np2, MixedView dst, const WmRebinScratch &sc,
                            cudaStream_t st);

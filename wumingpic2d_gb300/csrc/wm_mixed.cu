@@ -6,13 +6,15 @@
 // does, for one (species, row, 64-cell tile): the Buneman-Boris push of particle.f90:96-161 in
 // FP32, the Esirkepov deposit of field.f90:224-298 in FP32, the periodic wrap of
 // boundary_periodic.f90:61-96 and :143-165 as integer cell arithmetic, and the destination cell key
-// and row direction the rebin needs.  Four lanes share a cell and read its particles in 16-byte
-// runs straight from global memory; each lane reads the cell's 3x3x6 field stencil with 128-bit
-// shared loads and keeps the cell's 5x5x3 partial currents in registers (the cell's particles all
-// deposit on the same 5x5 nodes); the four lanes add theirs with shuffles, and the tile's node
-// currents are summed from the per-cell partials in a fixed order.  Tile currents go to a per-tile
-// buffer; k_mixed_jfold adds them into the FP64 global J node by node in a fixed order, so the
-// result is deterministic and no atomics touch the currents.
+// and row direction the rebin needs.  Four lanes share a cell; each lane's next particle is copied
+// into shared memory (cp.async) while the current one is pushed.  The TSC-weighted 3x3 gather of
+// each field is a biquadratic in the particle's offsets, so the kernel stages its nine
+// coefficients per cell and field and evaluates it by Horner's rule, two fields per packed
+// fma.rn.f32x2.  Each lane keeps the cell's 5x5x3 partial currents in registers (the cell's
+// particles all deposit on the same 5x5 nodes); the four lanes add theirs with shuffles, and the
+// tile's node currents are summed from the per-cell partials in a fixed order.  Tile currents go
+// to a per-tile buffer; k_mixed_jfold adds them into the FP64 global J node by node in a fixed
+// order, so the result is deterministic and no atomics touch the currents.
 #include <algorithm>
 
 #include "wm_launch.cuh"
@@ -39,6 +41,24 @@ __device__ __forceinline__ void shape3(float h, float &a0, float &a1, float &a2)
     a2 = 0.5f * (0.5f + h) * (0.5f + h);
 }
 
+// Two FP32 values in one 64-bit register pair, and the packed FMA of sm_100+ on such pairs.
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void unpack2(unsigned long long r, float &lo, float &hi)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(r));
+}
+__device__ __forceinline__ unsigned long long fma2(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt()
 {
     unsigned m;
@@ -55,17 +75,16 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src, unsigned
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
-// The pushed particle's five components, its destination key and row direction, stored only by
-// lanes that hold a particle (one predicate for the seven stores: the loop body has no branches).
-__device__ __forceinline__ void store_particle(const MixedView &b, long long p, float x, float y, float ux, float uy, float uz, int *key,
-                                               int kk, unsigned char *dir, unsigned dv, bool pred)
+// The pushed particle's five components and its move code, stored only by lanes that hold a
+// particle (one predicate for the six stores: the loop body has no branches).
+__device__ __forceinline__ void store_particle(const MixedView &b, long long p, float x, float y, float ux, float uy, float uz,
+                                               unsigned *code, unsigned cv, bool pred)
 {
     asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t"
                  "@q st.global.f32 [%1], %2;\n\t@q st.global.f32 [%3], %4;\n\t@q st.global.f32 [%5], %6;\n\t"
-                 "@q st.global.f32 [%7], %8;\n\t@q st.global.f32 [%9], %10;\n\t@q st.global.s32 [%11], %12;\n\t"
-                 "@q st.global.u8 [%13], %14;\n\t}"
+                 "@q st.global.f32 [%7], %8;\n\t@q st.global.f32 [%9], %10;\n\t@q st.global.u32 [%11], %12;\n\t}"
                  ::"r"((unsigned)pred), "l"(b.x + p), "f"(x), "l"(b.y + p), "f"(y), "l"(b.ux + p), "f"(ux), "l"(b.uy + p), "f"(uy),
-                 "l"(b.uz + p), "f"(uz), "l"(key + p), "r"(kk), "l"(dir + p), "r"(dv)
+                 "l"(b.uz + p), "f"(uz), "l"(code + p), "r"(cv)
                  : "memory");
 }
 
@@ -92,9 +111,9 @@ __global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__
 // current one is pushed.
 __global__ void __launch_bounds__(MX_THREADS, 2)
     k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const float *__restrict__ fcc, const int *__restrict__ cumcnt,
-                         int *__restrict__ key, unsigned char *__restrict__ dir, int *__restrict__ cellcnt,
-                         float *__restrict__ jtile, unsigned *status)
+                         unsigned *__restrict__ code, int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status)
 {
+    __shared__ int dcnt[MX_TW][9];  // per cell: particles so far that move in direction d
     __shared__ __align__(16) float fcell[MX_TW][MX_FS];  // [cell][(b*3 + a)*6 + m]
     __shared__ float cellpj[65][MX_PW];                   // per-cell partials; first holds the node rows
     __shared__ int cc[MX_TW + 1];
@@ -131,10 +150,26 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
             }
     }
     __syncthreads();
-    // each cell's 3x3 stencil of the six fields, stencil position major
-    for (int e = tid; e < MX_TW * 54; e += MX_THREADS) {
-        const int c = e / 54, k = e % 54, r = k / 6, m = k % 6;
-        fcell[c][k] = c < ncell ? tmp[m][r / 3][c + r % 3] : 0.f;
+    // Each cell's six fields as biquadratics in the centred offsets hx, hy of particle.f90:96-129:
+    // sum_ab T(a,b) sx_a(hx) sy_b(hy) = sum_pq C(q,p) hx^p hy^q, with the TSC weights
+    // sx = (1/8 - hx/2 + hx^2/2, 3/4 - hx^2, 1/8 + hx/2 + hx^2/2).  Stored [(q*3 + p)*6 + m].
+    for (int e = tid; e < MX_TW * 6; e += MX_THREADS) {
+        const int c = e / 6, m = e % 6;
+        float P[3][3];  // row b: coefficients of hx^0, hx^1, hx^2
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const float t0 = c < ncell ? tmp[m][b][c] : 0.f, t1 = c < ncell ? tmp[m][b][c + 1] : 0.f,
+                        t2 = c < ncell ? tmp[m][b][c + 2] : 0.f;
+            P[b][0] = 0.125f * t0 + 0.75f * t1 + 0.125f * t2;
+            P[b][1] = 0.5f * (t2 - t0);
+            P[b][2] = 0.5f * t0 - t1 + 0.5f * t2;
+        }
+#pragma unroll
+        for (int p = 0; p < 3; ++p) {
+            fcell[c][(0 * 3 + p) * 6 + m] = 0.125f * P[0][p] + 0.75f * P[1][p] + 0.125f * P[2][p];
+            fcell[c][(1 * 3 + p) * 6 + m] = 0.5f * (P[2][p] - P[0][p]);
+            fcell[c][(2 * 3 + p) * 6 + m] = 0.5f * P[0][p] - P[1][p] + 0.5f * P[2][p];
+        }
     }
     __syncthreads();
     // the node rows are consumed: zero the pad columns of the partials buffer
@@ -142,9 +177,11 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
         const int r = e >> 3, q = e & 7;
         cellpj[r][q < 4 ? q : MX_TW + q] = 0.f;
     }
+    for (int e = tid; e < MX_TW * 9; e += MX_THREADS) (&dcnt[0][0])[e] = 0;
+    __syncthreads();
 
     const float fac1 = spc[0], txxx = spc[1], fac2 = spc[2], mqdd = spc[3], qs = spc[4];
-    const int c = tid / MX_LPC, sub = tid % MX_LPC;
+    const int c = tid / MX_LPC, sub = tid % MX_LPC, lane = tid & 31;
     const bool has_cell = c < ncell;
     const int s_beg = has_cell ? cc[c] : 0, s_end = has_cell ? cc[c + 1] : 0;
     const int nmine = (s_end - s_beg > sub) ? (s_end - s_beg - sub + MX_LPC - 1) / MX_LPC : 0;
@@ -152,7 +189,7 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nwarp = max(nwarp, __shfl_xor_sync(FULL, nwarp, o));
     const long long rbase = a.rowbase[row];
-    const float4 *stencil = reinterpret_cast<const float4 *>(&fcell[has_cell ? c : 0][0]);
+    const ulonglong2 *stencil = reinterpret_cast<const ulonglong2 *>(&fcell[has_cell ? c : 0][0]);
     const int cg = c0 + c;
 
     float ax[5][4], ay[4][5], az[5][5];
@@ -193,22 +230,22 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
         shape3(dy - 0.5f, sy0, sy1, sy2);
         float f[6];
         {
-            const float w[9] = {sy0 * sx0, sy0 * sx1, sy0 * sx2, sy1 * sx0, sy1 * sx1, sy1 * sx2, sy2 * sx0, sy2 * sx1, sy2 * sx2};
-            float v[56];
+            // Horner in hx then hy, two fields per packed FMA: C pair j of (q, p) = word (q*3 + p)*3 + j
+            const unsigned long long hx2 = pack2(dx - 0.5f, dx - 0.5f), hy2 = pack2(dy - 0.5f, dy - 0.5f);
+            unsigned long long cw[28];
 #pragma unroll
             for (int q4 = 0; q4 < 14; ++q4) {
-                const float4 t = stencil[q4];
-                v[4 * q4] = t.x;
-                v[4 * q4 + 1] = t.y;
-                v[4 * q4 + 2] = t.z;
-                v[4 * q4 + 3] = t.w;
+                const ulonglong2 t = stencil[q4];
+                cw[2 * q4] = t.x;
+                cw[2 * q4 + 1] = t.y;
             }
 #pragma unroll
-            for (int m = 0; m < 6; ++m) f[m] = w[0] * v[m];
+            for (int j = 0; j < 3; ++j) {
+                unsigned long long r[3];
 #pragma unroll
-            for (int r = 1; r < 9; ++r)
-#pragma unroll
-                for (int m = 0; m < 6; ++m) f[m] = fmaf(w[r], v[6 * r + m], f[m]);
+                for (int q = 0; q < 3; ++q) r[q] = fma2(hx2, fma2(hx2, cw[(q * 3 + 2) * 3 + j], cw[(q * 3 + 1) * 3 + j]), cw[(q * 3) * 3 + j]);
+                unpack2(fma2(hy2, fma2(hy2, r[2], r[1]), r[0]), f[2 * j], f[2 * j + 1]);
+            }
         }
         // Buneman-Boris
         float v1 = u1 + fac1 * f[3], v2 = u2 + fac1 * f[4], v3 = u3 + fac1 * f[5];
@@ -289,17 +326,24 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
 #pragma unroll
             for (int m = 0; m < 4; ++m) ay[m][ip] = fmaf(fx, cy[m], ay[m][ip]);
         }
-        int ci = cg + incx;
-        ci = ci < 0 ? ci + g.nx : (ci >= g.nx ? ci - g.nx : ci);
-        int kr = jr + incy;
-        kr = kr < 0 ? kr + g.ny : (kr >= g.ny ? kr - g.ny : kr);
-        const int kk = valid ? (isp * g.ny + kr) * g.nx + ci : -1;
-        store_particle(b, p, nx1, ny1, u1, u2, u3, key, kk, dir, incy == 1 ? 1u : (incy == -1 ? 2u : 0u), valid);
-        // cell counts for the sort, aggregated over the lanes that share a destination
-        const unsigned peers = __match_any_sync(FULL, kk);
-        if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&cellcnt[kk], __popc(peers));
+        // direction d = (dy+1)*3 + dx+1 and the rank among this cell's particles moving that way,
+        // in particle order: the lanes of a cell with the same d this round, plus earlier rounds
+        // (a step of more than one cell is flagged above; the clamp keeps the move in bounds)
+        const int d = (min(max(incy, -1), 1) + 1) * 3 + (min(max(incx, -1), 1) + 1);
+        const unsigned peers = __match_any_sync(FULL, valid ? (c << 4) | d : (int)(0x7fff0000u | (unsigned)lane));
+        const int leader = __ffs(peers) - 1;
+        int base = (lane == leader && valid) ? dcnt[c][d] : 0;
+        base = __shfl_sync(FULL, base, leader);
+        const int rank = base + __popc(peers & lanemask_lt());
+        if (lane == leader && valid) dcnt[c][d] = base + __popc(peers);
+        __syncwarp();
+        bad |= valid & (rank >= (1 << 27));
+        store_particle(b, p, nx1, ny1, u1, u2, u3, code, ((unsigned)rank << 4) | (unsigned)d, valid);
     }
     if (bad) atomicOr(status, (unsigned)WMDEV_CELL);
+    // this tile's per-cell direction counts (the cells of a warp are its own)
+    if (has_cell)
+        for (int dd = sub; dd < 9; dd += MX_LPC) cnt9[((long long)row * g.nx + cg) * 9 + dd] = dcnt[c][dd];
 
     // the 4 lanes of a cell add their partial currents; lane 0 of the cell keeps the sum
 #pragma unroll
@@ -347,6 +391,67 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
     }
 }
 
+
+// Rebin of the mixed path (the wrap of boundary_periodic.f90:61-96 and :143-165 and the per-cell
+// order of sort.f90:36-82): a particle of source cell s that moved in direction d (code = rank << 4
+// | d) goes to cell s + d.  The particles of a destination cell are ordered by source, in the fixed
+// order k = (sy+1)*3 + sx+1 of the source's offset (sy, sx) from the destination (d = 8 - k),
+// then by rank, which is the particle order within the source cell: a deterministic cell-sorted
+// order.  (The FP64 path keeps the reference's particle_y slot order instead.)
+// off9[dest][k] = particles coming from the sources before k; cellcnt[dest] = all of them.
+__global__ void k_mixed_incoming(WmGeom g, const int *__restrict__ cnt9, int *__restrict__ off9, int *__restrict__ cellcnt)
+{
+    const long long n = (long long)g.nrows * g.nx;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(e % g.nx), row = (int)(e / g.nx);
+        const int isp = row / g.ny, jr = row % g.ny;
+        int run = 0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            int sr = jr + k / 3 - 1, sc = ci + k % 3 - 1;
+            sr += sr < 0 ? g.ny : (sr >= g.ny ? -g.ny : 0);
+            sc += sc < 0 ? g.nx : (sc >= g.nx ? -g.nx : 0);
+            off9[e * 9 + k] = run;
+            run += cnt9[((long long)(isp * g.ny + sr) * g.nx + sc) * 9 + (8 - k)];
+        }
+        cellcnt[e] = run;
+    }
+}
+
+// Move every pushed particle (src: the push output in the old order) to its slot in the new
+// cell-sorted order (dst), ids included.  One CTA per (tile, row, species) of source cells.
+__global__ void __launch_bounds__(MX_THREADS) k_mixed_move(WmGeom g, MixedView src, MixedView dst, const int *__restrict__ cumcnt_old,
+                                                           const int *__restrict__ cumcnt_new, const int *__restrict__ off9,
+                                                           const unsigned *__restrict__ code)
+{
+    __shared__ int cc[MX_TW + 1];
+    const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
+    const int row = isp * g.ny + jr;
+    const int c0 = tile * MX_TW;
+    const int ncell = min(MX_TW, g.nx - c0);
+    const int *ccrow = cumcnt_old + (long long)(g.nx + 1) * row;
+    for (int e = threadIdx.x; e <= ncell; e += MX_THREADS) cc[e] = ccrow[c0 + e];
+    __syncthreads();
+    const long long rb = src.rowbase[row];
+    for (int s = cc[0] + threadIdx.x; s < cc[ncell]; s += MX_THREADS) {
+        int lo = 0, hi = ncell - 1;  // source cell: the last c with cc[c] <= s
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (cc[mid] <= s) lo = mid;
+            else hi = mid - 1;
+        }
+        const long long p = rb + s;
+        const unsigned cv = code[p];
+        const int d = (int)(cv & 15u), rank = (int)(cv >> 4);
+        int dr = jr + d / 3 - 1, dc = c0 + lo + d % 3 - 1;
+        dr += dr < 0 ? g.ny : (dr >= g.ny ? -g.ny : 0);
+        dc += dc < 0 ? g.nx : (dc >= g.nx ? -g.nx : 0);
+        const int drow = isp * g.ny + dr;
+        const long long q = dst.rowbase[drow] + cumcnt_new[(long long)(g.nx + 1) * drow + dc] +
+                            off9[((long long)drow * g.nx + dc) * 9 + (8 - d)] + rank;
+        copy_particle(dst, q, src, p);
+    }
+}
 
 // uj(k, ix, iy) over the ghosted grid = sum of the tile currents that cover the node, in the
 // order (species, cell row, tile), accumulated in FP64.
@@ -454,7 +559,7 @@ int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cuda
 }
 
 int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const float *fcc,
-                                 const int *cumcnt, const WmRebinScratch &sc, float *jtile, cudaStream_t st)
+                                 const int *cumcnt, const WmRebinScratch &sc, int *cnt9, float *jtile, cudaStream_t st)
 {
     MxConst kc;
     for (int s = 0; s < WM_MAX_SP; ++s) {
@@ -468,10 +573,26 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
     kc.dt_dx = (float)(k.delt / k.delx);
     kc.inv_c2 = (float)(1.0 / (k.c * k.c));
     kc.c2 = (float)(k.c * k.c);
-    WM_CUDA(cudaMemsetAsync(sc.cellcnt, 0, sizeof(int) * (size_t)g.nrows * g.nx, st));
     dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
-    k_mixed_push_deposit<<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, sc.key, sc.dir, sc.cellcnt, jtile, sc.status);
+    k_mixed_push_deposit<<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, reinterpret_cast<unsigned *>(sc.key), cnt9, jtile,
+                                                       sc.status);
     return wm_check_launch("k_mixed_push_deposit");
+}
+
+int wm_launch_mixed_incoming(const WmGeom &g, const int *cnt9, int *off9, const WmRebinScratch &sc, cudaStream_t st)
+{
+    const long long n = (long long)g.nrows * g.nx;
+    const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16);
+    k_mixed_incoming<<<blocks, 256, 0, st>>>(g, cnt9, off9, sc.cellcnt);
+    return wm_check_launch("k_mixed_incoming");
+}
+
+int wm_launch_mixed_move(const WmGeom &g, MixedView src, MixedView dst, const int *cumcnt_old, const int *cumcnt_new, const int *off9,
+                         const WmRebinScratch &sc, cudaStream_t st)
+{
+    dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
+    k_mixed_move<<<grid, MX_THREADS, 0, st>>>(g, src, dst, cumcnt_old, cumcnt_new, off9, reinterpret_cast<const unsigned *>(sc.key));
+    return wm_check_launch("k_mixed_move");
 }
 
 int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> uj, cudaStream_t st)

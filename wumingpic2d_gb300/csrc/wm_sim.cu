@@ -69,6 +69,7 @@ struct wm_sim {
     cudaStream_t st = nullptr;
     DevBuf A[6], B[6];
     DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out, jtile, fcc, stage2;
+    DevBuf cumcnt_alt, mx_cnt9, mx_off9;  // mixed path: new cumcnt, per-cell direction counts and offsets
     // learned CG guess (off until wm_sim_set_guess)
     DevBuf cnn_params, cnn_wf[WM_CNN_LAYERS], cnn_x, cnn_a0, cnn_a1, cnn_pred, cnn_partial, cnn_scale, guess_cand, guess_stats;
     WmCnnNet net{};
@@ -186,6 +187,9 @@ struct wm_sim {
         if (mixed()) {
             WM_TRY(jtile.ensure(sizeof(float) * wm_mixed_jtile_floats(g)));
             WM_TRY(fcc.ensure(sizeof(float) * wm_mixed_fcc_floats(g)));
+            WM_TRY(cumcnt_alt.ensure(sizeof(int) * (size_t)(g.nx + 1) * g.nrows));
+            WM_TRY(mx_cnt9.ensure(sizeof(int) * 9 * (size_t)g.nx * g.nrows));
+            WM_TRY(mx_off9.ensure(sizeof(int) * 9 * (size_t)g.nx * g.nrows));
         }
         for (int c = 0; c < 2; ++c) {
             WM_TRY(rowbase[c].ensure(sizeof(long long) * (g.nrows + 1)));
@@ -223,7 +227,7 @@ struct wm_sim {
     {
         size_t t = 0;
         for (int c = 0; c < 6; ++c) t += A[c].bytes + B[c].bytes;
-        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &fcc, &f_uf, &f_uj, &f_df, &f_pj,
+        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &f_uf, &f_uj, &f_df, &f_pj,
                                 &f_b, &f_r, &f_p, &f_ap, &f_partial, &rb_dir, &rb_ord, &rb_P, &rb_key, &rb_holes, &rb_nup,
                                 &rb_ndown, &rb_cellcnt, &rb_pairs})
             t += b->bytes;
@@ -237,7 +241,7 @@ struct wm_sim {
             A[c].release();
             B[c].release();
         }
-        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &stage2,
+        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &stage2,
                           &f_uf, &f_uj, &f_df, &f_pj, &f_b, &f_r, &f_p, &f_ap, &f_partial, &f_ticket, &f_scal, &rb_dir, &rb_ord,
                           &rb_P, &rb_key, &rb_holes, &rb_nup, &rb_ndown, &rb_cellcnt, &rb_pairs, &rb_status})
             b->release();
@@ -335,7 +339,7 @@ struct wm_sim {
         WM_TRY(wm_launch_mixed_fields(g, uf(), fcc.as<float>(), st));
         ++nl;
         mark("fields");
-        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, fcc.as<float>(), cumcnt.as<int>(), sc, jtile.as<float>(), st));
+        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, fcc.as<float>(), cumcnt.as<int>(), sc, mx_cnt9.as<int>(), jtile.as<float>(), st));
         ++nl;
         mark("push_deposit");
         WM_TRY(wm_launch_mixed_jfold(g, jtile.as<float>(), uj(), st));
@@ -344,16 +348,18 @@ struct wm_sim {
         WmFieldWork w = work();
         const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl, guess());
         if (s != WM_OK) return s;
-        // destination counts came from the push: the new cumcnt and row bases first, then the
-        // particle_y slots scatter straight into the destination cells
-        WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
+        // the push counted each cell's particles per direction: destination counts and offsets,
+        // the new cumcnt (into the second buffer) and row bases, then one move into the new order
+        WM_TRY(wm_launch_mixed_incoming(g, mx_cnt9.as<int>(), mx_off9.as<int>(), sc, st));
+        WM_TRY(wm_launch_scan_cells(g, sc, cumcnt_alt.as<int>(), sc.np2_new, st));
         WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
-        nl += 2;
-        mark("scan");
-        WM_TRY(wm_launch_place_sort(g, mview(B, cur, pid_cur), mview(A, 1 - cur, 1 - pid_cur), np2[cur].as<int>(), max_row,
-                                    cumcnt.as<int>(), sc, st));
         nl += 3;
+        mark("scan");
+        WM_TRY(wm_launch_mixed_move(g, mview(B, cur, pid_cur), mview(A, 1 - cur, 1 - pid_cur), cumcnt.as<int>(), cumcnt_alt.as<int>(),
+                                    mx_off9.as<int>(), sc, st));
+        ++nl;
         mark("sort_move");
+        std::swap(cumcnt, cumcnt_alt);
         cur = 1 - cur;
         pid_cur = 1 - pid_cur;
         launches += nl;
