@@ -254,9 +254,14 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
         for _ in range(args.e2e_steps):
             sim.step_host(up_h, uf_h, np2_h, cc_h, 1)
         dt = dist.max(time.perf_counter() - t0)
+        sim.set_timing(True)  # one more call, untimed, for the phase breakdown
+        sim.step_host(up_h, uf_h, np2_h, cc_h, 1)
+        phases = {k: round(v, 2) for k, v in sim.kernel_times().items() if k.startswith("host_")}
+        sim.set_timing(False)
         e2e = {"value": dist.sum(float(ntot)) * args.e2e_steps / dt, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "path": "wm_sim_step_host: reference-layout host arrays in and out every step (pinned)"}
+               "path": "wm_sim_step_host: reference-layout host arrays in and out every step (pinned)",
+               "phase_ms": phases}
         unpin(up_h)
         unpin(uf_h)
         del up_h

@@ -213,6 +213,10 @@ int wm_host_unregister(void *ptr);
  * BF16 [9][cout][cin] (tap = (dy+1)*3 + dx+1), biases FP32.  stream: a cudaStream_t or NULL.  The
  * calls are asynchronous on the stream. */
 enum { WM_CNN_FWD_TRAIN = 0, WM_CNN_FWD_INFER = 1, WM_CNN_FWD_LINEAR = 2, WM_CNN_BWD = 3 };
+/* OR-ed into the mode (or the wgrad flags) of a (48, 48) layer: the weights are block-diagonal
+ * over three groups of 16 channels, as in the learned guess, and only the diagonal blocks are
+ * computed (the other weights must be zero; their gradient is returned as zero). */
+enum { WM_CNN_GROUPED = 16 };
 
 /* One 3x3 convolution, (cin, cout) in {(16, 48), (48, 48), (48, 8)}.  Modes:
  *   FWD_TRAIN  out = GELU(conv + bias) BF16 and zout = conv + bias BF16;
@@ -225,8 +229,8 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
 /* Weight and bias gradients dw[9][cout][cin] (FP32), db[cout] from the layer input x [.][cin] and
  * the pre-activation gradient dz [.][coutp], (cin, coutp) in {(16, 48), (48, 48), (48, 16)},
  * cout <= coutp.  scratch: at least 9*coutp*cin + coutp floats per CTA used (up to 304 CTAs). */
-int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int cout, int nimg, int h, int wd, float *dw, float *db,
-                         float *scratch, long long scratch_floats, void *stream);
+int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int cout, int nimg, int h, int wd, int flags, float *dw,
+                         float *db, float *scratch, long long scratch_floats, void *stream);
 /* *loss = sum over pixels and the 3 outputs of 0.5 (pred - target)^2 / (3 npix); dz = its gradient
  * as BF16 [npix][16].  pred FP32 [npix][8], target FP32 [npix][3]; partial holds nblocks doubles. */
 int wm_cnn_mse(const float *pred, const float *target, long long npix, void *dz, double *partial, int nblocks, double *loss, void *stream);

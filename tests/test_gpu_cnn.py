@@ -19,9 +19,10 @@ from wumingpic2d_gb300.weibel import WeibelConfig, weibel_particles
 pytestmark = pytest.mark.gpu
 
 
-def _case(seed, n=2, H=16, W=32):
+def _case(seed, n=2, H=16, W=32, grouped=True):
+    """grouped: the block-diagonal parameters of the learned guess; else dense weights."""
     rng = np.random.default_rng(seed)
-    params = cnn.init_params(seed)
+    params = cnn.init_params(seed) if grouped else C.flatten(C.init_params(seed))
     P = C.unflatten(params)
     for l, (w, b) in enumerate(P):  # non-zero biases on the real channels
         rout = 3 if l == 5 else w.shape[1]
@@ -37,9 +38,10 @@ def _dev_x(x):
     return torch.tensor(x, dtype=torch.float32).to("cuda", torch.bfloat16)
 
 
-def test_forward_matches_oracle(gpu):
-    params, P, x, _ = _case(1)
-    net = cnn.GuessNet(params)
+@pytest.mark.parametrize("grouped", [True, False])
+def test_forward_matches_oracle(gpu, grouped):
+    params, P, x, _ = _case(1, grouped=grouped)
+    net = cnn.GuessNet(params, grouped=grouped)
     pred_i, _ = net.forward(_dev_x(x), train=False)
     pred_t, (acts, zs) = net.forward(_dev_x(x), train=True)
     torch.cuda.synchronize()
@@ -54,10 +56,11 @@ def test_forward_matches_oracle(gpu):
     assert not pred_i.cpu().numpy()[..., 3:].any()  # padded outputs stay zero
 
 
-def test_gradients_match_oracle(gpu):
-    params, P, x, target = _case(2)
-    net = cnn.GuessNet(params)
-    tr = cnn.Trainer(net)
+@pytest.mark.parametrize("grouped", [True, False])
+def test_gradients_match_oracle(gpu, grouped):
+    params, P, x, target = _case(2, grouped=grouped)
+    net = cnn.GuessNet(params, grouped=grouped)
+    tr = cnn.Trainer(net, masked=grouped)
     loss = tr.loss_and_grad(_dev_x(x), torch.tensor(target, device="cuda"))
     torch.cuda.synchronize()
     pred, cache = C.forward(x, P, bf=True)

@@ -36,6 +36,7 @@ NOUT, GRAD_CH, GROUP_CH = 3, 16, 16
 PACKED_SOURCE = (3, 2, 8, 4, 2, 8, 5, 0, 1, 6, 7)
 PACKED_GROUP = (0, 0, 0, 1, 1, 1, 2, 2, 2, 2, 2)
 FWD_TRAIN, FWD_INFER, FWD_LINEAR, BWD = 0, 1, 2, 3
+GROUPED = 16  # block-diagonal (48, 48) layer: only the three 16-channel diagonal blocks are computed
 WGRAD_SCRATCH = 304 * (9 * 48 * 48 + 48)  # floats: per-CTA partial gradients, 304 CTAs at most
 
 
@@ -102,11 +103,12 @@ def _stream():
 class GuessNet:
     """Parameters (FP32 master copy on the device) and the BF16 layer weights the kernels read."""
 
-    def __init__(self, params: np.ndarray | None = None, seed: int = 0, device: str = "cuda"):
+    def __init__(self, params: np.ndarray | None = None, seed: int = 0, device: str = "cuda", grouped: bool = True):
         flat = init_params(seed) if params is None else np.asarray(params, dtype=np.float32)
         if flat.size != NPARAMS:
             raise ValueError(f"expected {NPARAMS} parameters, got {flat.size}")
         self.device = torch.device(device)
+        self.grouped = grouped  # the (48, 48) layers skip the zero blocks (the weights must be block-diagonal)
         self.params = torch.tensor(flat, device=self.device)
         self.wf = [torch.empty(9 * ci * co, dtype=torch.bfloat16, device=self.device) for ci, co in LAYERS]
         self.wt = [None] + [torch.empty(9 * ci * (GRAD_CH if l == len(LAYERS) - 1 else co), dtype=torch.bfloat16, device=self.device)
@@ -119,6 +121,9 @@ class GuessNet:
             coutb = GRAD_CH if l == len(LAYERS) - 1 else cout
             check(lib().wm_cnn_prep_weights(_pf(self.params, wo), cin, cout, coutb, _p(self.wf[l]), _p(self.wt[l]), _stream()),
                   "wm_cnn_prep_weights")
+
+    def _grp(self, cin, cout) -> int:
+        return GROUPED if (self.grouped and cin == 48 and cout == 48) else 0
 
     def host_params(self) -> np.ndarray:
         return self.params.detach().cpu().numpy().copy()
@@ -137,8 +142,9 @@ class GuessNet:
             wo, bo, cin, cout = OFFSETS[l]
             out = torch.empty((n, H, W, cout), dtype=torch.bfloat16, device=self.device)
             z = torch.empty_like(out) if train else None
-            check(lib().wm_cnn_conv3x3(_p(a), _p(self.wf[l]), _pf(self.params, bo), cin, cout, FWD_TRAIN if train else FWD_INFER,
-                                       n, H, W, _p(out), _p(z), None, _stream()), "wm_cnn_conv3x3")
+            mode = (FWD_TRAIN if train else FWD_INFER) | self._grp(cin, cout)
+            check(lib().wm_cnn_conv3x3(_p(a), _p(self.wf[l]), _pf(self.params, bo), cin, cout, mode, n, H, W, _p(out), _p(z), None,
+                                       _stream()), "wm_cnn_conv3x3")
             acts.append(out)
             zs.append(z)
             a = out
@@ -156,13 +162,13 @@ class GuessNet:
         for l in range(len(LAYERS) - 1, -1, -1):
             wo, bo, cin, cout = OFFSETS[l]
             coutp = GRAD_CH if l == len(LAYERS) - 1 else cout
-            check(lib().wm_cnn_conv3x3_wgrad(_p(acts[l]), _p(dz), cin, coutp, cout, n, H, W, _pf(grad, wo), _pf(grad, bo), _p(scratch),
-                                             scratch.numel(), _stream()), "wm_cnn_conv3x3_wgrad")
+            check(lib().wm_cnn_conv3x3_wgrad(_p(acts[l]), _p(dz), cin, coutp, cout, n, H, W, self._grp(cin, coutp), _pf(grad, wo),
+                                             _pf(grad, bo), _p(scratch), scratch.numel(), _stream()), "wm_cnn_conv3x3_wgrad")
             if l == 0:
                 break
             dprev = torch.empty((n, H, W, cin), dtype=torch.bfloat16, device=self.device)
-            check(lib().wm_cnn_conv3x3(_p(dz), _p(self.wt[l]), None, coutp, cin, BWD, n, H, W, _p(dprev), None, _p(zs[l - 1]),
-                                       _stream()), "wm_cnn_conv3x3")
+            check(lib().wm_cnn_conv3x3(_p(dz), _p(self.wt[l]), None, coutp, cin, BWD | self._grp(coutp, cin), n, H, W, _p(dprev), None,
+                                       _p(zs[l - 1]), _stream()), "wm_cnn_conv3x3")
             dz = dprev
 
 

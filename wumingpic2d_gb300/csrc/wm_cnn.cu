@@ -82,7 +82,7 @@ enum { EPI_TRAIN = 0, EPI_INFER = 1, EPI_LINEAR = 2, EPI_BWD = 3 };
 // CIN.  Four warps, each two tile rows.  Epilogues: TRAIN (z = acc + b stored as BF16, a = GELU(z)
 // as BF16), INFER (a only), LINEAR (acc + b as FP32), BWD (no bias; acc * GELU'(zprev) as BF16: the
 // input gradient of the previous layer's pre-activation).
-template <int CIN, int COUT, int EPI>
+template <int CIN, int COUT, int EPI, bool GROUPED>
 __global__ void __launch_bounds__(128) k_conv3x3(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ wk,
                                                  const float *__restrict__ bias, int nimg, int H, int W, void *out,
                                                  __nv_bfloat16 *__restrict__ zout, const __nv_bfloat16 *__restrict__ zprev)
@@ -130,6 +130,7 @@ __global__ void __launch_bounds__(128) k_conv3x3(const __nv_bfloat16 *__restrict
                 } else {
 #pragma unroll
                     for (int jp = 0; jp < NT / 2; ++jp) {
+                        if (GROUPED && jp != kc) continue;  // block-diagonal: output group jp reads input group jp only
                         uint32_t b[4];
                         ldsm_x4(b, w_s + (tap * COUT + 16 * jp + (lane >> 4) * 8 + (lane & 7)) * CP + kc * 16 + ((lane >> 3) & 1) * 8);
 #pragma unroll
@@ -176,7 +177,7 @@ __global__ void __launch_bounds__(128) k_conv3x3(const __nv_bfloat16 *__restrict
 // Weight gradient dW(tap, co, ci) = sum_p dz(p, co) * x(p + d_tap, ci) and bias gradient
 // db(co) = sum_p dz(p, co), per CTA over its tiles (nine warps, one per tap), written as per-CTA
 // partials that k_reduce_partials sums in CTA order.
-template <int CIN, int COUTP>
+template <int CIN, int COUTP, bool GROUPED>
 __global__ void __launch_bounds__(288) k_conv3x3_wgrad(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ dz, int nimg,
                                                        int H, int W, float *__restrict__ part)
 {
@@ -222,6 +223,7 @@ __global__ void __launch_bounds__(288) k_conv3x3_wgrad(const __nv_bfloat16 *__re
                 ldsm_x4_t(b, x_s + ((r + dy + 1) * HALO_W + (q & 1) * 8 + (lane & 7) + dx + 1) * CP + 8 * (2 * jp + (q >> 1)));
 #pragma unroll
                 for (int mt = 0; mt < MT; ++mt) {
+                    if (GROUPED && mt != jp) continue;  // off-block gradients stay zero
                     mma_bf16(acc[mt][2 * jp], a[mt], b[0], b[1]);
                     mma_bf16(acc[mt][2 * jp + 1], a[mt], b[2], b[3]);
                 }
@@ -332,22 +334,22 @@ __global__ void k_prep_weights(const float *__restrict__ w, int cin, int cout, i
     }
 }
 
-template <int CIN, int COUT, int EPI>
+template <int CIN, int COUT, int EPI, bool GROUPED = false>
 int launch_conv(const void *in, const void *wk, const float *bias, int nimg, int H, int W, void *out, void *zout, const void *zprev,
                 cudaStream_t st)
 {
     constexpr int CP = CIN + 8;
     const size_t smem = sizeof(__nv_bfloat16) * (9 * COUT * CP + HALO_H * HALO_W * CP);
-    WM_CUDA(cudaFuncSetAttribute(k_conv3x3<CIN, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    WM_CUDA(cudaFuncSetAttribute(k_conv3x3<CIN, COUT, EPI, GROUPED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long ntiles = (long long)nimg * (H / TH) * (W / TWD);
     const int grid = (int)std::min<long long>(ntiles, 152LL * 3);
-    k_conv3x3<CIN, COUT, EPI><<<grid, 128, smem, st>>>(static_cast<const __nv_bfloat16 *>(in), static_cast<const __nv_bfloat16 *>(wk), bias,
+    k_conv3x3<CIN, COUT, EPI, GROUPED><<<grid, 128, smem, st>>>(static_cast<const __nv_bfloat16 *>(in), static_cast<const __nv_bfloat16 *>(wk), bias,
                                                         nimg, H, W, out, static_cast<__nv_bfloat16 *>(zout),
                                                         static_cast<const __nv_bfloat16 *>(zprev));
     return wm_check_launch("k_conv3x3");
 }
 
-template <int CIN, int COUTP>
+template <int CIN, int COUTP, bool GROUPED = false>
 int launch_wgrad(const void *x, const void *dz, int nimg, int H, int W, int cout, float *dw, float *db, float *scratch,
                  long long scratch_floats, cudaStream_t st)
 {
@@ -358,7 +360,7 @@ int launch_wgrad(const void *x, const void *dz, int nimg, int H, int W, int cout
     int grid = (int)std::min<long long>(ntiles, 152LL * 2);
     grid = (int)std::min<long long>(grid, scratch_floats / per);
     if (grid < 1) return WM_ERR_BAD_ARG;
-    k_conv3x3_wgrad<CIN, COUTP><<<grid, 288, smem, st>>>(static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(dz), nimg,
+    k_conv3x3_wgrad<CIN, COUTP, GROUPED><<<grid, 288, smem, st>>>(static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(dz), nimg,
                                                          H, W, scratch);
     WM_TRY(wm_check_launch("k_conv3x3_wgrad"));
     const int nout = 9 * cout * CIN + cout;
@@ -497,8 +499,9 @@ int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf,
     const void *in = w.x;
     void *bufs[2] = {w.a0, w.a1};
     for (int l = 0; l < WM_CNN_LAYERS - 1; ++l) {
-        WM_TRY(wm_cnn_conv3x3(in, net.wf[l], net.bias[l], wm_cnn_cin[l], wm_cnn_cout[l], WM_CNN_FWD_INFER, 1, g.ny, g.nx, bufs[l & 1],
-                              nullptr, nullptr, st));
+        const int grp = (wm_cnn_cin[l] == 48 && wm_cnn_cout[l] == 48) ? WM_CNN_GROUPED : 0;
+        WM_TRY(wm_cnn_conv3x3(in, net.wf[l], net.bias[l], wm_cnn_cin[l], wm_cnn_cout[l], WM_CNN_FWD_INFER | grp, 1, g.ny, g.nx,
+                              bufs[l & 1], nullptr, nullptr, st));
         in = bufs[l & 1];
     }
     const int L = WM_CNN_LAYERS - 1;
@@ -515,6 +518,8 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
 {
     if (!in || !w || !out || !shape_ok(nimg, h, wd)) return WM_ERR_BAD_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const bool grouped = (mode & WM_CNN_GROUPED) != 0;
+    mode &= ~WM_CNN_GROUPED;
     if (mode != WM_CNN_BWD && !bias) return WM_ERR_BAD_ARG;
     if (mode == WM_CNN_FWD_TRAIN && !zout) return WM_ERR_BAD_ARG;
     if (mode == WM_CNN_BWD && !zprev) return WM_ERR_BAD_ARG;
@@ -522,6 +527,10 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
         if (mode == WM_CNN_FWD_TRAIN) return launch_conv<16, 48, EPI_TRAIN>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
         if (mode == WM_CNN_FWD_INFER) return launch_conv<16, 48, EPI_INFER>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
         if (mode == WM_CNN_BWD) return launch_conv<16, 48, EPI_BWD>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
+    } else if (cin == 48 && cout == 48 && grouped) {
+        if (mode == WM_CNN_FWD_TRAIN) return launch_conv<48, 48, EPI_TRAIN, true>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
+        if (mode == WM_CNN_FWD_INFER) return launch_conv<48, 48, EPI_INFER, true>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
+        if (mode == WM_CNN_BWD) return launch_conv<48, 48, EPI_BWD, true>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
     } else if (cin == 48 && cout == 48) {
         if (mode == WM_CNN_FWD_TRAIN) return launch_conv<48, 48, EPI_TRAIN>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
         if (mode == WM_CNN_FWD_INFER) return launch_conv<48, 48, EPI_INFER>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
@@ -532,11 +541,13 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
     return WM_ERR_UNSUPPORTED;
 }
 
-int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int cout, int nimg, int h, int wd, float *dw, float *db,
-                         float *scratch, long long scratch_floats, void *stream)
+int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int cout, int nimg, int h, int wd, int flags, float *dw,
+                         float *db, float *scratch, long long scratch_floats, void *stream)
 {
     if (!x || !dz || !dw || !db || !scratch || !shape_ok(nimg, h, wd) || cout < 1 || cout > coutp) return WM_ERR_BAD_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if ((flags & WM_CNN_GROUPED) && cin == 48 && coutp == 48)
+        return launch_wgrad<48, 48, true>(x, dz, nimg, h, wd, cout, dw, db, scratch, scratch_floats, st);
     if (cin == 16 && coutp == 48) return launch_wgrad<16, 48>(x, dz, nimg, h, wd, cout, dw, db, scratch, scratch_floats, st);
     if (cin == 48 && coutp == 48) return launch_wgrad<48, 48>(x, dz, nimg, h, wd, cout, dw, db, scratch, scratch_floats, st);
     if (cin == 48 && coutp == 16) return launch_wgrad<48, 16>(x, dz, nimg, h, wd, cout, dw, db, scratch, scratch_floats, st);

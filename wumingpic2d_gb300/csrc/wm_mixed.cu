@@ -21,7 +21,10 @@
 
 namespace {
 
-constexpr int MX_THREADS = 256;
+#ifndef WM_MX_THREADS
+#define WM_MX_THREADS 256  // threads per push CTA (a build-time tuning choice: 128 or 256)
+#endif
+constexpr int MX_THREADS = WM_MX_THREADS;
 constexpr int MX_LPC = 4;                   // lanes per cell
 constexpr int MX_TW = MX_THREADS / MX_LPC;  // cells per tile (one row, one species)
 constexpr int MX_JW = MX_TW + 4;            // node columns a tile deposits on
@@ -109,7 +112,7 @@ __global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__
 // a lane past the end of its cell runs on a zero particle with zero deposit weights and its stores
 // switched off.  Each lane's next particle is copied into shared memory (cp.async) while the
 // current one is pushed.
-__global__ void __launch_bounds__(MX_THREADS, 2)
+__global__ void __launch_bounds__(MX_THREADS, 512 / MX_THREADS)
     k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const float *__restrict__ fcc, const int *__restrict__ cumcnt,
                          unsigned *__restrict__ code, int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status)
 {

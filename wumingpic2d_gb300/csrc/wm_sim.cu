@@ -11,6 +11,7 @@
 //   classify B (wrap, direction, destination cell), particle_y slots, cell counts -> cumcnt,
 //   and one gather B->A into the new cell-sorted order.
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <vector>
 
@@ -559,9 +560,24 @@ int wm_sim_step(wm_sim *s, int nsteps)
 int wm_sim_step_host(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h, int nsteps)
 {
     if (!s || !up || !uf || !np2_h || !cumcnt_h) return WM_ERR_BAD_ARG;
-    WM_TRY(sim_load_common(s, up, uf, np2_h, cumcnt_h));
+    const auto t0 = std::chrono::steady_clock::now();
+    WM_TRY(sim_load_common(s, up, uf, np2_h, cumcnt_h));  // ends with a stream synchronisation
+    const auto t1 = std::chrono::steady_clock::now();
     WM_TRY(wm_sim_step(s, nsteps));
-    return wm_sim_store(s, up, uf, np2_h, cumcnt_h);
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    const auto t2 = std::chrono::steady_clock::now();
+    WM_TRY(wm_sim_store(s, up, uf, np2_h, cumcnt_h));
+    const auto t3 = std::chrono::steady_clock::now();
+    if (s->timing) {  // wall-clock phases of this call, after the steps' own kernel times
+        const auto ms = [](auto a, auto b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+        s->t_names.push_back("host_copy_in");
+        s->t_ms.push_back(ms(t0, t1));
+        s->t_names.push_back("host_steps");
+        s->t_ms.push_back(ms(t1, t2));
+        s->t_names.push_back("host_copy_out");
+        s->t_ms.push_back(ms(t2, t3));
+    }
+    return WM_OK;
 }
 
 int wm_sim_energy(wm_sim *s, double *out)
