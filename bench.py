@@ -256,7 +256,7 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
         dt = dist.max(time.perf_counter() - t0)
         sim.set_timing(True)  # one more call, untimed, for the phase breakdown
         sim.step_host(up_h, uf_h, np2_h, cc_h, 1)
-        phases = {k: round(v, 2) for k, v in sim.kernel_times().items() if k.startswith("host_")}
+        phases = {k: round(v, 2) for k, v in sim.kernel_times().items() if k.startswith(("host_", "copy_"))}
         sim.set_timing(False)
         e2e = {"value": dist.sum(float(ntot)) * args.e2e_steps / dt, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),

@@ -651,6 +651,28 @@ class Translator:
             stack.pop()
             self.emit("}", ind - 1)
             return
+        # select case on an integer: an if / else-if chain over the case value lists
+        m = re.match(r"^select\s+case\s*\((.*)\)$", ln)
+        if m:
+            self.labels += 1
+            sel = f"f90_sel{self.labels}"
+            self.emit(f"{{ const long {sel} = {self.cond(scope, m.group(1))};", ind)
+            self.emit("if (0) {", ind)
+            stack.append(("select", sel))
+            return
+        m = re.match(r"^case\s*\((.*)\)$", ln)
+        if m and stack and isinstance(stack[-1], tuple) and stack[-1][0] == "select":
+            sel = stack[-1][1]
+            vals = [Expr(scope, tokenize(v)).parse()[0] for v in split_top(m.group(1))]
+            self.emit("} else if (" + " || ".join(f"{sel} == ({v})" for v in vals) + ") {", ind - 1)
+            return
+        if re.match(r"^case\s+default$", ln) and stack and isinstance(stack[-1], tuple) and stack[-1][0] == "select":
+            self.emit("} else {", ind - 1)
+            return
+        if re.match(r"^end\s*select$", ln):
+            stack.pop()
+            self.emit("} }", ind - 1)
+            return
         m = re.match(r"^(?:([a-z_0-9]+)\s*:\s*)?do\s+while\s*\((.*)\)$", ln)
         if m:
             self.emit(f"while ({self.cond(scope, m.group(2))}) {{", ind)
@@ -947,12 +969,16 @@ static inline int f90_sqi(int x) { return x * x; }
 """
 
 
-def translate(common_dir: Path) -> str:
+def translate(common_dir: Path, extra=()) -> str:
+    """common/ modules, then extra module files (the applications' boundary modules), each
+    named after its file."""
     tr = Translator()
     tr.out.append(PRELUDE)
     for mod in MODULES:
         text = (common_dir / f"{mod}.f90").read_text().lower()
         tr.module(mod, logical_lines(text))
+    for path in extra:
+        tr.module(Path(path).stem, logical_lines(Path(path).read_text().lower()))
     return "\n".join(tr.out) + "\n"
 
 

@@ -45,7 +45,11 @@ class Par(ctypes.Structure):
         ("delx", ctypes.c_double), ("delt", ctypes.c_double), ("c", ctypes.c_double), ("gfac", ctypes.c_double),
         ("q", ctypes.c_double * 8), ("r", ctypes.c_double * 8),
         ("cg_err", ctypes.c_double), ("cg_itemax", ctypes.c_int),
+        ("bc", ctypes.c_int), ("u0", ctypes.c_double),
     ]
+
+
+BC = {"periodic": 0, "reconnection": 1, "shock": 2}
 
 
 _lib = None
@@ -65,7 +69,9 @@ def lib():
             "wmo_ele_cur": (None, [P, dp, dp, dp, dp, i, i]),
             "wmo_bc_curre": (None, [P, dp, i, i]),
             "wmo_bc_dfield": (None, [P, dp, i, i]),
-            "wmo_bc_phi": (None, [P, dp, i, i]),
+            "wmo_bc_phi": (None, [P, dp, i, i, i]),
+            "wmo_bc_particle_x_walls": (None, [P, dp, dp, i, i]),
+            "wmo_bc_injection": (None, [P, dp, dp, i, i, ctypes.c_double]),
             "wmo_cgm": (i, [P, dp, dp, i, i, dp]),
             "wmo_field_fdtd_i": (i, [P, dp, dp, dp, dp, i, i, dp, dp, dp, dp]),
             "wmo_bc_particle_x": (None, [P, dp, dp]),
@@ -91,7 +97,7 @@ def _p(a: np.ndarray):
     return a.ctypes.data
 
 
-def make_par(dims, delt, q, r, c=1.0, delx=1.0, gfac=0.501, cg_err=1e-6, cg_itemax=100) -> Par:
+def make_par(dims, delt, q, r, c=1.0, delx=1.0, gfac=0.501, cg_err=1e-6, cg_itemax=100, bc="periodic", u0=0.0) -> Par:
     p = Par()
     p.ndim, p.np, p.nsp = dims.ndim, dims.np, dims.nsp
     p.nxgs, p.nxge, p.nygs, p.nyge = dims.nxgs, dims.nxge, dims.nygs, dims.nyge
@@ -101,6 +107,7 @@ def make_par(dims, delt, q, r, c=1.0, delx=1.0, gfac=0.501, cg_err=1e-6, cg_item
         p.q[k] = float(q[k])
         p.r[k] = float(r[k])
     p.cg_err, p.cg_itemax = cg_err, cg_itemax
+    p.bc, p.u0 = BC[bc], u0
     return p
 
 
@@ -141,8 +148,8 @@ def bc_dfield(par, dims, df):
     lib().wmo_bc_dfield(ctypes.byref(par), _p(df), dims.nxs, dims.nxe)
 
 
-def bc_phi(par, dims, phi):
-    lib().wmo_bc_phi(ctypes.byref(par), _p(phi), dims.nxs, dims.nxe)
+def bc_phi(par, dims, phi, l=1):
+    lib().wmo_bc_phi(ctypes.byref(par), _p(phi), dims.nxs, dims.nxe, l)
 
 
 def cgm(par, dims, db, gkl):
@@ -160,6 +167,14 @@ def field_fdtd_i(par, dims, uf, up, gp, cumcnt, state: OracleState):
 
 def bc_particle_x(par, dims, up, np2):
     lib().wmo_bc_particle_x(ctypes.byref(par), _p(up), _p(np2))
+
+
+def bc_particle_x_walls(par, dims, up, np2):
+    lib().wmo_bc_particle_x_walls(ctypes.byref(par), _p(up), _p(np2), dims.nxs, dims.nxe)
+
+
+def bc_injection(par, dims, up, np2, u0):
+    lib().wmo_bc_injection(ctypes.byref(par), _p(up), _p(np2), dims.nxs, dims.nxe, u0)
 
 
 def bc_particle_y(par, dims, up, np2):

@@ -19,6 +19,21 @@ void ref_boundary_periodic__dfield(double *, int *, int *, int *, int *, int *, 
 void ref_boundary_periodic__curre(double *, int *, int *, int *, int *, int *, int *);
 void ref_boundary_periodic__phi(double *, int *, int *, int *, int *, int *);
 void ref_boundary_periodic__mom(double *);
+/* the applications' boundary modules: proj/reconnection/boundary_reconnection.f90 and
+ * proj/shock/boundary_shock.f90 (same init arguments) */
+#define WALL_DECLS(M)                                                                                                                \
+    void ref_boundary_##M##__init(int *, int *, int *, int *, int *, int *, int *, int *, int *, int *, int *, int *, int *, int *,  \
+                                  int *, int *, long, double *, double *, double *);                                                 \
+    void ref_boundary_##M##__particle_x(double *, int *, int *, int *);                                                             \
+    void ref_boundary_##M##__particle_y(double *, int *);                                                                           \
+    void ref_boundary_##M##__dfield(double *, int *, int *, int *, int *, int *, int *);                                            \
+    void ref_boundary_##M##__curre(double *, int *, int *, int *, int *, int *, int *);                                             \
+    void ref_boundary_##M##__phi(double *, int *, int *, int *, int *, int *);                                                      \
+    void ref_boundary_##M##__mom(double *);                                                                                         \
+    extern int boundary_##M##__boundary_##M##__particle_y__lflag;
+WALL_DECLS(reconnection)
+WALL_DECLS(shock)
+void ref_boundary_shock__injection(double *, int *, int *, int *, double *);
 void ref_particle__init(int *, int *, int *, int *, int *, int *, int *, int *, int *, double *, double *, double *, double *,
                         double *);
 void ref_particle__solv(double *, double *, double *, int *, int *, int *);
@@ -58,6 +73,12 @@ int wmr_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, 
     boundary_periodic__boundary_periodic__particle_y__lflag = 1;
     ref_boundary_periodic__init(&ndim, &np, &nsp, &nxgs, &nxge, &nygs, &nyge, &nys, &nye, &nup, &ndown, &mnpi, &mnpr, &ncomw, &nerr,
                                 nstat, 1, &delx, &delt, &c);
+    boundary_reconnection__boundary_reconnection__particle_y__lflag = 1;
+    boundary_shock__boundary_shock__particle_y__lflag = 1;
+    ref_boundary_reconnection__init(&ndim, &np, &nsp, &nxgs, &nxge, &nygs, &nyge, &nys, &nye, &nup, &ndown, &mnpi, &mnpr, &ncomw,
+                                    &nerr, nstat, 1, &delx, &delt, &c);
+    ref_boundary_shock__init(&ndim, &np, &nsp, &nxgs, &nxge, &nygs, &nyge, &nys, &nye, &nup, &ndown, &mnpi, &mnpr, &ncomw, &nerr,
+                             nstat, 1, &delx, &delt, &c);
     ref_particle__init(&ndim, &np, &nsp, &nxgs, &nxge, &nygs, &nyge, &nys, &nye, &delx, &delt, &c, qq, rr);
     ref_field__init(&ndim, &np, &nsp, &nxgs, &nxge, &nygs, &nyge, &nys, &nye, &mnpr, &ncomw, &opsum, &nerr, &delx, &delt, &c, qq, rr,
                     &gfac);
@@ -91,11 +112,20 @@ int wmr_mom_nvt(double *mom, double *up, int *np2)
     return 0;
 }
 
+/* boundary module the procedures below use: 0 periodic (Weibel), 1 reconnection, 2 shock */
+static int g_bc;
+int wmr_set_bc(int kind)
+{
+    g_bc = kind;
+    return 0;
+}
+#define BC_PROC(name) (g_bc == 1 ? (void (*)())ref_boundary_reconnection__##name \
+                                 : g_bc == 2 ? (void (*)())ref_boundary_shock__##name : (void (*)())ref_boundary_periodic__##name)
+
 int wmr_field_fdtd_i(double *uf, double *up, double *gp, int *cumcnt, int nxs, int nxe)
 {
     GUARD
-    ref_field__fdtd_i(uf, up, gp, cumcnt, &nxs, &nxe, (void (*)())ref_boundary_periodic__dfield,
-                      (void (*)())ref_boundary_periodic__curre, (void (*)())ref_boundary_periodic__phi);
+    ref_field__fdtd_i(uf, up, gp, cumcnt, &nxs, &nxe, BC_PROC(dfield), BC_PROC(curre), BC_PROC(phi));
     return 0;
 }
 
@@ -121,10 +151,26 @@ int wmr_bc_particle_x(double *up, int *np2)
     return 0;
 }
 
+/* the walls' particle_x (reconnection app) and the shock's injection boundary */
+int wmr_bc_particle_x_walls(double *up, int *np2, int nxs, int nxe)
+{
+    GUARD
+    if (g_bc == 2) ref_boundary_shock__particle_x(up, np2, &nxs, &nxe);
+    else ref_boundary_reconnection__particle_x(up, np2, &nxs, &nxe);
+    return 0;
+}
+
+int wmr_bc_injection(double *up, int *np2, int nxs, int nxe, double u0)
+{
+    GUARD
+    ref_boundary_shock__injection(up, np2, &nxs, &nxe, &u0);
+    return 0;
+}
+
 int wmr_bc_particle_y(double *up, int *np2)
 {
     GUARD
-    ref_boundary_periodic__particle_y(up, np2);
+    ((void (*)(double *, int *))BC_PROC(particle_y))(up, np2);
     return 0;
 }
 
@@ -138,27 +184,27 @@ int wmr_sort_bucket(double *gp, double *up, int *cumcnt, int *np2, int nxs, int 
 int wmr_bc_dfield(double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
 {
     GUARD
-    ref_boundary_periodic__dfield(df, &nxs, &nxe, &nys, &nye, &nxgs, &nxge);
+    ((void (*)(double *, int *, int *, int *, int *, int *, int *))BC_PROC(dfield))(df, &nxs, &nxe, &nys, &nye, &nxgs, &nxge);
     return 0;
 }
 
 int wmr_bc_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
 {
     GUARD
-    ref_boundary_periodic__curre(uj, &nxs, &nxe, &nys, &nye, &nxgs, &nxge);
+    ((void (*)(double *, int *, int *, int *, int *, int *, int *))BC_PROC(curre))(uj, &nxs, &nxe, &nys, &nye, &nxgs, &nxge);
     return 0;
 }
 
 int wmr_bc_phi(double *phi, int nxs, int nxe, int nys, int nye, int l)
 {
     GUARD
-    ref_boundary_periodic__phi(phi, &nxs, &nxe, &nys, &nye, &l);
+    ((void (*)(double *, int *, int *, int *, int *, int *))BC_PROC(phi))(phi, &nxs, &nxe, &nys, &nye, &l);
     return 0;
 }
 
 int wmr_bc_mom(double *mom)
 {
     GUARD
-    ref_boundary_periodic__mom(mom);
+    ((void (*)(double *))BC_PROC(mom))(mom);
     return 0;
 }

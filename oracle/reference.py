@@ -32,7 +32,9 @@ def generate(source: Path = DEFAULT_SOURCE) -> bool:
     import f90c  # noqa: E402
 
     REF_DIR.mkdir(exist_ok=True)
-    text = f90c.translate(source)
+    proj = source.parent / "proj"
+    extra = [proj / "reconnection" / "boundary_reconnection.f90", proj / "shock" / "boundary_shock.f90"]
+    text = f90c.translate(source, [e for e in extra if e.exists()])
     if not GEN_C.exists() or GEN_C.read_text() != text:
         GEN_C.write_text(text)
     return True
@@ -83,6 +85,9 @@ def lib():
             "wmr_bc_curre": [P, I, I, I, I, I, I],
             "wmr_bc_phi": [P, I, I, I, I, I],
             "wmr_bc_mom": [P],
+            "wmr_set_bc": [I],
+            "wmr_bc_particle_x_walls": [P, P, I, I],
+            "wmr_bc_injection": [P, P, I, I, D],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -99,12 +104,15 @@ def _p(a):
 class Reference:
     """One configuration of the translated reference modules (their module state is global)."""
 
-    def __init__(self, dims, delt, q, r, c=1.0, delx=1.0, gfac=0.501):
+    BC = {"periodic": 0, "reconnection": 1, "shock": 2}
+
+    def __init__(self, dims, delt, q, r, c=1.0, delx=1.0, gfac=0.501, bc="periodic"):
         self.d = dims
         q = np.ascontiguousarray(q, dtype=np.float64)
         r = np.ascontiguousarray(r, dtype=np.float64)
         d = dims
         assert lib().wmr_init(d.ndim, d.np, d.nsp, d.nxgs, d.nxge, d.nygs, d.nyge, delx, delt, c, _p(q), _p(r), gfac) == 0
+        assert lib().wmr_set_bc(self.BC[bc]) == 0
         self._fdtd_ready = False
 
     def particle_solv(self, gp, up, uf, cumcnt):
@@ -138,6 +146,12 @@ class Reference:
     def field_fdtd_i(self, uf, up, gp, cumcnt):
         self._fdtd_ready = True
         return lib().wmr_field_fdtd_i(_p(uf), _p(up), _p(gp), _p(cumcnt), self.d.nxs, self.d.nxe)
+
+    def bc_particle_x_walls(self, up, np2):
+        return lib().wmr_bc_particle_x_walls(_p(up), _p(np2), self.d.nxs, self.d.nxe)
+
+    def bc_injection(self, up, np2, u0):
+        return lib().wmr_bc_injection(_p(up), _p(np2), self.d.nxs, self.d.nxe, u0)
 
     def bc_particle_x(self, up, np2):
         return lib().wmr_bc_particle_x(_p(up), _p(np2))

@@ -42,6 +42,11 @@
 
 enum { WMO_OK = 0, WMO_ERR_CG_MAXITER = 1, WMO_ERR_OVERFLOW = 2, WMO_ERR_BAD_ARG = 3, WMO_ERR_CELL = 4 };
 
+/* Boundary module of the application: common/boundary_periodic.f90 (Weibel),
+ * proj/reconnection/boundary_reconnection.f90 (walls in x, periodic in y) or
+ * proj/shock/boundary_shock.f90 (reflecting wall at nxs, injection boundary at nxe). */
+enum { WMO_BC_PERIODIC = 0, WMO_BC_RECONNECTION = 1, WMO_BC_SHOCK = 2 };
+
 typedef struct wmo_par {
     int ndim, np, nsp;
     int nxgs, nxge, nygs, nyge, nys, nye;
@@ -49,6 +54,8 @@ typedef struct wmo_par {
     double q[8], r[8];
     double cg_err;  /* field.f90:339  err = 1d-6 */
     int cg_itemax;  /* field.f90:337  ite_max = 100 */
+    int bc;         /* WMO_BC_* */
+    double u0;      /* shock: upstream four-velocity of the injection boundary (proj/shock/app.f90) */
 } wmo_par;
 
 /* ---------------------------------------------------------------- indexing helpers */
@@ -333,6 +340,8 @@ void wmo_bc_curre(const wmo_par *P, double *uj, int nxs, int nxe)
             UJ(k, i, nys - 2) = UJ(k, i, nye - 1);
             UJ(k, i, nys - 1) = UJ(k, i, nye);
         }
+    /* walls in x (boundary_reconnection.f90:364-502, boundary_shock.f90:410-548): y only */
+    if (P->bc != WMO_BC_PERIODIC) return;
     /* x fold, then x refill (:495-506); each line is a whole-column statement */
     for (int j = nys - 2; j <= nye + 2; ++j)
         for (int k = 1; k <= 3; ++k) UJ(k, nxe - 1, j) = UJ(k, nxe - 1, j) + UJ(k, nxs - 2, j);
@@ -365,27 +374,52 @@ void wmo_bc_dfield(const wmo_par *P, double *df, int nxs, int nxe)
             DF(k, i, nys - 2) = DF(k, i, nye - 1);
             DF(k, i, nys - 1) = DF(k, i, nye);
         }
-    for (int j = nys - 2; j <= nye + 2; ++j)
-        for (int k = 1; k <= 6; ++k) {
-            DF(k, nxs - 2, j) = DF(k, nxe - 1, j);
-            DF(k, nxs - 1, j) = DF(k, nxe, j);
-            DF(k, nxe + 1, j) = DF(k, nxs, j);
-            DF(k, nxe + 2, j) = DF(k, nxs + 1, j);
+    if (P->bc == WMO_BC_PERIODIC) {
+        for (int j = nys - 2; j <= nye + 2; ++j)
+            for (int k = 1; k <= 6; ++k) {
+                DF(k, nxs - 2, j) = DF(k, nxe - 1, j);
+                DF(k, nxs - 1, j) = DF(k, nxe, j);
+                DF(k, nxe + 1, j) = DF(k, nxs, j);
+                DF(k, nxe + 2, j) = DF(k, nxs + 1, j);
+            }
+        return;
+    }
+    /* conducting wall at nxs (boundary_reconnection.f90:351-360, boundary_shock.f90:397-406) */
+    for (int j = nys - 2; j <= nye + 2; ++j) {
+        DF(1, nxs - 1, j) = -DF(1, nxs, j);
+        for (int k = 2; k <= 4; ++k) DF(k, nxs - 1, j) = DF(k, nxs + 1, j);
+        for (int k = 5; k <= 6; ++k) DF(k, nxs - 1, j) = -DF(k, nxs, j);
+        if (P->bc == WMO_BC_RECONNECTION) {  /* conducting wall at nxe */
+            DF(1, nxe, j) = -DF(1, nxe - 1, j);
+            for (int k = 2; k <= 4; ++k) DF(k, nxe + 1, j) = DF(k, nxe - 1, j);
+            for (int k = 5; k <= 6; ++k) DF(k, nxe, j) = -DF(k, nxe - 1, j);
+        } else {  /* shock: zero beyond the injection boundary */
+            for (int k = 1; k <= 6; ++k) DF(k, nxe + 1, j) = 0.0;
         }
+    }
 }
 
-/* boundary_periodic.f90:511-568; phi(nxs-1:nxe+1, nys-1:nye+1) */
-static void bc_phi(const wmo_par *P, double *phi, int nxs, int nxe)
+/* boundary_periodic.f90:511-568; phi(nxs-1:nxe+1, nys-1:nye+1).  Walls in x
+ * (boundary_reconnection.f90:557-577, boundary_shock.f90:603-623): component l = 1 (Bx) odd
+ * about nxs - 1/2, l = 2, 3 even about nxs; zero at nxe + 1. */
+static void bc_phi(const wmo_par *P, double *phi, int nxs, int nxe, int l)
 {
     const int nys = P->nys, nye = P->nye, pw = nxe - nxs + 3;
 #define PHI(i, j) phi[(size_t)((i) - (nxs - 1)) + (size_t)pw * (size_t)((j) - (nys - 1))]
     for (int i = nxs; i <= nxe; ++i) PHI(i, nye + 1) = PHI(i, nys);
     for (int i = nxs; i <= nxe; ++i) PHI(i, nys - 1) = PHI(i, nye);
-    for (int j = nys - 1; j <= nye + 1; ++j) PHI(nxs - 1, j) = PHI(nxe, j);
-    for (int j = nys - 1; j <= nye + 1; ++j) PHI(nxe + 1, j) = PHI(nxs, j);
+    if (P->bc == WMO_BC_PERIODIC) {
+        for (int j = nys - 1; j <= nye + 1; ++j) PHI(nxs - 1, j) = PHI(nxe, j);
+        for (int j = nys - 1; j <= nye + 1; ++j) PHI(nxe + 1, j) = PHI(nxs, j);
+    } else {
+        for (int j = nys - 1; j <= nye + 1; ++j) {
+            PHI(nxs - 1, j) = (l == 1) ? -PHI(nxs, j) : PHI(nxs + 1, j);
+            PHI(nxe + 1, j) = 0.0;
+        }
+    }
 #undef PHI
 }
-void wmo_bc_phi(const wmo_par *P, double *phi, int nxs, int nxe) { bc_phi(P, phi, nxs, nxe); }
+void wmo_bc_phi(const wmo_par *P, double *phi, int nxs, int nxe, int l) { bc_phi(P, phi, nxs, nxe, l); }
 
 /* ---------------------------------------------------------- conjugate gradient
  * field.f90:319-461 (cgm).  db has the df layout; gkl(3, nxgs:nxge, nys:nye).  iters[l-1]
@@ -425,7 +459,7 @@ int wmo_cgm(const wmo_par *P, double *db, const double *gkl, int nxs, int nxe, i
             }
         sum_g = sum;
         eps = sqrt(sum_g) * err;
-        bc_phi(P, phi, nxs, nxe);
+        bc_phi(P, phi, nxs, nxe, l);
         sumr = 0.0;
 #pragma omp parallel for reduction(+ : sumr)
         for (int j = nys; j <= nye; ++j)
@@ -438,7 +472,7 @@ int wmo_cgm(const wmo_par *P, double *db, const double *gkl, int nxs, int nxe, i
         if (sqrt(sumr_g) > eps) {
             while (sum_g > eps) {
                 ite = ite + 1;
-                bc_phi(P, p, nxs, nxe);
+                bc_phi(P, p, nxs, nxe, l);
                 sumr = 0.0;
                 sum2 = 0.0;
 #pragma omp parallel for reduction(+ : sumr, sum2)
@@ -573,6 +607,50 @@ void wmo_bc_particle_x(const wmo_par *P, double *up, const int *np2)
             fesetround(save);
         }
     }
+}
+
+/* Reflecting walls, boundary_reconnection.f90:61-99 (= boundary_shock.f90:62-100): a particle
+ * in cell ipos < nxs+1 is mirrored about x = nxs+1, one in ipos >= nxe-1 about nxe-1, and its
+ * momentum reversed.  `2.*(nxs+1)` is a default-real (FP32) product, exact here. */
+void wmo_bc_particle_x_walls(const wmo_par *P, double *up, const int *np2, int nxs, int nxe)
+{
+    const double delx = P->delx;
+    const double xl = (double)(2.0f * (float)(nxs + 1)) * delx, xr = (double)(2.0f * (float)(nxe - 1)) * delx;
+    for (int isp = 1; isp <= P->nsp; ++isp)
+#pragma omp parallel for
+        for (int j = P->nys; j <= P->nye; ++j)
+            for (int ii = 1; ii <= NP2(j, isp); ++ii) {
+                const int ipos = (int)(UP(1, ii, j, isp) / delx);
+                if (ipos < nxs + 1 || ipos >= nxe - 1) {
+                    UP(1, ii, j, isp) = (ipos < nxs + 1 ? xl : xr) - UP(1, ii, j, isp);
+                    for (int k = 3; k <= 5; ++k) UP(k, ii, j, isp) = -UP(k, ii, j, isp);
+                }
+            }
+}
+
+/* boundary_shock.f90:255-297: reflecting wall at nxs+1 and the injection boundary
+ * xend = nxe*delx + u0/sqrt(1+u0^2/c^2)*delt, where particles are mirrored into the inflow
+ * (u_x -> 2 u0 - u_x). */
+void wmo_bc_injection(const wmo_par *P, double *up, const int *np2, int nxs, int nxe, double u0)
+{
+    const double delx = P->delx, c = P->c;
+    const double xend = nxe * delx + u0 / sqrt(1 + (u0 * u0) / (c * c)) * P->delt;
+    const double xl = (double)(2.0f * (float)(nxs + 1)) * delx;
+    for (int isp = 1; isp <= P->nsp; ++isp)
+#pragma omp parallel for
+        for (int j = P->nys; j <= P->nye; ++j)
+            for (int ii = 1; ii <= NP2(j, isp); ++ii) {
+                const int ipos = (int)(UP(1, ii, j, isp) / delx);
+                if (ipos < nxs + 1) {
+                    UP(1, ii, j, isp) = xl - UP(1, ii, j, isp);
+                    for (int k = 3; k <= 5; ++k) UP(k, ii, j, isp) = -UP(k, ii, j, isp);
+                } else if (UP(1, ii, j, isp) > xend) {
+                    UP(1, ii, j, isp) = 2.0 * xend - UP(1, ii, j, isp);
+                    UP(3, ii, j, isp) = 2.0 * u0 - UP(3, ii, j, isp);
+                    UP(4, ii, j, isp) = -UP(4, ii, j, isp);
+                    UP(5, ii, j, isp) = -UP(5, ii, j, isp);
+                }
+            }
 }
 
 /* boundary_periodic.f90:99-248, single-thread semantics.  The reference sizes its exchange
@@ -784,11 +862,12 @@ void wmo_mom_nvt(const wmo_par *P, double *mom, const double *up, const int *np2
 void wmo_bc_mom(const wmo_par *P, double *mom)
 {
     const int nxgs = P->nxgs, nxge = P->nxge, nys = P->nys, nye = P->nye;
+    const int walls = P->bc != WMO_BC_PERIODIC;  /* boundary_reconnection.f90:590-593: fold onto the own edge */
     for (int isp = 1; isp <= P->nsp; ++isp)
         for (int j = nys - 1; j <= nye + 1; ++j)
             for (int k = 1; k <= 7; ++k) {
-                MOM(k, nxgs, j, isp) = MOM(k, nxgs, j, isp) + MOM(k, nxge + 1, j, isp);
-                MOM(k, nxge, j, isp) = MOM(k, nxge, j, isp) + MOM(k, nxgs - 1, j, isp);
+                MOM(k, nxgs, j, isp) = MOM(k, nxgs, j, isp) + MOM(k, walls ? nxgs - 1 : nxge + 1, j, isp);
+                MOM(k, nxge, j, isp) = MOM(k, nxge, j, isp) + MOM(k, walls ? nxge + 1 : nxgs - 1, j, isp);
             }
     for (int isp = 1; isp <= P->nsp; ++isp) {
         for (int i = nxgs - 1; i <= nxge + 1; ++i)
@@ -830,8 +909,13 @@ int wmo_step(const wmo_par *P, double *up, double *gp, double *uf, int *cumcnt, 
 {
     int st;
     wmo_particle_solv(P, gp, up, uf, cumcnt, nxs, nxe);
+    if (P->bc == WMO_BC_SHOCK)  /* proj/shock/app.f90:112-117: injection boundary before the field solve */
+        wmo_bc_injection(P, gp, np2, nxs, nxe, P->u0);
     if ((st = wmo_field_fdtd_i(P, uf, up, gp, cumcnt, nxs, nxe, df, gkl, uj, iters)) != WMO_OK) return st;
-    wmo_bc_particle_x(P, gp, np2);
+    if (P->bc == WMO_BC_PERIODIC)
+        wmo_bc_particle_x(P, gp, np2);
+    else if (P->bc == WMO_BC_RECONNECTION)  /* proj/reconnection/app.f90:101-106 */
+        wmo_bc_particle_x_walls(P, gp, np2, nxs, nxe);
     if ((st = wmo_bc_particle_y(P, gp, np2)) != WMO_OK) return st;
     return wmo_sort_bucket(P, up, gp, cumcnt, np2, nxs, nxe);
 }

@@ -22,7 +22,7 @@
 namespace {
 
 #ifndef WM_MX_THREADS
-#define WM_MX_THREADS 256  // threads per push CTA (a build-time tuning choice: 128 or 256)
+#define WM_MX_THREADS 128  // threads per push CTA (a build-time choice, 128 or 256; 128 measured 2.6 % faster)
 #endif
 constexpr int MX_THREADS = WM_MX_THREADS;
 constexpr int MX_LPC = 4;                   // lanes per cell

@@ -175,6 +175,21 @@ struct wm_sim {
         ++nmarks;
     }
     static void mark_cb(void *self, const char *name) { static_cast<wm_sim *>(self)->mark(name); }
+    // phase events of the host-buffer path (load and store), recorded only with timing on
+    std::vector<Mark> phases;
+    size_t nphases = 0;
+    void pmark(const char *name)
+    {
+        if (!timing) return;
+        if (nphases == phases.size()) {
+            Mark m{name, nullptr};
+            cudaEventCreate(&m.ev);
+            phases.push_back(m);
+        }
+        phases[nphases].name = name;
+        cudaEventRecord(phases[nphases].ev, st);
+        ++nphases;
+    }
 
     int alloc(long long capacity)
     {
@@ -252,6 +267,8 @@ struct wm_sim {
         guess_on = false;
         for (Mark &m : marks) cudaEventDestroy(m.ev);
         marks.clear();
+        for (Mark &m : phases) cudaEventDestroy(m.ev);
+        phases.clear();
         if (scal_host) cudaFreeHost(scal_host);
         if (status_host) cudaFreeHost(status_host);
         scal_host = nullptr;
@@ -278,6 +295,7 @@ struct wm_sim {
         WM_TRY(stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
         WM_CUDA(cudaMemcpy2DAsync(stage.p, sizeof(double) * 6 * maxc, up, sizeof(double) * 6 * g.np, sizeof(double) * 6 * maxc,
                                   g.nrows, cudaMemcpyHostToDevice, st));
+        pmark("copy_in_h2d");
         WM_CUDA(cudaMemcpyAsync(np2[cur].p, np2_h, sizeof(int) * g.nrows, cudaMemcpyHostToDevice, st));
         WM_TRY(wm_launch_rowbase(g.nrows, np2[cur].as<int>(), rowbase[cur].as<long long>(), st));
         if (mixed()) {  // offsets against int(x) and the row; also the load-sort keys and counts
@@ -290,6 +308,7 @@ struct wm_sim {
             WM_TRY(wm_check_launch("k_unpack"));
         }
         max_row = maxc;
+        pmark("copy_in_unpack");
         return WM_OK;
     }
 
@@ -480,6 +499,7 @@ static int sim_load_common(wm_sim *s, const double *up, const double *uf, const 
         WM_TRY(s->sort_B_into_A());
     }
     WM_TRY(s->upload_fields(uf));
+    s->pmark("copy_in_fields");
     if (!s->loaded) {
         const size_t nf = (size_t)g.nxw * g.nyw;
         WM_CUDA(cudaMemsetAsync(s->f_df.p, 0, sizeof(double) * 6 * nf, s->st));
@@ -505,6 +525,7 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
     WM_CUDA(cudaStreamSynchronize(s->st));
     const int maxc = std::max(1, *std::max_element(cnt.begin(), cnt.end()));
     if (maxc > g.np) return WM_ERR_OVERFLOW;
+    s->pmark("store_start");
     if (up) {
         WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
         dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
@@ -515,8 +536,10 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
             k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), maxc, s->stage.as<double>());
             WM_TRY(wm_check_launch("k_pack"));
         }
+        s->pmark("copy_out_pack");
         WM_CUDA(cudaMemcpy2DAsync(up, sizeof(double) * 6 * g.np, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * maxc,
                                   g.nrows, cudaMemcpyDeviceToHost, s->st));
+        s->pmark("copy_out_d2h");
     }
     if (uf) {
         const long long npts = (long long)g.nxw * g.nyw;
@@ -526,6 +549,7 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
     }
     if (cumcnt_h)
         WM_CUDA(cudaMemcpyAsync(cumcnt_h, s->cumcnt.p, sizeof(int) * (size_t)(g.nx + 1) * g.nrows, cudaMemcpyDeviceToHost, s->st));
+    s->pmark("copy_out_fields");
     WM_CUDA(cudaStreamSynchronize(s->st));
     if (np2_h) std::memcpy(np2_h, cnt.data(), sizeof(int) * g.nrows);
     return WM_OK;
@@ -561,6 +585,8 @@ int wm_sim_step_host(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_
 {
     if (!s || !up || !uf || !np2_h || !cumcnt_h) return WM_ERR_BAD_ARG;
     const auto t0 = std::chrono::steady_clock::now();
+    s->nphases = 0;
+    s->pmark("start");
     WM_TRY(sim_load_common(s, up, uf, np2_h, cumcnt_h));  // ends with a stream synchronisation
     const auto t1 = std::chrono::steady_clock::now();
     WM_TRY(wm_sim_step(s, nsteps));
@@ -576,6 +602,15 @@ int wm_sim_step_host(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_
         s->t_ms.push_back(ms(t1, t2));
         s->t_names.push_back("host_copy_out");
         s->t_ms.push_back(ms(t2, t3));
+        // GPU-side phases (events on the stream): each interval is named by the mark that ends it;
+        // the one ending at store_start holds the steps and is left out
+        for (size_t m = 1; m < s->nphases; ++m) {
+            if (std::strcmp(s->phases[m].name, "store_start") == 0) continue;
+            float e = 0.f;
+            WM_CUDA(cudaEventElapsedTime(&e, s->phases[m - 1].ev, s->phases[m].ev));
+            s->t_names.push_back(s->phases[m].name);
+            s->t_ms.push_back(e);
+        }
     }
     return WM_OK;
 }
