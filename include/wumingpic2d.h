@@ -49,6 +49,11 @@ enum {
 };
 
 enum { WM_PREC_FP64 = 0, WM_PREC_MIXED = 1 };
+/* Boundary module of the application (x direction; y is periodic in all three):
+ * common/boundary_periodic.f90 (Weibel), proj/reconnection/boundary_reconnection.f90 (conducting,
+ * reflecting walls at both x ends), proj/shock/boundary_shock.f90 (reflecting wall at nxs,
+ * injection boundary at nxe). */
+enum { WM_BC_PERIODIC = 0, WM_BC_RECONNECTION = 1, WM_BC_SHOCK = 2 };
 
 /* ---------------------------------------------------------------- particle.f90 */
 /* particle__init, common/particle.f90:18-45 */
@@ -99,6 +104,42 @@ int wm_bc_periodic_phi(double *phi, int nxs, int nxe, int nys, int nye, int l);
 /* boundary_periodic__mom(mom), :571-636 */
 int wm_bc_periodic_mom(double *mom);
 
+/* ------------------------------------------- proj/reconnection/boundary_reconnection.f90 */
+/* boundary_reconnection__init, :26-58 (same arguments as boundary_periodic__init) */
+int wm_bc_reconnection_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, int nup,
+                            int ndown, int mnpi, int mnpr, int ncomw, int nerr, const int *nstat, int nstat_len, double delx,
+                            double delt, double c);
+/* boundary_reconnection__particle_x(up, np2, nxs, nxe), :61-99: reflecting walls */
+int wm_bc_reconnection_particle_x(double *up, const int *np2, int nxs, int nxe);
+/* boundary_reconnection__particle_y(up, np2), :102-251 */
+int wm_bc_reconnection_particle_y(double *up, int *np2);
+/* boundary_reconnection__dfield(df, nxs, nxe, nys, nye, nxgs, nxge), :254-361: conducting walls */
+int wm_bc_reconnection_dfield(double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge);
+/* boundary_reconnection__curre(uj, nxs, nxe, nys, nye, nxgs, nxge), :364-502: y fold only */
+int wm_bc_reconnection_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge);
+/* boundary_reconnection__phi(phi, nxs, nxe, nys, nye, l), :505-579 */
+int wm_bc_reconnection_phi(double *phi, int nxs, int nxe, int nys, int nye, int l);
+/* boundary_reconnection__mom(mom), :582-647 */
+int wm_bc_reconnection_mom(double *mom);
+
+/* ------------------------------------------------------- proj/shock/boundary_shock.f90 */
+/* boundary_shock__init, :27-59 */
+int wm_bc_shock_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, int nup, int ndown,
+                     int mnpi, int mnpr, int ncomw, int nerr, const int *nstat, int nstat_len, double delx, double delt, double c);
+/* boundary_shock__particle_x(up, np2, nxs, nxe), :62-100 */
+int wm_bc_shock_particle_x(double *up, const int *np2, int nxs, int nxe);
+/* boundary_shock__particle_y(up, np2), :103-252 */
+int wm_bc_shock_particle_y(double *up, int *np2);
+/* boundary_shock__injection(up, np2, nxs, nxe, u0), :255-297 */
+int wm_bc_shock_injection(double *up, const int *np2, int nxs, int nxe, double u0);
+/* boundary_shock__dfield, :300-407; __curre, :410-548; __phi, :551-625; __mom, :628-693 */
+int wm_bc_shock_dfield(double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge);
+int wm_bc_shock_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge);
+int wm_bc_shock_phi(double *phi, int nxs, int nxe, int nys, int nye, int l);
+int wm_bc_shock_mom(double *mom);
+/* field__fdtd_i uses the boundary procedures of the module whose *_init ran last.  The walls'
+ * procedures support the whole grid as the active range (nxs = nxgs, nxe = nxge). */
+
 /* ------------------------------------------------------------- diagnostics */
 /* Energy sums of energy_history, proj/weibel/app.f90:479-545:
  * out[0..nsp-1] = sum m_s (gamma-1), out[nsp] = sum E^2/8pi, out[nsp+1] = sum B^2/8pi.
@@ -130,6 +171,8 @@ typedef struct wm_sim_config {
     int cg_itemax;        /* CG iteration limit (field.f90:337 uses 100) */
     int precision;        /* WM_PREC_FP64 or WM_PREC_MIXED */
     int64_t capacity;     /* particle slots held on the GPU; 0 = 1.05 x loaded count */
+    int bc;               /* WM_BC_* (the step follows that application's main loop) */
+    double u0;            /* WM_BC_SHOCK: upstream four-velocity at the injection boundary */
 } wm_sim_config;
 
 int wm_sim_create(const wm_sim_config *cfg, wm_sim **out);

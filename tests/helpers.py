@@ -55,6 +55,23 @@ class State:
         return s
 
 
+def confine_x(st: "State", margin_lo: int = 1, margin_hi: int = 2) -> None:
+    """Squeeze the particles of st into [nxgs + margin_lo, nxge + 1 - margin_hi) (where the wall
+    applications keep them) and cell-sort them again; up, gp and cumcnt are replaced."""
+    d = st.d
+    lo, hi = d.nxgs + margin_lo, d.nxge + 1 - margin_hi
+    up = st.up.copy(order="F")
+    for isp in range(d.nsp):
+        for j in range(d.ny):
+            n = int(st.np2[j, isp])
+            x = up[0, :n, j, isp]
+            up[0, :n, j, isp] = lo + (x - d.nxgs) * (hi - lo) / (d.nxge + 1 - d.nxgs)
+    st.up = d.alloc_up()
+    st.cumcnt = d.alloc_cumcnt()
+    assert O.sort_bucket(st.par, d, st.up, up, st.cumcnt, st.np2) == 0
+    st.gp = st.up.copy(order="F")
+
+
 def rel_err(a: np.ndarray, b: np.ndarray) -> float:
     """max |a - b| / max |b| (normwise relative error, 0 when both are zero)."""
     a = np.asarray(a, dtype=np.float64)

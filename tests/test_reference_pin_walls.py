@@ -9,7 +9,7 @@ import pytest
 
 from oracle import oracle as O
 from oracle import reference as R
-from tests.helpers import State
+from tests.helpers import State, confine_x
 
 pytestmark = pytest.mark.skipif(not R.available(), reason="reference translation unavailable")
 
@@ -78,6 +78,7 @@ def test_wall_particle_boundaries(bc):
 @pytest.mark.parametrize("bc", ["reconnection", "shock"])
 def test_wall_steps(bc):
     st, ref = setup(bc, nx=32, ny=24, ppc=8, field_amp=0.02, seed=44)
+    confine_x(st)  # inside the walls, where the applications keep their particles
     a, b = st.copy(), st.copy()
     S = a.oracle_state()
     iters = []

@@ -30,6 +30,7 @@ class SimConfig(ctypes.Structure):
         ("q", ctypes.c_double * 4), ("r", ctypes.c_double * 4),
         ("cg_err", ctypes.c_double), ("cg_itemax", ctypes.c_int),
         ("precision", ctypes.c_int), ("capacity", ctypes.c_int64),
+        ("bc", ctypes.c_int), ("u0", ctypes.c_double),
     ]
 
 
@@ -52,6 +53,21 @@ SIGNATURES = {
     "wm_bc_periodic_curre": [_P, _I, _I, _I, _I, _I, _I],
     "wm_bc_periodic_phi": [_P, _I, _I, _I, _I, _I],
     "wm_bc_periodic_mom": [_P],
+    "wm_bc_reconnection_init": [_I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P, _I, _D, _D, _D],
+    "wm_bc_reconnection_particle_x": [_P, _P, _I, _I],
+    "wm_bc_reconnection_particle_y": [_P, _P],
+    "wm_bc_reconnection_dfield": [_P, _I, _I, _I, _I, _I, _I],
+    "wm_bc_reconnection_curre": [_P, _I, _I, _I, _I, _I, _I],
+    "wm_bc_reconnection_phi": [_P, _I, _I, _I, _I, _I],
+    "wm_bc_reconnection_mom": [_P],
+    "wm_bc_shock_init": [_I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _P, _I, _D, _D, _D],
+    "wm_bc_shock_particle_x": [_P, _P, _I, _I],
+    "wm_bc_shock_particle_y": [_P, _P],
+    "wm_bc_shock_injection": [_P, _P, _I, _I, _D],
+    "wm_bc_shock_dfield": [_P, _I, _I, _I, _I, _I, _I],
+    "wm_bc_shock_curre": [_P, _I, _I, _I, _I, _I, _I],
+    "wm_bc_shock_phi": [_P, _I, _I, _I, _I, _I],
+    "wm_bc_shock_mom": [_P],
     "wm_energy_sums": [_P, _P, _P, _P],
     "wm_field_cg_iters": [_P],
     "wm_field_get_work": [_P, _P],

@@ -11,10 +11,12 @@ the reference calls `stop` raise WmError.
     mom_calc__init / __accl / __nvt         common/mom_calc.f90:18-249
     boundary_periodic__init / __particle_x / __particle_y / __dfield /
         __curre / __phi / __mom             common/boundary_periodic.f90:26-636
+    boundary_reconnection__*                proj/reconnection/boundary_reconnection.f90:26-647
+    boundary_shock__* (with __injection)    proj/shock/boundary_shock.f90:27-693
 
 field__fdtd_i takes the three boundary procedures as arguments in the
-reference; here they are the boundary_periodic ones, and the module whose
-*__init ran last supplies them (pass them for symmetry, they are checked).
+reference; here the boundary module whose *__init ran last supplies them (pass
+them for symmetry, they are checked to belong to one module).
 """
 from __future__ import annotations
 
@@ -73,10 +75,13 @@ def field__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, mnpr, ncomw, o
 
 def field__fdtd_i(uf, up, gp, cumcnt, nxs, nxe, set_boundary_dfield=None, set_boundary_curre=None,
                   set_boundary_phi=None):
-    for f, want in ((set_boundary_dfield, boundary_periodic__dfield), (set_boundary_curre, boundary_periodic__curre),
-                    (set_boundary_phi, boundary_periodic__phi)):
-        if f is not None and f is not want:
-            raise NotImplementedError("only the boundary_periodic procedures run on the GPU")
+    kinds = {"periodic": (boundary_periodic__dfield, boundary_periodic__curre, boundary_periodic__phi),
+             "reconnection": (boundary_reconnection__dfield, boundary_reconnection__curre, boundary_reconnection__phi),
+             "shock": (boundary_shock__dfield, boundary_shock__curre, boundary_shock__phi)}
+    given = (set_boundary_dfield, set_boundary_curre, set_boundary_phi)
+    if any(f is not None for f in given) and not any(all(f is None or f is w for f, w in zip(given, want))
+                                                   for want in kinds.values()):
+        raise NotImplementedError("the boundary procedures must be those of one boundary module")
     check(lib().wm_field_fdtd_i(_p(_f64(uf, "uf")), _p(_f64(up, "up")), _p(_f64(gp, "gp")), _p(_i32(cumcnt, "cumcnt")),
                                 nxs, nxe), "field__fdtd_i")
 
@@ -155,6 +160,75 @@ def boundary_periodic__mom(mom):
     check(lib().wm_bc_periodic_mom(_p(_f64(mom, "mom"))), "boundary_periodic__mom")
 
 
+# ---------------------------------------- proj/reconnection/boundary_reconnection.f90
+def boundary_reconnection__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, nup, ndown, mnpi, mnpr, ncomw, nerr,
+                                nstat, delx, delt, c):
+    st = np.ascontiguousarray(np.asarray(nstat if nstat is not None else [0], dtype=np.int32))
+    check(lib().wm_bc_reconnection_init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, nup, ndown, mnpi, mnpr, ncomw, nerr,
+                                        _p(st), st.size, delx, delt, c), "boundary_reconnection__init")
+
+
+def boundary_reconnection__particle_x(up, np2, nxs, nxe):
+    check(lib().wm_bc_reconnection_particle_x(_p(_f64(up, "up")), _p(_i32(np2, "np2")), nxs, nxe),
+          "boundary_reconnection__particle_x")
+
+
+def boundary_reconnection__particle_y(up, np2):
+    check(lib().wm_bc_reconnection_particle_y(_p(_f64(up, "up")), _p(_i32(np2, "np2"))), "boundary_reconnection__particle_y")
+
+
+def boundary_reconnection__dfield(df, nxs, nxe, nys, nye, nxgs, nxge):
+    check(lib().wm_bc_reconnection_dfield(_p(_f64(df, "df")), nxs, nxe, nys, nye, nxgs, nxge), "boundary_reconnection__dfield")
+
+
+def boundary_reconnection__curre(uj, nxs, nxe, nys, nye, nxgs, nxge):
+    check(lib().wm_bc_reconnection_curre(_p(_f64(uj, "uj")), nxs, nxe, nys, nye, nxgs, nxge), "boundary_reconnection__curre")
+
+
+def boundary_reconnection__phi(phi, nxs, nxe, nys, nye, l):
+    check(lib().wm_bc_reconnection_phi(_p(_f64(phi, "phi")), nxs, nxe, nys, nye, l), "boundary_reconnection__phi")
+
+
+def boundary_reconnection__mom(mom):
+    check(lib().wm_bc_reconnection_mom(_p(_f64(mom, "mom"))), "boundary_reconnection__mom")
+
+
+# ------------------------------------------------------ proj/shock/boundary_shock.f90
+def boundary_shock__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, nup, ndown, mnpi, mnpr, ncomw, nerr, nstat, delx, delt,
+                         c):
+    st = np.ascontiguousarray(np.asarray(nstat if nstat is not None else [0], dtype=np.int32))
+    check(lib().wm_bc_shock_init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, nup, ndown, mnpi, mnpr, ncomw, nerr, _p(st),
+                                 st.size, delx, delt, c), "boundary_shock__init")
+
+
+def boundary_shock__particle_x(up, np2, nxs, nxe):
+    check(lib().wm_bc_shock_particle_x(_p(_f64(up, "up")), _p(_i32(np2, "np2")), nxs, nxe), "boundary_shock__particle_x")
+
+
+def boundary_shock__particle_y(up, np2):
+    check(lib().wm_bc_shock_particle_y(_p(_f64(up, "up")), _p(_i32(np2, "np2"))), "boundary_shock__particle_y")
+
+
+def boundary_shock__injection(up, np2, nxs, nxe, u0):
+    check(lib().wm_bc_shock_injection(_p(_f64(up, "up")), _p(_i32(np2, "np2")), nxs, nxe, u0), "boundary_shock__injection")
+
+
+def boundary_shock__dfield(df, nxs, nxe, nys, nye, nxgs, nxge):
+    check(lib().wm_bc_shock_dfield(_p(_f64(df, "df")), nxs, nxe, nys, nye, nxgs, nxge), "boundary_shock__dfield")
+
+
+def boundary_shock__curre(uj, nxs, nxe, nys, nye, nxgs, nxge):
+    check(lib().wm_bc_shock_curre(_p(_f64(uj, "uj")), nxs, nxe, nys, nye, nxgs, nxge), "boundary_shock__curre")
+
+
+def boundary_shock__phi(phi, nxs, nxe, nys, nye, l):
+    check(lib().wm_bc_shock_phi(_p(_f64(phi, "phi")), nxs, nxe, nys, nye, l), "boundary_shock__phi")
+
+
+def boundary_shock__mom(mom):
+    check(lib().wm_bc_shock_mom(_p(_f64(mom, "mom"))), "boundary_shock__mom")
+
+
 # ------------------------------------------------------------- diagnostics
 def energy_sums(up, uf, np2, nsp) -> np.ndarray:
     """energy_history's sums (proj/weibel/app.f90:507-534): [KE_1..KE_nsp, E^2/8pi, B^2/8pi]."""
@@ -171,11 +245,14 @@ def build_info() -> str:
     return lib().wm_build_info().decode()
 
 
-def init_all(dims, delt, q, r, c=1.0, delx=1.0, gfac=0.501):
-    """Call every module's *__init the way proj/weibel/app.f90:331-347 does (single rank)."""
+def init_all(dims, delt, q, r, c=1.0, delx=1.0, gfac=0.501, bc="periodic"):
+    """Call every module's *__init the way proj/weibel/app.f90:331-347 does (single rank); bc
+    names the boundary module ("periodic", "reconnection" or "shock")."""
     d = dims
     args = (d.ndim, d.np, d.nsp, d.nxgs, d.nxge, d.nygs, d.nyge, d.nys, d.nye)
-    boundary_periodic__init(*args, 0, 0, _MPI_DUMMY, _MPI_DUMMY, _MPI_DUMMY, 0, None, delx, delt, c)
+    init_bc = {"periodic": boundary_periodic__init, "reconnection": boundary_reconnection__init,
+               "shock": boundary_shock__init}[bc]
+    init_bc(*args, 0, 0, _MPI_DUMMY, _MPI_DUMMY, _MPI_DUMMY, 0, None, delx, delt, c)
     particle__init(*args, delx, delt, c, q, r)
     field__init(*args, _MPI_DUMMY, _MPI_DUMMY, _MPI_DUMMY, 0, delx, delt, c, q, r, gfac)
     sort__init(*args)

@@ -190,6 +190,7 @@ struct ModuleState {
     RebinBufs rb;
     bool field_work_zeroed = false;
     int last_iters[3] = {0, 0, 0};
+    int bc_kind = WM_BC_PERIODIC;  // the boundary module whose *_init ran last
 
     int stream()
     {
@@ -293,8 +294,9 @@ static int field_work_ready(const WmGeom &g)
 int wm_field_fdtd_i(double *uf, const double *up, const double *gp, const int *cumcnt, int nxs, int nxe)
 {
     if (!M.field_ok) return WM_ERR_NOT_INIT;
-    if (!M.bc_ok) return WM_ERR_NOT_INIT;  // the boundary procedures come from boundary_periodic
-    const WmGeom &g = M.gfield;
+    if (!M.bc_ok) return WM_ERR_NOT_INIT;  // the boundary procedures: those of the module initialised last
+    WmGeom g = M.gfield;
+    g.bc = M.bc_kind;
     if (nxs != g.nxgs || nxe != g.nxge) return WM_ERR_UNSUPPORTED;
     WM_TRY(field_work_ready(g));
     cudaStream_t st = M.st;
@@ -393,22 +395,76 @@ int wm_mom_calc_nvt(double *mom, const double *up, const int *np2)
     return finish(st);
 }
 
+static int bc_init(int kind, int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, double delx,
+                   double delt, double c)
+{
+    WM_TRY(make_geom(M.gbc, ndim, np, nsp, nxgs, nxge, nygs, nyge, nys, nye));
+    make_const(M.kbc, nsp, delx, delt, c, nullptr, nullptr, 0.501);
+    M.gbc.bc = kind;
+    M.bc_kind = kind;
+    M.bc_ok = true;
+    return WM_OK;
+}
+
+// particle_x of the walls (inject = 0) or the shock's injection boundary (inject = 1), x range
+// nxs..nxe (the whole grid here)
+static int walls_x_dropin(double *up, const int *np2, int nxs, int nxe, int inject, double u0)
+{
+    if (!M.bc_ok) return WM_ERR_NOT_INIT;
+    const WmGeom &g = M.gbc;
+    if (nxs != g.nxgs || nxe != g.nxge) return WM_ERR_UNSUPPORTED;
+    for (int r = 0; r < g.nrows; ++r)
+        if (np2[r] < 0 || np2[r] > g.np) return WM_ERR_BAD_ARG;
+    WM_TRY(M.stream());
+    cudaStream_t st = M.st;
+    const size_t nup = up_doubles(g) * sizeof(double);
+    WM_TRY(h2d(M.a, up, nup, st));
+    WM_TRY(h2d(M.np2, np2, sizeof(int) * g.nrows, st));
+    AoSView va{M.a.as<double>(), g.np};
+    WM_TRY(wm_launch_walls_x(g, M.kbc, va, M.np2.as<int>(), max_of(np2, (size_t)g.nrows), inject, u0, st));
+    WM_TRY(d2h(up, M.a, nup, st));
+    return finish(st);
+}
+
 int wm_bc_periodic_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, int nup,
                         int ndown, int mnpi, int mnpr, int ncomw, int nerr, const int *nstat, int nstat_len, double delx,
                         double delt, double c)
 {
-    (void)nup;
-    (void)ndown;
-    (void)mnpi;
-    (void)mnpr;
-    (void)ncomw;
-    (void)nerr;
-    (void)nstat;
-    (void)nstat_len;
-    WM_TRY(make_geom(M.gbc, ndim, np, nsp, nxgs, nxge, nygs, nyge, nys, nye));
-    make_const(M.kbc, nsp, delx, delt, c, nullptr, nullptr, 0.501);
-    M.bc_ok = true;
-    return WM_OK;
+    (void)nup, (void)ndown, (void)mnpi, (void)mnpr, (void)ncomw, (void)nerr, (void)nstat, (void)nstat_len;
+    return bc_init(WM_BC_PERIODIC, ndim, np, nsp, nxgs, nxge, nygs, nyge, nys, nye, delx, delt, c);
+}
+
+int wm_bc_reconnection_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, int nup,
+                            int ndown, int mnpi, int mnpr, int ncomw, int nerr, const int *nstat, int nstat_len, double delx,
+                            double delt, double c)
+{
+    (void)nup, (void)ndown, (void)mnpi, (void)mnpr, (void)ncomw, (void)nerr, (void)nstat, (void)nstat_len;
+    return bc_init(WM_BC_RECONNECTION, ndim, np, nsp, nxgs, nxge, nygs, nyge, nys, nye, delx, delt, c);
+}
+
+int wm_bc_shock_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, int nup, int ndown,
+                     int mnpi, int mnpr, int ncomw, int nerr, const int *nstat, int nstat_len, double delx, double delt, double c)
+{
+    (void)nup, (void)ndown, (void)mnpi, (void)mnpr, (void)ncomw, (void)nerr, (void)nstat, (void)nstat_len;
+    return bc_init(WM_BC_SHOCK, ndim, np, nsp, nxgs, nxge, nygs, nyge, nys, nye, delx, delt, c);
+}
+
+int wm_bc_reconnection_particle_x(double *up, const int *np2, int nxs, int nxe)
+{
+    if (M.bc_kind != WM_BC_RECONNECTION) return WM_ERR_NOT_INIT;
+    return walls_x_dropin(up, np2, nxs, nxe, 0, 0.0);
+}
+
+int wm_bc_shock_particle_x(double *up, const int *np2, int nxs, int nxe)
+{
+    if (M.bc_kind != WM_BC_SHOCK) return WM_ERR_NOT_INIT;
+    return walls_x_dropin(up, np2, nxs, nxe, 0, 0.0);
+}
+
+int wm_bc_shock_injection(double *up, const int *np2, int nxs, int nxe, double u0)
+{
+    if (M.bc_kind != WM_BC_SHOCK) return WM_ERR_NOT_INIT;
+    return walls_x_dropin(up, np2, nxs, nxe, 1, u0);
 }
 
 int wm_bc_periodic_particle_x(double *up, const int *np2)
@@ -471,10 +527,13 @@ static int check_range_args(const WmGeom &g, int nxs, int nxe, int nys, int nye,
     return WM_OK;
 }
 
-int wm_bc_periodic_dfield(double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+// The ghost routines of the three boundary modules share one implementation each; kind selects
+// the x treatment (y is periodic in all three).
+static int dfield_impl(int kind, double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
 {
     if (!M.bc_ok) return WM_ERR_NOT_INIT;
-    const WmGeom &g = M.gbc;
+    WmGeom g = M.gbc;
+    g.bc = kind;
     WM_TRY(check_range_args(g, nxs, nxe, nys, nye, nxgs, nxge));
     WM_TRY(M.stream());
     const size_t bytes = sizeof(double) * 6 * f_points(g);
@@ -484,10 +543,11 @@ int wm_bc_periodic_dfield(double *df, int nxs, int nxe, int nys, int nye, int nx
     return finish(M.st);
 }
 
-int wm_bc_periodic_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+static int curre_impl(int kind, double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
 {
     if (!M.bc_ok) return WM_ERR_NOT_INIT;
-    const WmGeom &g = M.gbc;
+    WmGeom g = M.gbc;
+    g.bc = kind;
     WM_TRY(check_range_args(g, nxs, nxe, nys, nye, nxgs, nxge));
     WM_TRY(M.stream());
     const size_t bytes = sizeof(double) * 3 * f_points(g);
@@ -497,24 +557,25 @@ int wm_bc_periodic_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxg
     return finish(M.st);
 }
 
-int wm_bc_periodic_phi(double *phi, int nxs, int nxe, int nys, int nye, int l)
+static int phi_impl(int kind, double *phi, int nxs, int nxe, int nys, int nye, int l)
 {
-    (void)l;
     if (!M.bc_ok) return WM_ERR_NOT_INIT;
     const WmGeom &g = M.gbc;
     if (nxs != g.nxgs || nxe != g.nxge || nys != g.nys || nye != g.nye) return WM_ERR_UNSUPPORTED;
+    if (l < 1 || l > 3) return WM_ERR_BAD_ARG;
     WM_TRY(M.stream());
     const size_t bytes = sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2);
     WM_TRY(h2d(M.phi, phi, bytes, M.st));
-    WM_TRY(wm_launch_phi_bc(g.nx, g.ny, M.phi.as<double>(), M.st));
+    WM_TRY(wm_launch_phi_bc(g.nx, g.ny, M.phi.as<double>(), kind, l, M.st));
     WM_TRY(d2h(phi, M.phi, bytes, M.st));
     return finish(M.st);
 }
 
-int wm_bc_periodic_mom(double *mom)
+static int mom_impl(int kind, double *mom)
 {
     if (!M.bc_ok) return WM_ERR_NOT_INIT;
-    const WmGeom &g = M.gbc;
+    WmGeom g = M.gbc;
+    g.bc = kind;
     WM_TRY(M.stream());
     const size_t bytes = sizeof(double) * mom_doubles(g);
     WM_TRY(h2d(M.mom, mom, bytes, M.st));
@@ -522,6 +583,58 @@ int wm_bc_periodic_mom(double *mom)
     WM_TRY(d2h(mom, M.mom, bytes, M.st));
     return finish(M.st);
 }
+
+int wm_bc_periodic_dfield(double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+{
+    return dfield_impl(WM_BC_PERIODIC, df, nxs, nxe, nys, nye, nxgs, nxge);
+}
+int wm_bc_periodic_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+{
+    return curre_impl(WM_BC_PERIODIC, uj, nxs, nxe, nys, nye, nxgs, nxge);
+}
+int wm_bc_periodic_phi(double *phi, int nxs, int nxe, int nys, int nye, int l)
+{
+    return phi_impl(WM_BC_PERIODIC, phi, nxs, nxe, nys, nye, l);
+}
+int wm_bc_periodic_mom(double *mom) { return mom_impl(WM_BC_PERIODIC, mom); }
+
+int wm_bc_reconnection_particle_y(double *up, int *np2)
+{
+    if (M.bc_kind != WM_BC_RECONNECTION) return WM_ERR_NOT_INIT;
+    return wm_bc_periodic_particle_y(up, np2);  // the same procedure (boundary_reconnection.f90:102-251)
+}
+int wm_bc_reconnection_dfield(double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+{
+    return dfield_impl(WM_BC_RECONNECTION, df, nxs, nxe, nys, nye, nxgs, nxge);
+}
+int wm_bc_reconnection_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+{
+    return curre_impl(WM_BC_RECONNECTION, uj, nxs, nxe, nys, nye, nxgs, nxge);
+}
+int wm_bc_reconnection_phi(double *phi, int nxs, int nxe, int nys, int nye, int l)
+{
+    return phi_impl(WM_BC_RECONNECTION, phi, nxs, nxe, nys, nye, l);
+}
+int wm_bc_reconnection_mom(double *mom) { return mom_impl(WM_BC_RECONNECTION, mom); }
+
+int wm_bc_shock_particle_y(double *up, int *np2)
+{
+    if (M.bc_kind != WM_BC_SHOCK) return WM_ERR_NOT_INIT;
+    return wm_bc_periodic_particle_y(up, np2);  // the same procedure (boundary_shock.f90:103-252)
+}
+int wm_bc_shock_dfield(double *df, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+{
+    return dfield_impl(WM_BC_SHOCK, df, nxs, nxe, nys, nye, nxgs, nxge);
+}
+int wm_bc_shock_curre(double *uj, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+{
+    return curre_impl(WM_BC_SHOCK, uj, nxs, nxe, nys, nye, nxgs, nxge);
+}
+int wm_bc_shock_phi(double *phi, int nxs, int nxe, int nys, int nye, int l)
+{
+    return phi_impl(WM_BC_SHOCK, phi, nxs, nxe, nys, nye, l);
+}
+int wm_bc_shock_mom(double *mom) { return mom_impl(WM_BC_SHOCK, mom); }
 
 int wm_energy_sums(const double *up, const double *uf, const int *np2, double *out)
 {

@@ -83,10 +83,23 @@ __global__ void k_dfield_bc_x(WmGeom g, FV df)
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nyr * 6) return;
     const int iy = t % nyr, k = t / nyr;
-    df(k, 0, iy) = df(k, g.nx, iy);
-    df(k, 1, iy) = df(k, g.nx + 1, iy);
-    df(k, g.nx + 2, iy) = df(k, 2, iy);
-    df(k, g.nx + 3, iy) = df(k, 3, iy);
+    if (g.bc == WM_BC_PERIODIC) {
+        df(k, 0, iy) = df(k, g.nx, iy);
+        df(k, 1, iy) = df(k, g.nx + 1, iy);
+        df(k, g.nx + 2, iy) = df(k, 2, iy);
+        df(k, g.nx + 3, iy) = df(k, 3, iy);
+        return;
+    }
+    // conducting wall at nxs (boundary_reconnection.f90:351-360, boundary_shock.f90:397-406):
+    // column nxs-1 (ghosted 1) from nxs (2) or nxs+1 (3)
+    if (k == 0 || k >= 4) df(k, 1, iy) = -df(k, 2, iy);
+    else df(k, 1, iy) = df(k, 3, iy);
+    if (g.bc == WM_BC_RECONNECTION) {  // conducting wall at nxe (ghosted nx+1), mirror of the left
+        if (k == 0 || k >= 4) df(k, g.nx + 1, iy) = -df(k, g.nx, iy);
+        else df(k, g.nx + 2, iy) = df(k, g.nx, iy);
+    } else {  // shock: zero beyond the injection boundary
+        df(k, g.nx + 2, iy) = 0.0;
+    }
 }
 
 // phi(nxs-1:nxe+1, nys-1:nye+1), x fastest
@@ -98,13 +111,18 @@ __global__ void k_phi_bc_y(int nx, int ny, double *phi)
     phi[ix + (long long)pw * (ny + 1)] = phi[ix + (long long)pw * 1];
     phi[ix + 0] = phi[ix + (long long)pw * ny];
 }
-__global__ void k_phi_bc_x(int nx, int ny, double *phi)
+__global__ void k_phi_bc_x(int nx, int ny, double *phi, int bc, int l)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ny + 2) return;
     const int pw = nx + 2;
-    phi[0 + (long long)pw * t] = phi[nx + (long long)pw * t];
-    phi[nx + 1 + (long long)pw * t] = phi[1 + (long long)pw * t];
+    if (bc == WM_BC_PERIODIC) {
+        phi[0 + (long long)pw * t] = phi[nx + (long long)pw * t];
+        phi[nx + 1 + (long long)pw * t] = phi[1 + (long long)pw * t];
+    } else {  // walls (boundary_reconnection.f90:557-577): Bx odd about nxs-1/2, By, Bz even about nxs; zero at nxe+1
+        phi[0 + (long long)pw * t] = (l == 1) ? -phi[1 + (long long)pw * t] : phi[2 + (long long)pw * t];
+        phi[nx + 1 + (long long)pw * t] = 0.0;
+    }
 }
 
 // mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp), reference layout
@@ -115,8 +133,9 @@ __global__ void k_mom_bc_x(WmGeom g, double *mom)
     if (t >= my * g.nsp * 7) return;
     const int k = t % 7, jy = (t / 7) % my, isp = t / (7 * my);
     double *rowp = mom + 7 * (long long)mx * (jy + (long long)my * isp);
-    rowp[k + 7 * 1] = rowp[k + 7 * 1] + rowp[k + 7 * (mx - 1)];
-    rowp[k + 7 * (mx - 2)] = rowp[k + 7 * (mx - 2)] + rowp[k + 7 * 0];
+    const bool walls = g.bc != WM_BC_PERIODIC;  // boundary_reconnection.f90:590-593: onto the own edge
+    rowp[k + 7 * 1] = rowp[k + 7 * 1] + rowp[k + 7 * (walls ? 0 : mx - 1)];
+    rowp[k + 7 * (mx - 2)] = rowp[k + 7 * (mx - 2)] + rowp[k + 7 * (walls ? mx - 1 : 0)];
 }
 __global__ void k_mom_bc_y(WmGeom g, double *mom)
 {
@@ -222,6 +241,22 @@ struct FieldK {
 
 __device__ __forceinline__ int wrapm(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
 
+// The x neighbours of interior cell ci (0-based) of component l (0 = Bx) of a CG vector, read
+// through at(c) = value at interior column c of the same row: periodic wrap, or the walls' halo
+// (boundary_reconnection__phi / boundary_shock__phi): Bx odd about nxs - 1/2, By and Bz even
+// about nxs, zero beyond nxe.
+template <class F>
+__device__ __forceinline__ void x_neighbours(const WmGeom &g, int l, int ci, const F &at, double &left, double &right)
+{
+    if (g.bc == WM_BC_PERIODIC) {
+        left = at(wrapm(ci - 1, g.nx));
+        right = at(wrapm(ci + 1, g.nx));
+        return;
+    }
+    left = ci > 0 ? at(ci - 1) : (l == 0 ? -at(0) : at(1));
+    right = ci < g.nx - 1 ? at(ci + 1) : 0.0;
+}
+
 // gkl (field.f90:125-146), b = f5*gkl and ||b||^2 (:351-364).
 template <class FV6, class FV3>
 __global__ void __launch_bounds__(CG_THREADS) k_cg_rhs(WmGeom g, FieldK fk, FV6 uf, FV3 uj, double *__restrict__ b,
@@ -268,11 +303,12 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_resid(WmGeom g, FieldK fk, FV
     double acc[3] = {0.0, 0.0, 0.0};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
         const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
-        const int xm = wrapm(ci - 1, g.nx) + 2, xp = wrapm(ci + 1, g.nx) + 2, ym = wrapm(cj - 1, g.ny) + 2,
-                  yp = wrapm(cj + 1, g.ny) + 2, x = ci + 2, y = cj + 2;
+        const int ym = wrapm(cj - 1, g.ny) + 2, yp = wrapm(cj + 1, g.ny) + 2, x = ci + 2, y = cj + 2;
 #pragma unroll
         for (int l = 0; l < 3; ++l) {
-            const double rv = b[l * ncell + e] + df(l, x, ym) + df(l, xm, y) - fk.f4 * df(l, x, y) + df(l, xp, y) + df(l, x, yp);
+            double xl, xr;
+            x_neighbours(g, l, ci, [&](int c) { return df(l, c + 2, y); }, xl, xr);
+            const double rv = b[l * ncell + e] + df(l, x, ym) + xl - fk.f4 * df(l, x, y) + xr + df(l, x, yp);
             r[l * ncell + e] = rv;
             p[l * ncell + e] = rv;
             acc[l] += rv * rv;
@@ -308,11 +344,12 @@ __global__ void __launch_bounds__(CG_THREADS) k_guess_resid(WmGeom g, FieldK fk,
     double acc[3] = {0.0, 0.0, 0.0};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
         const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
-        const int xm = wrapm(ci - 1, g.nx) + 2, xp = wrapm(ci + 1, g.nx) + 2, ym = wrapm(cj - 1, g.ny) + 2,
-                  yp = wrapm(cj + 1, g.ny) + 2, xx = ci + 2, yy = cj + 2;
+        const int ym = wrapm(cj - 1, g.ny) + 2, yp = wrapm(cj + 1, g.ny) + 2, xx = ci + 2, yy = cj + 2;
 #pragma unroll
         for (int l = 0; l < 3; ++l) {
-            const double rv = b[l * ncell + e] + x(l, xx, ym) + x(l, xm, yy) - fk.f4 * x(l, xx, yy) + x(l, xp, yy) + x(l, xx, yp);
+            double xl, xr;
+            x_neighbours(g, l, ci, [&](int c) { return x(l, c + 2, yy); }, xl, xr);
+            const double rv = b[l * ncell + e] + x(l, xx, ym) + xl - fk.f4 * x(l, xx, yy) + xr + x(l, xx, yp);
             acc[l] += rv * rv;
         }
     }
@@ -351,14 +388,16 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_ap(WmGeom g, FieldK fk, const
     double acc[3] = {0.0, 0.0, 0.0};
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
         const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
-        const long long em = (long long)cj * g.nx + wrapm(ci - 1, g.nx), ep = (long long)cj * g.nx + wrapm(ci + 1, g.nx);
+        const long long row = (long long)cj * g.nx;
         const long long es = (long long)wrapm(cj - 1, g.ny) * g.nx + ci, en = (long long)wrapm(cj + 1, g.ny) * g.nx + ci;
 #pragma unroll
         for (int l = 0; l < 3; ++l) {
             if (!act[l]) continue;
             const double *pl = p + l * ncell;
             const double pc = pl[e];
-            const double a = -pl[es] - pl[em] + fk.f4 * pc - pl[ep] - pl[en];
+            double xl, xr;
+            x_neighbours(g, l, ci, [&](int c) { return pl[row + c]; }, xl, xr);
+            const double a = -pl[es] - xl + fk.f4 * pc - xr - pl[en];
             ap[l * ncell + e] = a;
             acc[l] += pc * a;
         }
@@ -495,6 +534,7 @@ int wm_launch_curre_bc(const WmGeom &g, FV uj, cudaStream_t st)
 {
     k_curre_bc_y<FV><<<wm_div_up((g.nx + 4) * 3, 128), 128, 0, st>>>(g, uj);
     WM_TRY(wm_check_launch("k_curre_bc_y"));
+    if (g.bc != WM_BC_PERIODIC) return WM_OK;  // walls: no x fold (boundary_reconnection.f90:364-502)
     k_curre_bc_x<FV><<<wm_div_up((g.ny + 4) * 3, 128), 128, 0, st>>>(g, uj);
     return wm_check_launch("k_curre_bc_x");
 }
@@ -508,11 +548,11 @@ int wm_launch_dfield_bc(const WmGeom &g, FV df, cudaStream_t st)
     return wm_check_launch("k_dfield_bc_x");
 }
 
-int wm_launch_phi_bc(int nx, int ny, double *phi, cudaStream_t st)
+int wm_launch_phi_bc(int nx, int ny, double *phi, int bc, int l, cudaStream_t st)
 {
     k_phi_bc_y<<<wm_div_up(nx, 128), 128, 0, st>>>(nx, ny, phi);
     WM_TRY(wm_check_launch("k_phi_bc_y"));
-    k_phi_bc_x<<<wm_div_up(ny + 2, 128), 128, 0, st>>>(nx, ny, phi);
+    k_phi_bc_x<<<wm_div_up(ny + 2, 128), 128, 0, st>>>(nx, ny, phi, bc, l);
     return wm_check_launch("k_phi_bc_x");
 }
 

@@ -20,6 +20,7 @@ struct WmGeom {
     int nxgs, nxge, nygs, nyge, nys, nye;
     int nx, ny, nrows;  // nrows = nsp * ny
     int nxw, nyw;       // ghosted extents nx+4, ny+4
+    int bc;             // WM_BC_*: boundary module of the application (x direction; y is periodic in all three)
 };
 
 struct WmConst {

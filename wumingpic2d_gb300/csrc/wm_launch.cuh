@@ -20,6 +20,11 @@ int wm_launch_energy_particles(const WmGeom &g, const WmConst &k, PV up, const i
                                cudaStream_t st);
 
 // wm_rebin.cu
+// particle_x of the walls (inject = 0) or the shock's injection boundary (inject = 1) over the
+// first np2[row] particles of every row; x range nxgs..nxge.
+template <class PV>
+int wm_launch_walls_x(const WmGeom &g, const WmConst &k, PV v, const int *np2, int max_row_count, int inject, double u0,
+                      cudaStream_t st);
 template <class PV>
 int wm_launch_wrap_classify(const WmGeom &g, double delx, PV v, const int *np2, int max_row_count, int mode,
                             const WmRebinScratch &sc, cudaStream_t st);
@@ -58,7 +63,7 @@ template <class FV>
 int wm_launch_curre_bc(const WmGeom &g, FV uj, cudaStream_t st);
 template <class FV>
 int wm_launch_dfield_bc(const WmGeom &g, FV df, cudaStream_t st);
-int wm_launch_phi_bc(int nx, int ny, double *phi, cudaStream_t st);
+int wm_launch_phi_bc(int nx, int ny, double *phi, int bc, int l, cudaStream_t st);
 int wm_launch_mom_bc(const WmGeom &g, double *mom, cudaStream_t st);
 int wm_launch_aos_to_soa(int nc, long long npts, const double *a, double *s, cudaStream_t st);
 int wm_launch_soa_to_aos(int nc, long long npts, const double *s, double *a, cudaStream_t st);

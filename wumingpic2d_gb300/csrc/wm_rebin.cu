@@ -36,9 +36,68 @@ __device__ __forceinline__ unsigned lanemask_lt()
     return m;
 }
 
+// ------------------------------------------------------------ walls in x
+// Reflecting walls, boundary_reconnection.f90:61-99 (= boundary_shock.f90:62-100): a particle in
+// cell ipos < nxs+1 is mirrored about x = nxs+1, one in ipos >= nxe-1 about nxe-1, its momentum
+// reversed.  inject != 0: boundary_shock.f90:255-297 instead -- the same left wall, and beyond
+// xend = nxe*delx + u0/sqrt(1+u0^2/c^2)*delt the particle is mirrored into the inflow
+// (u_x -> 2 u0 - u_x).  `2.*(nxs+1)` is a default-real (FP32) product, exact here.
+template <class PV>
+__device__ __forceinline__ void walls_x_one(const PV &v, long long p, double delx, double xl, double xr, double xend, int nxs, int nxe,
+                                            int inject, double u0)
+{
+    const double x = v.X(p);
+    const int ipos = (int)(x / delx);
+    if (ipos < nxs + 1) {
+        v.X(p) = xl - x;
+        v.UX(p) = -v.UX(p);
+        v.UY(p) = -v.UY(p);
+        v.UZ(p) = -v.UZ(p);
+    } else if (!inject && ipos >= nxe - 1) {
+        v.X(p) = xr - x;
+        v.UX(p) = -v.UX(p);
+        v.UY(p) = -v.UY(p);
+        v.UZ(p) = -v.UZ(p);
+    } else if (inject && x > xend) {
+        v.X(p) = 2.0 * xend - x;
+        v.UX(p) = 2.0 * u0 - v.UX(p);
+        v.UY(p) = -v.UY(p);
+        v.UZ(p) = -v.UZ(p);
+    }
+}
+
+struct WallsX {
+    double delx, xl, xr, xend, u0;
+    int nxs, nxe, inject;
+};
+
+WallsX walls_x_params(const WmGeom &g, double delx, double delt, double c, int inject, double u0)
+{
+    WallsX w;
+    w.delx = delx;
+    w.nxs = g.nxgs;
+    w.nxe = g.nxge;
+    w.xl = (double)(2.0f * (float)(w.nxs + 1)) * delx;
+    w.xr = (double)(2.0f * (float)(w.nxe - 1)) * delx;
+    w.xend = w.nxe * delx + u0 / sqrt(1 + (u0 * u0) / (c * c)) * delt;
+    w.u0 = u0;
+    w.inject = inject;
+    return w;
+}
+
+template <class PV>
+__global__ void k_walls_x(WmGeom g, WallsX w, PV v, const int *__restrict__ np2)
+{
+    const int row = blockIdx.y;
+    const int n = np2[row];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x)
+        walls_x_one(v, v.idx(row, s), w.delx, w.xl, w.xr, w.xend, w.nxs, w.nxe, w.inject, w.u0);
+}
+
 // ------------------------------------------------------- wrap + classify + key
 // mode bits: 1 = particle_x wrap, 2 = particle_y wrap + dir, 4 = sort key + cell count
-// (key from the wrapped row), 8 = sort key from the current row (sort__bucket alone).
+// (key from the wrapped row), 8 = sort key from the current row (sort__bucket alone),
+// 16 = particle_x of the walls (reflect at nxs+1 and nxe-1) instead of the wrap.
 template <class PV>
 __global__ void k_wrap_classify(WmGeom g, double delx, PV v, const int *__restrict__ np2, int mode,
                                 unsigned char *__restrict__ dir, int *__restrict__ key, int *__restrict__ cellcnt,
@@ -63,6 +122,10 @@ __global__ void k_wrap_classify(WmGeom g, double delx, PV v, const int *__restri
         int k = -1;
         if (valid) {
             const long long p = v.idx(row, s);
+            if (mode & 16) {
+                const double xl = (double)(2.0f * (float)(g.nxgs + 1)) * delx, xr = (double)(2.0f * (float)(g.nxge - 1)) * delx;
+                walls_x_one(v, p, delx, xl, xr, 0.0, g.nxgs, g.nxge, 0, 0.0);
+            }
             double x = v.X(p);
             if (mode & 1) {  // boundary_periodic.f90:82-88, rounding mode downward
                 const int ipos = unit ? (int)x : (int)__ddiv_rd(x, delx);
@@ -660,7 +723,17 @@ int wm_launch_sort_move(const WmGeom &g, PV src, PV dst, const int *src_np2, int
     return wm_check_launch("k_cellsort_gather");
 }
 
+template <class PV>
+int wm_launch_walls_x(const WmGeom &g, const WmConst &k, PV v, const int *np2, int max_row_count, int inject, double u0,
+                      cudaStream_t st)
+{
+    const WallsX w = walls_x_params(g, k.delx, k.delt, k.c, inject, u0);
+    k_walls_x<PV><<<row_grid(g, max_row_count, 256), 256, 0, st>>>(g, w, v, np2);
+    return wm_check_launch("k_walls_x");
+}
+
 #define WM_INST(PV)                                                                                                   \
+    template int wm_launch_walls_x<PV>(const WmGeom &, const WmConst &, PV, const int *, int, int, double, cudaStream_t); \
     template int wm_launch_wrap_classify<PV>(const WmGeom &, double, PV, const int *, int, int, const WmRebinScratch &, \
                                              cudaStream_t);                                                            \
     template int wm_launch_place<PV>(const WmGeom &, PV, const int *, int, const WmRebinScratch &, int *, cudaStream_t); \

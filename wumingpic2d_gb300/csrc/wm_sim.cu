@@ -66,6 +66,7 @@ struct wm_sim {
     WmGeom g{};
     WmConst k{};
     int precision = WM_PREC_FP64;
+    double u0 = 0.0;  // shock: upstream four-velocity of the injection boundary
     long long cap_req = 0, cap = 0, ntot = 0;
     cudaStream_t st = nullptr;
     DevBuf A[6], B[6];
@@ -396,6 +397,10 @@ struct wm_sim {
         SoAView va = view(A, cur), vb = view(B, cur);
         WM_TRY(wm_launch_push(g, k, va, vb, uf(), cumcnt.as<int>(), 0, 1, st));
         ++nl;
+        if (g.bc == WM_BC_SHOCK) {  // proj/shock/app.f90:112-117: the injection boundary before the field solve
+            WM_TRY(wm_launch_walls_x(g, k, vb, np2[cur].as<int>(), max_row, 1, u0, st));
+            ++nl;
+        }
         mark("push");
         WM_TRY(wm_launch_deposit_cells(g, k, va, vb, cumcnt.as<int>(), f_pj.as<double>(), sc.status, st));
         WM_TRY(wm_launch_deposit_fold(g, uj(), f_pj.as<double>(), st));
@@ -404,7 +409,10 @@ struct wm_sim {
         WmFieldWork w = work();
         const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl, guess());
         if (s != WM_OK) return s;
-        WM_TRY(wm_launch_wrap_classify(g, k.delx, vb, np2[cur].as<int>(), max_row, 1 | 2 | 4, sc, st));
+        // particle_x of the application (periodic wrap, the reconnection walls, none in the shock
+        // loop), particle_y, and the sort keys
+        const int xmode = g.bc == WM_BC_PERIODIC ? 1 : (g.bc == WM_BC_RECONNECTION ? 16 : 0);
+        WM_TRY(wm_launch_wrap_classify(g, k.delx, vb, np2[cur].as<int>(), max_row, xmode | 2 | 4, sc, st));
         nl += 1;
         mark("classify");
         WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
@@ -429,8 +437,12 @@ int wm_sim_create(const wm_sim_config *cfg, wm_sim **out)
     if (cfg->precision != WM_PREC_FP64 && cfg->precision != WM_PREC_MIXED) return WM_ERR_BAD_ARG;
     if (cfg->nsp < 1 || cfg->nsp > WM_MAX_SP || cfg->nx < 4 || cfg->ny < 4 || cfg->np < 1) return WM_ERR_BAD_ARG;
     if (cfg->cg_itemax < 1 || !(cfg->cg_err > 0)) return WM_ERR_BAD_ARG;
+    if (cfg->bc != WM_BC_PERIODIC && cfg->bc != WM_BC_RECONNECTION && cfg->bc != WM_BC_SHOCK) return WM_ERR_BAD_ARG;
+    if (cfg->bc != WM_BC_PERIODIC && cfg->precision == WM_PREC_MIXED) return WM_ERR_UNSUPPORTED;
     wm_sim *s = new wm_sim();
     WmGeom &g = s->g;
+    g.bc = cfg->bc;
+    s->u0 = cfg->u0;
     g.ndim = 6;
     g.np = cfg->np;
     g.nsp = cfg->nsp;

@@ -15,11 +15,15 @@ from ._native import WM_PREC_FP64, WM_PREC_MIXED, SimConfig, check, lib
 from .layout import Dims
 
 PRECISIONS = {"fp64": WM_PREC_FP64, "mixed": WM_PREC_MIXED}
+BOUNDARIES = {"periodic": 0, "reconnection": 1, "shock": 2}
 
 
 class Simulation:
     def __init__(self, dims: Dims, delt: float, q, r, c: float = 1.0, delx: float = 1.0, gfac: float = 0.501,
-                 cg_err: float = 1e-6, cg_itemax: int = 100, precision: str = "fp64", capacity: int = 0):
+                 cg_err: float = 1e-6, cg_itemax: int = 100, precision: str = "fp64", capacity: int = 0, bc: str = "periodic",
+                 u0: float = 0.0):
+        """bc: the application's boundary module -- "periodic" (Weibel), "reconnection" (walls in x) or
+        "shock" (reflecting wall and injection boundary, upstream four-velocity u0)."""
         if dims.nxgs != 2 or dims.nygs != 2:
             raise ValueError("the resident simulation uses nxgs = nygs = 2 like the reference apps")
         self.dims = dims
@@ -32,6 +36,8 @@ class Simulation:
         cfg.cg_err, cfg.cg_itemax = cg_err, cg_itemax
         cfg.precision = PRECISIONS[precision]
         cfg.capacity = capacity
+        cfg.bc = BOUNDARIES[bc]
+        cfg.u0 = u0
         self._h = ctypes.c_void_p()
         check(lib().wm_sim_create(ctypes.byref(cfg), ctypes.byref(self._h)), "wm_sim_create")
 
