@@ -45,7 +45,9 @@ enum {
     WM_ERR_CELL = 4,         /* a particle outside nxs..nxe, or moved more than one row in a step  */
     WM_ERR_CUDA = 5,         /* a CUDA runtime call failed                                         */
     WM_ERR_NOT_INIT = 6,     /* *_init was not called first (the reference stops there)           */
-    WM_ERR_UNSUPPORTED = 7   /* option outside the periodic single-GPU path                        */
+    WM_ERR_UNSUPPORTED = 7,  /* option outside the supported single-GPU path                       */
+    WM_ERR_IO = 8            /* a snapshot/output file could not be opened, written or read, or its
+                                contents do not match the module parameters (paraio.f90 stops)   */
 };
 
 enum { WM_PREC_FP64 = 0, WM_PREC_MIXED = 1 };
@@ -191,6 +193,23 @@ int wm_sim_energy(wm_sim *s, double *out);
 /* mom_calc__accl + mom_calc__nvt + boundary_periodic__mom on the resident state, into a host
  * array mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp). */
 int wm_sim_moments(wm_sim *s, double *mom);
+/* Snapshot and output files of the resident state, in the format of common/paraio.f90 for one
+ * rank (a <name>.json description and a <name>.raw data file; `dir` is a prefix joined to the
+ * file name as the Fortran does, so it ends in '/').  The data are put into file order on the GPU
+ * (moments, cell-centred fields, ordered compaction of particles) and streamed to disk.
+ *   write_snapshot   = paraio__output (paraio.f90:93-222) with nxs = nxgs, nxe = nxge; slots
+ *                      beyond a row's count are written as zeros
+ *   read_snapshot    = paraio__input (:227-417) followed by wm_sim_load; *it = the step
+ *   write_moments    = mom_calc__accl/__nvt + boundary__mom, then paraio__mom (:555-713), file
+ *                      <it:07d>_mom
+ *   write_particles  = paraio__ptcl (tracers_only = 0, file <it:07d>_ptcl) or paraio__orb (1,
+ *                      ids > 0, <it:07d>_orb), write_particle (:743-849).  In the mixed path the
+ *                      particles of a cell follow that path's order (the FP64 path keeps the
+ *                      reference's). */
+int wm_sim_write_snapshot(wm_sim *s, const char *dir, const char *filename, int it);
+int wm_sim_read_snapshot(wm_sim *s, const char *dir, const char *filename, int *it);
+int wm_sim_write_moments(wm_sim *s, const char *dir, int it);
+int wm_sim_write_particles(wm_sim *s, const char *dir, int it, int tracers_only);
 /* CG iterations per component of the last step. */
 int wm_sim_cg_iters(wm_sim *s, int *iters3);
 /* Per-kernel GPU time of the last wm_sim_step call, from CUDA events on the simulation's
@@ -247,6 +266,33 @@ int wm_deposit_current_noalloc(const double *up, const double *gp, const int *cu
 /* Page-lock (pin) a host buffer so that copies from and to it run at full link speed. */
 int wm_host_register(void *ptr, size_t bytes);
 int wm_host_unregister(void *ptr);
+
+/* Allocate / free page-locked host memory (cudaHostAlloc, portable across devices).  The state
+ * arrays up and uf that wm_sim_step_host copies every call are best placed here: the copy engines
+ * reach their full rate on such memory whatever the CPU did to it before, while a buffer that was
+ * registered after the CPU first touched it can copy several times slower on Grace hosts. */
+int wm_host_alloc(void **ptr, size_t bytes);
+int wm_host_free(void *ptr);
+
+/* -------------------------------------------------------------- module paraio (host arrays)
+ * common/paraio.f90, procedure for procedure, for one rank (nproc = 1; other values return
+ * WM_ERR_UNSUPPORTED).  Host-side file I/O on the caller's arrays in the reference layout; the
+ * file pair is <dir><name>.json + <dir><name>.raw.  Where the Fortran stops (uninitialised
+ * module, parameter mismatch on input) these return WM_ERR_NOT_INIT / WM_ERR_IO.  The GPU-resident
+ * state is written by the wm_sim_write_* functions above instead. */
+int wm_paraio_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int nyge, int nys, int nye, int nproc, int nrank,
+                   double delx, double delt, double c, const double *q, const double *r, const char *dir); /* :37-72 */
+int wm_paraio_finalize(void);                                                                     /* :77-85 */
+int wm_paraio_output(const double *up, const double *uf, const int *np2, int nxs, int nxe, int it,
+                     const char *filename);                                                       /* :93-222 */
+int wm_paraio_input(double *up, double *uf, int *np2, int *nxs, int *nxe, int *it, const char *filename); /* :227-417 */
+int wm_paraio_param(int n0, double wpe, double wpi, double wge, double wgi, double vti, double vte,
+                    const char *filename);                                                        /* :422-550 */
+/* mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp) is intent(inout): velocity and temperature rows are
+ * divided by the density in place, ghost cells included, as the Fortran does (:641-660). */
+int wm_paraio_mom(double *mom, const double *uf, int it);                                         /* :555-713 */
+int wm_paraio_ptcl(const double *up, const double *uf, const int *np2, int it);                   /* :718-726 */
+int wm_paraio_orb(const double *up, const double *uf, const int *np2, int it);                    /* :731-738 */
 
 /* ------------------------------------------------- learned initial guess for the implicit solve
  * No reference counterpart: the reference starts its CG (common/field.f90:319-461) from the

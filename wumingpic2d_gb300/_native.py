@@ -12,7 +12,7 @@ LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libwmpic2d.so"
 
 STATUS = {
     0: "WM_OK", 1: "WM_ERR_CG_MAXITER", 2: "WM_ERR_OVERFLOW", 3: "WM_ERR_BAD_ARG", 4: "WM_ERR_CELL",
-    5: "WM_ERR_CUDA", 6: "WM_ERR_NOT_INIT", 7: "WM_ERR_UNSUPPORTED",
+    5: "WM_ERR_CUDA", 6: "WM_ERR_NOT_INIT", 7: "WM_ERR_UNSUPPORTED", 8: "WM_ERR_IO",
 }
 WM_PREC_FP64, WM_PREC_MIXED = 0, 1
 
@@ -98,6 +98,20 @@ SIGNATURES = {
     "wm_deposit_current_noalloc": [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _P, _P],
     "wm_host_register": [_P, ctypes.c_size_t],
     "wm_host_unregister": [_P],
+    "wm_host_alloc": [_P, ctypes.c_size_t],
+    "wm_host_free": [_P],
+    "wm_sim_write_snapshot": [_P, ctypes.c_char_p, ctypes.c_char_p, _I],
+    "wm_sim_read_snapshot": [_P, ctypes.c_char_p, ctypes.c_char_p, _P],
+    "wm_sim_write_moments": [_P, ctypes.c_char_p, _I],
+    "wm_sim_write_particles": [_P, ctypes.c_char_p, _I, _I],
+    "wm_paraio_init": [_I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _P, _P, ctypes.c_char_p],
+    "wm_paraio_finalize": [],
+    "wm_paraio_output": [_P, _P, _P, _I, _I, _I, ctypes.c_char_p],
+    "wm_paraio_input": [_P, _P, _P, _P, _P, _P, ctypes.c_char_p],
+    "wm_paraio_param": [_I, _D, _D, _D, _D, _D, _D, ctypes.c_char_p],
+    "wm_paraio_mom": [_P, _P, _I],
+    "wm_paraio_ptcl": [_P, _P, _P, _I],
+    "wm_paraio_orb": [_P, _P, _P, _I],
     "wm_cnn_conv3x3": [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P, _P],
     "wm_cnn_conv3x3_wgrad": [_P, _P, _I, _I, _I, _I, _I, _I, _I, _P, _P, _P, ctypes.c_int64, _P],
     "wm_cnn_mse": [_P, _P, ctypes.c_int64, _P, _P, _I, _P, _P],

@@ -13,6 +13,8 @@ the reference calls `stop` raise WmError.
         __curre / __phi / __mom             common/boundary_periodic.f90:26-636
     boundary_reconnection__*                proj/reconnection/boundary_reconnection.f90:26-647
     boundary_shock__* (with __injection)    proj/shock/boundary_shock.f90:27-693
+    paraio__init / __output / __input / __param / __mom / __ptcl / __orb
+                                            common/paraio.f90:37-849 (host file I/O)
 
 field__fdtd_i takes the three boundary procedures as arguments in the
 reference; here the boundary module whose *__init ran last supplies them (pass
@@ -227,6 +229,52 @@ def boundary_shock__phi(phi, nxs, nxe, nys, nye, l):
 
 def boundary_shock__mom(mom):
     check(lib().wm_bc_shock_mom(_p(_f64(mom, "mom"))), "boundary_shock__mom")
+
+
+# ---------------------------------------------------------------- paraio.f90
+def _name(s: str) -> bytes:
+    return s.encode()
+
+
+def paraio__init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, nproc, nrank, delx, delt, c, q, r, dir):
+    """dir is a prefix joined to the file names, as in the Fortran (end it with '/')."""
+    q = _qr(q, nsp)
+    r = _qr(r, nsp)
+    check(lib().wm_paraio_init(ndim, np_, nsp, nxgs, nxge, nygs, nyge, nys, nye, nproc, nrank, delx, delt, c, _p(q), _p(r),
+                               _name(dir)), "paraio__init")
+
+
+def paraio__finalize():
+    check(lib().wm_paraio_finalize(), "paraio__finalize")
+
+
+def paraio__output(up, uf, np2, nxs, nxe, it, filename):
+    check(lib().wm_paraio_output(_p(_f64(up, "up")), _p(_f64(uf, "uf")), _p(_i32(np2, "np2")), nxs, nxe, it, _name(filename)),
+          "paraio__output")
+
+
+def paraio__input(up, uf, np2, filename):
+    """Fills up, uf, np2 in place; returns (nxs, nxe, it), the Fortran's intent(out) scalars."""
+    v = (ctypes.c_int * 3)()
+    check(lib().wm_paraio_input(_p(_f64(up, "up")), _p(_f64(uf, "uf")), _p(_i32(np2, "np2")), ctypes.byref(v, 0),
+                                ctypes.byref(v, 4), ctypes.byref(v, 8), _name(filename)), "paraio__input")
+    return v[0], v[1], v[2]
+
+
+def paraio__param(n0, wpe, wpi, wge, wgi, vti, vte, filename):
+    check(lib().wm_paraio_param(n0, wpe, wpi, wge, wgi, vti, vte, _name(filename)), "paraio__param")
+
+
+def paraio__mom(mom, uf, it):
+    check(lib().wm_paraio_mom(_p(_f64(mom, "mom")), _p(_f64(uf, "uf")), it), "paraio__mom")
+
+
+def paraio__ptcl(up, uf, np2, it):
+    check(lib().wm_paraio_ptcl(_p(_f64(up, "up")), _p(_f64(uf, "uf")), _p(_i32(np2, "np2")), it), "paraio__ptcl")
+
+
+def paraio__orb(up, uf, np2, it):
+    check(lib().wm_paraio_orb(_p(_f64(up, "up")), _p(_f64(uf, "uf")), _p(_i32(np2, "np2")), it), "paraio__orb")
 
 
 # ------------------------------------------------------------- diagnostics

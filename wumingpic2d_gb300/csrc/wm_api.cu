@@ -723,6 +723,7 @@ const char *wm_status_string(int s)
     case WM_ERR_CUDA: return "CUDA error";
     case WM_ERR_NOT_INIT: return "module not initialised";
     case WM_ERR_UNSUPPORTED: return "unsupported option";
+    case WM_ERR_IO: return "snapshot/output file error";
     default: return "unknown status";
     }
 }

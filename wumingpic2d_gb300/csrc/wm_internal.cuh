@@ -28,6 +28,7 @@ struct WmConst {
     double q[WM_MAX_SP], r[WM_MAX_SP];
     double cg_err;
     int cg_itemax;
+    double u0;  // shock: upstream four-velocity of the injection boundary
 };
 
 // ------------------------------------------------------------------ particles

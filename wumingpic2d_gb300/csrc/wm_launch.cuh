@@ -121,3 +121,10 @@ size_t wm_cnn_param_count();
 int wm_cnn_net_prepare(WmCnnNet &net, cudaStream_t st);
 int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf, FView<3, false> uj, const WmCnnWork &w, double *cand,
                        cudaStream_t st);
+
+// wm_paraio.cu: the resident state in the order of the paraio files
+int wm_launch_mom_file(const WmGeom &g, const double *mom, FView<6, false> uf, double *out, cudaStream_t st);
+int wm_launch_uf_interior(const WmGeom &g, FView<6, false> uf, double *out, cudaStream_t st);
+int wm_launch_row_count(int nrows, const double *stage, int pitch, const int *np2, int mode, long long *cnt, cudaStream_t st);
+int wm_launch_row_compact(int nrows, const double *stage, int pitch, const int *np2, int mode, const long long *off, double *out,
+                          cudaStream_t st);

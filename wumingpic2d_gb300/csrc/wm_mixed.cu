@@ -35,7 +35,23 @@ constexpr unsigned FULL = 0xffffffffu;
 struct MxConst {
     float fac1[WM_MAX_SP], txxx[WM_MAX_SP], fac2[WM_MAX_SP], mqdd[WM_MAX_SP], q[WM_MAX_SP];
     float dt_dx, inv_c2, c2;
+    // walls in x (WM_BC_RECONNECTION, WM_BC_SHOCK); the shock's injection boundary
+    // xend - nxgs*delx = xe_cell + xe_off (in cells) and its four-velocity u0
+    int bc, xe_cell;
+    float xe_off, u0;
 };
+
+// A particle at interior cell cn + offset off (cell units) mirrored about the wall at interior
+// position w: cn' + off' = 2w - (cn + off).
+__device__ __forceinline__ void mirror(int w2, int &cn, float &off)
+{
+    if (off == 0.f) {
+        cn = w2 - cn;
+    } else {
+        cn = w2 - cn - 1;
+        off = 1.f - off;
+    }
+}
 
 __device__ __forceinline__ void shape3(float h, float &a0, float &a1, float &a2)
 {
@@ -112,6 +128,7 @@ __global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__
 // a lane past the end of its cell runs on a zero particle with zero deposit weights and its stores
 // switched off.  Each lane's next particle is copied into shared memory (cp.async) while the
 // current one is pushed.
+template <int BC>  // WM_BC_*: the walls' code is compiled only where it runs
 __global__ void __launch_bounds__(MX_THREADS, 512 / MX_THREADS)
     k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const float *__restrict__ fcc, const int *__restrict__ cumcnt,
                          unsigned *__restrict__ code, int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status)
@@ -278,6 +295,27 @@ __global__ void __launch_bounds__(MX_THREADS, 512 / MX_THREADS)
         incx += ox;
         incy += oy;
         bad |= valid & (incx < -1 || incx > 1 || incy < -1 || incy > 1);
+        float ig_dep = ig;
+        if constexpr (BC == WM_BC_SHOCK) {  // the injection boundary acts before the deposit (proj/shock/app.f90:112-117)
+            int cn = cg + incx;
+            if (cn < 1) {  // wall at nxs+1 (boundary_shock.f90:272-276)
+                mirror(2, cn, nx1);
+                u1 = -u1;
+                u2 = -u2;
+                u3 = -u3;
+            } else if (cn > kc.xe_cell || (cn == kc.xe_cell && nx1 > kc.xe_off)) {  // beyond xend (:277-281)
+                const float v = 2.f * kc.xe_off - nx1;
+                const float fl = floorf(v);
+                cn = 2 * kc.xe_cell - cn + (int)fl;
+                nx1 = v - fl;
+                u1 = 2.f * kc.u0 - u1;
+                u2 = -u2;
+                u3 = -u3;
+                ig_dep = rsqrtf(1.f + (u1 * u1 + u2 * u2 + u3 * u3) * kc.inv_c2);
+            }
+            incx = cn - cg;
+            bad |= valid & (incx < -1 || incx > 1);
+        }
         // Esirkepov: old shape on nodes 1..3 about the old cell, new shape on 1+inc..3+inc
         float dsx[5], dsy[5];
         {
@@ -299,7 +337,7 @@ __global__ void __launch_bounds__(MX_THREADS, 512 / MX_THREADS)
         }
         const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f}, s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
         const float mq = valid ? mqdd : 0.f;           // zero weights for a lane past its cell
-        const float qg = valid ? qs * u3 * ig : 0.f;
+        const float qg = valid ? qs * u3 * ig_dep : 0.f;
         float cx[4], cy[4];
         cx[0] = dsx[0];
         cy[0] = dsy[0];
@@ -328,6 +366,16 @@ __global__ void __launch_bounds__(MX_THREADS, 512 / MX_THREADS)
             const float fx = mq * ((ip >= 1 && ip <= 3) ? s0x[ip] + 0.5f * dsx[ip] : 0.5f * dsx[ip]);
 #pragma unroll
             for (int m = 0; m < 4; ++m) ay[m][ip] = fmaf(fx, cy[m], ay[m][ip]);
+        }
+        if constexpr (BC == WM_BC_RECONNECTION) {  // particle_x after the field solve (boundary_reconnection.f90:80-91)
+            int cn = cg + incx;
+            if (cn < 1 || cn >= g.nx - 2) {
+                mirror(cn < 1 ? 2 : 2 * (g.nx - 2), cn, nx1);
+                u1 = -u1;
+                u2 = -u2;
+                u3 = -u3;
+            }
+            incx = cn - cg;
         }
         // direction d = (dy+1)*3 + dx+1 and the rank among this cell's particles moving that way,
         // in particle order: the lanes of a cell with the same d this round, plus earlier rounds
@@ -576,9 +624,22 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
     kc.dt_dx = (float)(k.delt / k.delx);
     kc.inv_c2 = (float)(1.0 / (k.c * k.c));
     kc.c2 = (float)(k.c * k.c);
+    kc.bc = g.bc;
+    {  // xend of boundary_shock.f90:266 in interior cells
+        const double xend = g.nxge * k.delx + k.u0 / sqrt(1 + (k.u0 * k.u0) / (k.c * k.c)) * k.delt;
+        const double xe = xend / k.delx - g.nxgs;
+        kc.xe_cell = (int)floor(xe);
+        kc.xe_off = (float)(xe - kc.xe_cell);
+        kc.u0 = (float)k.u0;
+    }
     dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
-    k_mixed_push_deposit<<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, reinterpret_cast<unsigned *>(sc.key), cnt9, jtile,
-                                                       sc.status);
+    unsigned *code = reinterpret_cast<unsigned *>(sc.key);
+    if (g.bc == WM_BC_RECONNECTION)
+        k_mixed_push_deposit<WM_BC_RECONNECTION><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, code, cnt9, jtile, sc.status);
+    else if (g.bc == WM_BC_SHOCK)
+        k_mixed_push_deposit<WM_BC_SHOCK><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, code, cnt9, jtile, sc.status);
+    else
+        k_mixed_push_deposit<WM_BC_PERIODIC><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, code, cnt9, jtile, sc.status);
     return wm_check_launch("k_mixed_push_deposit");
 }
 

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "wm_launch.cuh"
+#include "wm_pio.cuh"
 
 namespace {
 
@@ -72,6 +73,7 @@ struct wm_sim {
     DevBuf A[6], B[6];
     DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out, jtile, fcc, stage2;
     DevBuf cumcnt_alt, mx_cnt9, mx_off9;  // mixed path: new cumcnt, per-cell direction counts and offsets
+    DevBuf mom_dev, out_dev, out_cnt;     // moments and the file-ordered data of the paraio outputs
     // learned CG guess (off until wm_sim_set_guess)
     DevBuf cnn_params, cnn_wf[WM_CNN_LAYERS], cnn_x, cnn_a0, cnn_a1, cnn_pred, cnn_partial, cnn_scale, guess_cand, guess_stats;
     WmCnnNet net{};
@@ -259,6 +261,7 @@ struct wm_sim {
             B[c].release();
         }
         for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &stage2,
+                          &mom_dev, &out_dev, &out_cnt,
                           &f_uf, &f_uj, &f_df, &f_pj, &f_b, &f_r, &f_p, &f_ap, &f_partial, &f_ticket, &f_scal, &rb_dir, &rb_ord,
                           &rb_P, &rb_key, &rb_holes, &rb_nup, &rb_ndown, &rb_cellcnt, &rb_pairs, &rb_status})
             b->release();
@@ -289,12 +292,13 @@ struct wm_sim {
     }
 
     // Upload a reference-layout particle array (np slots per row, np2 used) into set S.
-    int upload_particles(const double *up, const int *np2_h, DevBuf *S)
+    // up: host rows of `host_pitch` slots (6 doubles each); the reference layout has np slots
+    int upload_particles(const double *up, const int *np2_h, DevBuf *S, int host_pitch)
     {
         const int maxc = std::max(1, *std::max_element(np2_h, np2_h + g.nrows));
-        if (maxc > g.np) return WM_ERR_BAD_ARG;
+        if (maxc > g.np || maxc > host_pitch) return WM_ERR_BAD_ARG;
         WM_TRY(stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
-        WM_CUDA(cudaMemcpy2DAsync(stage.p, sizeof(double) * 6 * maxc, up, sizeof(double) * 6 * g.np, sizeof(double) * 6 * maxc,
+        WM_CUDA(cudaMemcpy2DAsync(stage.p, sizeof(double) * 6 * maxc, up, sizeof(double) * 6 * host_pitch, sizeof(double) * 6 * maxc,
                                   g.nrows, cudaMemcpyHostToDevice, st));
         pmark("copy_in_h2d");
         WM_CUDA(cudaMemcpyAsync(np2[cur].p, np2_h, sizeof(int) * g.nrows, cudaMemcpyHostToDevice, st));
@@ -438,11 +442,11 @@ int wm_sim_create(const wm_sim_config *cfg, wm_sim **out)
     if (cfg->nsp < 1 || cfg->nsp > WM_MAX_SP || cfg->nx < 4 || cfg->ny < 4 || cfg->np < 1) return WM_ERR_BAD_ARG;
     if (cfg->cg_itemax < 1 || !(cfg->cg_err > 0)) return WM_ERR_BAD_ARG;
     if (cfg->bc != WM_BC_PERIODIC && cfg->bc != WM_BC_RECONNECTION && cfg->bc != WM_BC_SHOCK) return WM_ERR_BAD_ARG;
-    if (cfg->bc != WM_BC_PERIODIC && cfg->precision == WM_PREC_MIXED) return WM_ERR_UNSUPPORTED;
     wm_sim *s = new wm_sim();
     WmGeom &g = s->g;
     g.bc = cfg->bc;
     s->u0 = cfg->u0;
+    s->k.u0 = cfg->u0;
     g.ndim = 6;
     g.np = cfg->np;
     g.nsp = cfg->nsp;
@@ -489,8 +493,10 @@ int wm_sim_destroy(wm_sim *s)
     return WM_OK;
 }
 
-static int sim_load_common(wm_sim *s, const double *up, const double *uf, const int *np2_h, const int *cumcnt_h)
+static int sim_load_common(wm_sim *s, const double *up, const double *uf, const int *np2_h, const int *cumcnt_h,
+                           int host_pitch = -1)
 {
+    if (host_pitch < 0) host_pitch = s->g.np;
     const WmGeom &g = s->g;
     long long ntot = 0;
     for (int r = 0; r < g.nrows; ++r) {
@@ -503,11 +509,11 @@ static int sim_load_common(wm_sim *s, const double *up, const double *uf, const 
     if (!s->loaded || cap > s->cap) WM_TRY(s->alloc(cap));
     s->ntot = ntot;
     if (cumcnt_h) {  // already sorted: upload straight into A
-        WM_TRY(s->upload_particles(up, np2_h, s->A));
+        WM_TRY(s->upload_particles(up, np2_h, s->A, host_pitch));
         s->pid_cur = 0;
         WM_CUDA(cudaMemcpyAsync(s->cumcnt.p, cumcnt_h, sizeof(int) * (size_t)(g.nx + 1) * g.nrows, cudaMemcpyHostToDevice, s->st));
     } else {
-        WM_TRY(s->upload_particles(up, np2_h, s->B));
+        WM_TRY(s->upload_particles(up, np2_h, s->B, host_pitch));
         WM_TRY(s->sort_B_into_A());
     }
     WM_TRY(s->upload_fields(uf));
@@ -528,26 +534,42 @@ int wm_sim_load(wm_sim *s, const double *up, const double *uf, const int *np2_h)
     return sim_load_common(s, up, uf, np2_h, nullptr);
 }
 
+// Row counts of the current state (host copy) and their maximum.
+static int sim_row_counts(wm_sim *s, std::vector<int> &cnt, int &maxc)
+{
+    const WmGeom &g = s->g;
+    cnt.resize(g.nrows);
+    WM_CUDA(cudaMemcpyAsync(cnt.data(), s->np2[s->cur].p, sizeof(int) * g.nrows, cudaMemcpyDeviceToHost, s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    maxc = std::max(1, *std::max_element(cnt.begin(), cnt.end()));
+    return WM_OK;
+}
+
+// The current particles as reference-layout rows in s->stage: 6 doubles per slot, `pitch` slots
+// per row, slots past a row's count zero.
+static int sim_pack_stage(wm_sim *s, int pitch)
+{
+    const WmGeom &g = s->g;
+    WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)pitch * g.nrows));
+    if (s->mixed())
+        return wm_launch_mixed_pack(g, s->mview(s->A, s->cur, s->pid_cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), pitch,
+                                    s->stage.as<double>(), s->st);
+    dim3 grid(std::min(wm_div_up(pitch, 256), 64u), g.nrows);
+    k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), pitch, s->stage.as<double>());
+    return wm_check_launch("k_pack");
+}
+
 int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
 {
     if (!s || !s->loaded) return WM_ERR_NOT_INIT;
     const WmGeom &g = s->g;
-    std::vector<int> cnt(g.nrows);
-    WM_CUDA(cudaMemcpyAsync(cnt.data(), s->np2[s->cur].p, sizeof(int) * g.nrows, cudaMemcpyDeviceToHost, s->st));
-    WM_CUDA(cudaStreamSynchronize(s->st));
-    const int maxc = std::max(1, *std::max_element(cnt.begin(), cnt.end()));
+    std::vector<int> cnt;
+    int maxc;
+    WM_TRY(sim_row_counts(s, cnt, maxc));
     if (maxc > g.np) return WM_ERR_OVERFLOW;
     s->pmark("store_start");
     if (up) {
-        WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
-        dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
-        if (s->mixed()) {
-            WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur, s->pid_cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), maxc,
-                                        s->stage.as<double>(), s->st));
-        } else {
-            k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), maxc, s->stage.as<double>());
-            WM_TRY(wm_check_launch("k_pack"));
-        }
+        WM_TRY(sim_pack_stage(s, maxc));
         s->pmark("copy_out_pack");
         WM_CUDA(cudaMemcpy2DAsync(up, sizeof(double) * 6 * g.np, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * maxc,
                                   g.nrows, cudaMemcpyDeviceToHost, s->st));
@@ -649,11 +671,13 @@ int wm_sim_energy(wm_sim *s, double *out)
     return WM_OK;
 }
 
-int wm_sim_moments(wm_sim *s, double *mom)
+// mom_calc__accl + mom_calc__nvt + boundary__mom of the current state into s->mom_dev
+// (reference layout mom(7, nxgs-1:nxge+1, nys-1:nye+1, nsp)).
+static int sim_moments_device(wm_sim *s)
 {
-    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
     const WmGeom &g = s->g;
     const size_t nm = (size_t)7 * (g.nx + 2) * (g.ny + 2) * g.nsp;
+    WM_TRY(s->mom_dev.ensure(sizeof(double) * nm));
     if (s->mixed()) {
         // moment steps are rare: expand the mixed state to FP64 rows (pitch = largest row) and run
         // the FP64 half-step push and moment deposit on that copy
@@ -662,27 +686,209 @@ int wm_sim_moments(wm_sim *s, double *mom)
         WM_CUDA(cudaStreamSynchronize(s->st));
         const int pitch = std::max(1, *std::max_element(cnt.begin(), cnt.end()));
         const size_t nstage = (size_t)6 * pitch * g.nrows;
-        WM_TRY(s->uf_aos.ensure(sizeof(double) * nm));
         WM_TRY(s->stage.ensure(sizeof(double) * nstage));
         WM_TRY(s->stage2.ensure(sizeof(double) * nstage));
         WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur, s->pid_cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), pitch,
                                     s->stage.as<double>(), s->st));
         AoSView va{s->stage.as<double>(), pitch}, vb{s->stage2.as<double>(), pitch};
         WM_TRY(wm_launch_push(g, s->k, va, vb, s->uf(), s->cumcnt.as<int>(), 1, 0, s->st));
-        WM_TRY(wm_launch_mom_nvt(g, s->k, vb, s->np2[s->cur].as<int>(), s->uf_aos.as<double>(), pitch, s->st));
-        WM_TRY(wm_launch_mom_bc(g, s->uf_aos.as<double>(), s->st));
-        WM_CUDA(cudaMemcpyAsync(mom, s->uf_aos.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s->st));
-        WM_CUDA(cudaStreamSynchronize(s->st));
-        return WM_OK;
+        WM_TRY(wm_launch_mom_nvt(g, s->k, vb, s->np2[s->cur].as<int>(), s->mom_dev.as<double>(), pitch, s->st));
+    } else {
+        SoAView va = s->view(s->A, s->cur), vb = s->view(s->B, s->cur);
+        WM_TRY(wm_launch_push(g, s->k, va, vb, s->uf(), s->cumcnt.as<int>(), 1, 0, s->st));
+        WM_TRY(wm_launch_mom_nvt(g, s->k, vb, s->np2[s->cur].as<int>(), s->mom_dev.as<double>(), s->max_row, s->st));
     }
-    SoAView va = s->view(s->A, s->cur), vb = s->view(s->B, s->cur);
-    WM_TRY(wm_launch_push(g, s->k, va, vb, s->uf(), s->cumcnt.as<int>(), 1, 0, s->st));
-    WM_TRY(s->stage.ensure(sizeof(double) * nm));
-    WM_TRY(wm_launch_mom_nvt(g, s->k, vb, s->np2[s->cur].as<int>(), s->stage.as<double>(), s->max_row, s->st));
-    WM_TRY(wm_launch_mom_bc(g, s->stage.as<double>(), s->st));
-    WM_CUDA(cudaMemcpyAsync(mom, s->stage.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, s->st));
+    return wm_launch_mom_bc(g, s->mom_dev.as<double>(), s->st);
+}
+
+int wm_sim_moments(wm_sim *s, double *mom)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    if (!mom) return WM_ERR_BAD_ARG;
+    const WmGeom &g = s->g;
+    WM_TRY(sim_moments_device(s));
+    WM_CUDA(cudaMemcpyAsync(mom, s->mom_dev.p, sizeof(double) * 7 * (g.nx + 2) * (g.ny + 2) * g.nsp, cudaMemcpyDeviceToHost, s->st));
     WM_CUDA(cudaStreamSynchronize(s->st));
     return WM_OK;
+}
+
+// ------------------------------------------------- snapshot and output files from the GPU
+// The module parameters paraio__init would hold for this simulation (one rank, ndim = 6).
+static wmpio::Params sim_pio_params(const wm_sim *s)
+{
+    const WmGeom &g = s->g;
+    wmpio::Params P;
+    P.ndim = 6;
+    P.np = g.np;
+    P.nsp = g.nsp;
+    P.nxgs = g.nxgs;
+    P.nxge = g.nxge;
+    P.nygs = g.nygs;
+    P.nyge = g.nyge;
+    P.nys = g.nys;
+    P.nye = g.nye;
+    P.nproc = 1;
+    P.delx = s->k.delx;
+    P.delt = s->k.delt;
+    P.c = s->k.c;
+    for (int i = 0; i < g.nsp; ++i) {
+        P.q[i] = s->k.q[i];
+        P.r[i] = s->k.r[i];
+    }
+    return P;
+}
+
+int wm_sim_write_snapshot(wm_sim *s, const char *dir, const char *filename, int it)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    if (!dir || !filename) return WM_ERR_BAD_ARG;
+    const WmGeom &g = s->g;
+    std::vector<int> cnt;
+    int maxc;
+    WM_TRY(sim_row_counts(s, cnt, maxc));
+    if (maxc > g.np) return WM_ERR_OVERFLOW;
+    WM_TRY(sim_pack_stage(s, maxc));
+    const wmpio::Params P = sim_pio_params(s);
+    wmpio::Writer w;
+    WM_TRY(w.open(dir, filename));
+    WM_TRY(wmpio::write_head(w, P, it, {{"nxs", g.nxgs}, {"nxe", g.nxge}}));
+    WM_TRY(w.dataset("up", "f8", {6, g.np, g.ny, g.nsp, 1}, "particles"));
+    WM_TRY(wmpio::write_rows_from_device(w, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * g.np, g.nrows, s->st));
+    WM_TRY(w.dataset("np2", "i4", {g.ny, g.nsp, 1}, "number of active particles"));
+    WM_TRY(w.write(cnt.data(), sizeof(int) * g.nrows));
+    const long long npts = (long long)g.nxw * g.nyw;
+    WM_TRY(s->uf_aos.ensure(sizeof(double) * 6 * npts));
+    WM_TRY(wm_launch_soa_to_aos(6, npts, s->f_uf.as<double>(), s->uf_aos.as<double>(), s->st));
+    WM_TRY(w.dataset("uf", "f8", {6, g.nxw, g.nyw, 1}, "electromagnetic fields including ghost cells"));
+    WM_TRY(wmpio::write_from_device(w, s->uf_aos.p, sizeof(double) * 6 * npts, s->st));
+    return w.close();
+}
+
+int wm_sim_read_snapshot(wm_sim *s, const char *dir, const char *filename, int *it)
+{
+    if (!s || !dir || !filename || !it) return WM_ERR_BAD_ARG;
+    const WmGeom &g = s->g;
+    wmpio::Reader rd;
+    WM_TRY(rd.open(dir, filename));
+    const wmpio::Params P = sim_pio_params(s);
+    const char *names[8] = {"ndim", "np", "nxgs", "nxge", "nygs", "nyge", "nsp", "nproc"};
+    const int want[8] = {6, P.np, P.nxgs, P.nxge, P.nygs, P.nyge, P.nsp, 1};
+    for (int i = 0; i < 8; ++i) {
+        int v;
+        WM_TRY(rd.read_i4(names[i], v));
+        if (v != want[i]) return WM_ERR_IO;  // paraio.f90:329-340
+    }
+    int nxs, nxe;
+    WM_TRY(rd.read_i4("it", *it));
+    WM_TRY(rd.read_i4("nxs", nxs));
+    WM_TRY(rd.read_i4("nxe", nxe));
+    if (nxs != g.nxgs || nxe != g.nxge) return WM_ERR_UNSUPPORTED;
+    wmpio::Entry e_up, e_np2, e_uf;
+    WM_TRY(rd.find("dataset", "up", e_up));
+    WM_TRY(rd.find("dataset", "np2", e_np2));
+    WM_TRY(rd.find("dataset", "uf", e_uf));
+    if (e_up.shape != std::vector<long long>{6, g.np, g.ny, g.nsp, 1} || e_np2.shape != std::vector<long long>{g.ny, g.nsp, 1} ||
+        e_uf.shape != std::vector<long long>{6, g.nxw, g.nyw, 1})
+        return WM_ERR_IO;
+    std::vector<int> np2_h(g.nrows);
+    WM_TRY(rd.read(e_np2, np2_h.data(), sizeof(int) * g.nrows));
+    int maxc = 1;
+    for (int r = 0; r < g.nrows; ++r) {
+        if (np2_h[r] < 0 || np2_h[r] > g.np) return WM_ERR_IO;
+        maxc = std::max(maxc, np2_h[r]);
+    }
+    std::vector<double> uf_h((size_t)6 * g.nxw * g.nyw);
+    WM_TRY(rd.read(e_uf, uf_h.data(), sizeof(double) * uf_h.size()));
+    // only the active part of each row (the first maxc slots) is read, into page-locked memory
+    const size_t row_bytes = sizeof(double) * 6 * (size_t)maxc;
+    double *up_h = nullptr;
+    WM_CUDA(cudaHostAlloc((void **)&up_h, row_bytes * g.nrows, cudaHostAllocPortable));
+    int st = WM_OK;
+    for (int r = 0; r < g.nrows && st == WM_OK; ++r) {
+        wmpio::Entry row = e_up;
+        row.offset = e_up.offset + (long long)r * sizeof(double) * 6 * g.np;
+        st = rd.read(row, (char *)up_h + r * row_bytes, row_bytes);
+    }
+    if (st == WM_OK) st = sim_load_common(s, up_h, uf_h.data(), np2_h.data(), nullptr, maxc);
+    cudaFreeHost(up_h);
+    return st;
+}
+
+int wm_sim_write_moments(wm_sim *s, const char *dir, int it)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    if (!dir) return WM_ERR_BAD_ARG;
+    const WmGeom &g = s->g;
+    WM_TRY(sim_moments_device(s));
+    const long long ncs = (long long)g.nx * g.ny * g.nsp, nc = (long long)g.nx * g.ny;
+    WM_TRY(s->out_dev.ensure(sizeof(double) * (7 * ncs + 6 * nc)));
+    WM_TRY(wm_launch_mom_file(g, s->mom_dev.as<double>(), s->uf(), s->out_dev.as<double>(), s->st));
+    const wmpio::Params P = sim_pio_params(s);
+    char name[32];
+    snprintf(name, sizeof name, "%07d_mom", it);
+    wmpio::Writer w;
+    WM_TRY(w.open(dir, name));
+    WM_TRY(wmpio::write_head(w, P, it, {}));
+    const double *o = s->out_dev.as<double>();
+    WM_TRY(w.dataset("den", "f8", {g.nx, g.ny, g.nsp}, "density"));
+    WM_TRY(wmpio::write_from_device(w, o, sizeof(double) * ncs, s->st));
+    WM_TRY(w.dataset("vel", "f8", {3, g.nx, g.ny, g.nsp}, "velocity"));
+    WM_TRY(wmpio::write_from_device(w, o + ncs, sizeof(double) * 3 * ncs, s->st));
+    WM_TRY(w.dataset("temp", "f8", {3, g.nx, g.ny, g.nsp}, "temperature"));
+    WM_TRY(wmpio::write_from_device(w, o + 4 * ncs, sizeof(double) * 3 * ncs, s->st));
+    WM_TRY(w.dataset("uf", "f8", {6, g.nx, g.ny}, "electromagnetic field"));
+    WM_TRY(wmpio::write_from_device(w, o + 7 * ncs, sizeof(double) * 6 * nc, s->st));
+    return w.close();
+}
+
+int wm_sim_write_particles(wm_sim *s, const char *dir, int it, int tracers_only)
+{
+    if (!s || !s->loaded) return WM_ERR_NOT_INIT;
+    if (!dir) return WM_ERR_BAD_ARG;
+    const WmGeom &g = s->g;
+    const int mode = tracers_only ? 1 : 0;
+    std::vector<int> cnt;
+    int maxc;
+    WM_TRY(sim_row_counts(s, cnt, maxc));
+    WM_TRY(sim_pack_stage(s, maxc));
+    // rows in file order (species, then j), compacted on the GPU with their slot order kept
+    WM_TRY(s->out_cnt.ensure(sizeof(long long) * 2 * g.nrows));
+    long long *dcnt = s->out_cnt.as<long long>(), *doff = dcnt + g.nrows;
+    WM_TRY(wm_launch_row_count(g.nrows, s->stage.as<double>(), maxc, s->np2[s->cur].as<int>(), mode, dcnt, s->st));
+    std::vector<long long> rc(g.nrows), off(g.nrows);
+    WM_CUDA(cudaMemcpyAsync(rc.data(), dcnt, sizeof(long long) * g.nrows, cudaMemcpyDeviceToHost, s->st));
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    long long total = 0;
+    std::vector<long long> nsp_count(g.nsp, 0);
+    for (int r = 0; r < g.nrows; ++r) {
+        off[r] = total;
+        total += rc[r];
+        nsp_count[r / g.ny] += rc[r];
+    }
+    const long long nc = (long long)g.nx * g.ny;
+    WM_TRY(s->out_dev.ensure(sizeof(double) * (6 * std::max(total, 1LL) + 6 * nc)));
+    double *parts = s->out_dev.as<double>(), *ufi = parts + 6 * std::max(total, 1LL);
+    WM_CUDA(cudaMemcpyAsync(doff, off.data(), sizeof(long long) * g.nrows, cudaMemcpyHostToDevice, s->st));
+    WM_TRY(wm_launch_row_compact(g.nrows, s->stage.as<double>(), maxc, s->np2[s->cur].as<int>(), mode, doff, parts, s->st));
+    WM_TRY(wm_launch_uf_interior(g, s->uf(), ufi, s->st));
+    const wmpio::Params P = sim_pio_params(s);
+    char name[32];
+    snprintf(name, sizeof name, "%07d%s", it, mode ? "_orb" : "_ptcl");
+    wmpio::Writer w;
+    WM_TRY(w.open(dir, name));
+    WM_TRY(wmpio::write_head(w, P, it, {}));
+    WM_TRY(w.dataset("uf", "f8", {6, g.nx, g.ny}, "electromagnetic field"));
+    WM_TRY(wmpio::write_from_device(w, ufi, sizeof(double) * 6 * nc, s->st));
+    long long done = 0;
+    for (int isp = 0; isp < g.nsp; ++isp) {
+        char ds[16], desc[64];
+        snprintf(ds, sizeof ds, "up%02d", isp + 1);
+        snprintf(desc, sizeof desc, "particle species #%02d", isp + 1);
+        WM_TRY(w.dataset(ds, "f8", {6, nsp_count[isp]}, desc));
+        WM_TRY(wmpio::write_from_device(w, parts + 6 * done, sizeof(double) * 6 * nsp_count[isp], s->st));
+        done += nsp_count[isp];
+    }
+    return w.close();
 }
 
 int wm_sim_cg_iters(wm_sim *s, int *iters3)
@@ -839,6 +1045,20 @@ int wm_host_register(void *ptr, size_t bytes)
 int wm_host_unregister(void *ptr)
 {
     WM_CUDA(cudaHostUnregister(ptr));
+    return WM_OK;
+}
+
+int wm_host_alloc(void **ptr, size_t bytes)
+{
+    if (!ptr) return WM_ERR_BAD_ARG;
+    *ptr = nullptr;
+    WM_CUDA(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocPortable));
+    return WM_OK;
+}
+
+int wm_host_free(void *ptr)
+{
+    if (ptr) WM_CUDA(cudaFreeHost(ptr));
     return WM_OK;
 }
 

@@ -104,6 +104,30 @@ class Simulation:
         check(lib().wm_sim_moments(self._h, mom.ctypes.data), "wm_sim_moments")
         return mom
 
+    # ------------------------------------------------------- files (common/paraio.f90 format)
+    @staticmethod
+    def _dir(d: str) -> bytes:
+        return (d if d.endswith("/") else d + "/").encode()
+
+    def write_snapshot(self, dirname: str, filename: str, it: int) -> None:
+        """The restart snapshot of paraio__output: <dirname>/<filename>.json + .raw."""
+        check(lib().wm_sim_write_snapshot(self._h, self._dir(dirname), filename.encode(), int(it)), "wm_sim_write_snapshot")
+
+    def read_snapshot(self, dirname: str, filename: str) -> int:
+        """Load a paraio__output snapshot (this library's or the reference's); returns its step."""
+        it = ctypes.c_int()
+        check(lib().wm_sim_read_snapshot(self._h, self._dir(dirname), filename.encode(), ctypes.byref(it)), "wm_sim_read_snapshot")
+        return it.value
+
+    def write_moments(self, dirname: str, it: int) -> None:
+        """paraio__mom of the current moments and fields: <dirname>/<it:07d>_mom.json + .raw."""
+        check(lib().wm_sim_write_moments(self._h, self._dir(dirname), int(it)), "wm_sim_write_moments")
+
+    def write_particles(self, dirname: str, it: int, tracers_only: bool = False) -> None:
+        """paraio__ptcl (all active particles) or paraio__orb (ids > 0): <it:07d>_ptcl / _orb."""
+        check(lib().wm_sim_write_particles(self._h, self._dir(dirname), int(it), int(bool(tracers_only))),
+              "wm_sim_write_particles")
+
     def cg_iters(self) -> np.ndarray:
         out = np.zeros(3, dtype=np.int32)
         check(lib().wm_sim_cg_iters(self._h, out.ctypes.data), "wm_sim_cg_iters")
@@ -168,3 +192,29 @@ def pin(a: np.ndarray) -> None:
 
 def unpin(a: np.ndarray) -> None:
     check(lib().wm_host_unregister(a.ctypes.data), "wm_host_unregister")
+
+
+class _PinnedBlock:
+    """Page-locked host bytes from wm_host_alloc, freed when the last array over them goes."""
+
+    def __init__(self, nbytes: int):
+        p = ctypes.c_void_p()
+        check(lib().wm_host_alloc(ctypes.byref(p), int(nbytes)), "wm_host_alloc")
+        self.ptr, self.nbytes = p.value, int(nbytes)
+        self.__array_interface__ = {"shape": (self.nbytes,), "typestr": "|u1", "data": (self.ptr, False), "version": 3}
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().wm_host_free(self.ptr)
+            self.ptr = None
+
+
+def pinned_zeros(shape, dtype=np.float64, order: str = "F") -> np.ndarray:
+    """A zero-filled array in page-locked host memory (the layout of np.zeros(shape, dtype, order)),
+    for the state that wm_sim_step_host copies in and out every call."""
+    dtype = np.dtype(dtype)
+    n = int(np.prod(shape)) * dtype.itemsize
+    a = np.asarray(_PinnedBlock(max(n, 1)))[:n].view(dtype)
+    a = a.reshape(shape, order=order)
+    a[...] = 0
+    return a
