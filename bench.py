@@ -211,7 +211,7 @@ def make_state(args, dist: Dist):
 
 
 def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
-    from wumingpic2d_gb300.sim import Simulation, pin, set_device, unpin
+    from wumingpic2d_gb300.sim import Simulation, pinned_zeros, set_device
 
     set_device(dist.local)
     cfg, up0, np2, t_init = state
@@ -239,12 +239,14 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
     total = dist.sum(float(ntot)) * args.steps
     value = total / (ms_max / 1e3)
 
-    # e2e through the host-buffer entry point, pinned host state
+    # e2e through the host-buffer entry point; the host state lives in page-locked memory from
+    # wm_host_alloc (registering an existing array instead copies several times slower on Grace)
     e2e = None
     if do_e2e:
-        up_h, uf_h, np2_h, cc_h = sim.store(up=d.alloc_up())
-        pin(up_h)
-        pin(uf_h)
+        up_h = pinned_zeros((d.ndim, d.np, d.ny, d.nsp))
+        uf_h = pinned_zeros((6, d.nx + 4, d.ny + 4))
+        np2_h, cc_h = d.alloc_np2(), d.alloc_cumcnt()
+        sim.store(up_h, uf_h, np2_h, cc_h)
         maxc = int(np2_h.max())
         h2d = 48 * maxc * d.nsp * d.ny + uf_h.nbytes + np2_h.nbytes + cc_h.nbytes
         d2h = h2d
@@ -260,11 +262,9 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
         sim.set_timing(False)
         e2e = {"value": dist.sum(float(ntot)) * args.e2e_steps / dt, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-               "path": "wm_sim_step_host: reference-layout host arrays in and out every step (pinned)",
+               "path": "wm_sim_step_host: reference-layout host arrays (page-locked, wm_host_alloc) in and out every step",
                "phase_ms": phases}
-        unpin(up_h)
-        unpin(uf_h)
-        del up_h
+        del up_h, uf_h
 
     # the same loop with the learned CG initial guess (each component starts from the better of the
     # network's dB and the previous step's; same tolerance)

@@ -208,6 +208,24 @@ int wm_sim_moments(wm_sim *s, double *mom);
  *                      reference's). */
 int wm_sim_write_snapshot(wm_sim *s, const char *dir, const char *filename, int it);
 int wm_sim_read_snapshot(wm_sim *s, const char *dir, const char *filename, int *it);
+/* Seeded initial conditions generated on the GPU (two species: ions, electrons) and loaded as
+ * wm_sim_load would, cell-sorted, with zero dB history.  Random numbers are Philox4x32-10 draws
+ * keyed by `seed` and counted per particle, so a seed gives the same state on any GPU and launch
+ * shape (the CPU restatement is oracle/init.py).
+ *   weibel  ppc*nx particles per row and species at uniform random positions; ions Maxwellian
+ *           (vth_i), electrons Maxwellian (vth_e) drifting along z at +/- v_drift (in c) by slot
+ *           parity; ids 1..n per species; fields zero
+ *   harris  proj/reconnection/app.f90:353-470 (bc = WM_BC_RECONNECTION): nbg background and ncs
+ *           sheet particles per cell, half-thickness lcs (cells), field b0, perturbation e1,
+ *           thermal speeds vte/vti, temperature ratio rtemp = Te/Ti (drifts split by it)
+ *   shock   proj/shock/app.f90:408-525 (bc = WM_BC_SHOCK) with the box at full size: n0 per cell,
+ *           upstream four-velocity u0 (< 0), field b0 at angles theta_bn/phi_bn, damping length
+ *           l_damp_ini, tracer window [xrs, xre] (positive ids) */
+int wm_sim_init_weibel(wm_sim *s, int ppc, double v_drift, double vth_e, double vth_i, uint64_t seed);
+int wm_sim_init_harris(wm_sim *s, int nbg, int ncs, double lcs, double b0, double e1, double vte, double vti, double rtemp,
+                       uint64_t seed);
+int wm_sim_init_shock(wm_sim *s, int n0, double u0, double vth_e, double vth_i, double b0, double theta_bn, double phi_bn,
+                      double l_damp_ini, double xrs, double xre, uint64_t seed);
 int wm_sim_write_moments(wm_sim *s, const char *dir, int it);
 int wm_sim_write_particles(wm_sim *s, const char *dir, int it, int tracers_only);
 /* CG iterations per component of the last step. */

@@ -103,6 +103,9 @@ SIGNATURES = {
     "wm_sim_write_snapshot": [_P, ctypes.c_char_p, ctypes.c_char_p, _I],
     "wm_sim_read_snapshot": [_P, ctypes.c_char_p, ctypes.c_char_p, _P],
     "wm_sim_write_moments": [_P, ctypes.c_char_p, _I],
+    "wm_sim_init_weibel": [_P, _I, _D, _D, _D, ctypes.c_uint64],
+    "wm_sim_init_harris": [_P, _I, _I, _D, _D, _D, _D, _D, _D, ctypes.c_uint64],
+    "wm_sim_init_shock": [_P, _I, _D, _D, _D, _D, _D, _D, _D, _D, _D, ctypes.c_uint64],
     "wm_sim_write_particles": [_P, ctypes.c_char_p, _I, _I],
     "wm_paraio_init": [_I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _P, _P, ctypes.c_char_p],
     "wm_paraio_finalize": [],

@@ -128,3 +128,19 @@ int wm_launch_uf_interior(const WmGeom &g, FView<6, false> uf, double *out, cuda
 int wm_launch_row_count(int nrows, const double *stage, int pitch, const int *np2, int mode, long long *cnt, cudaStream_t st);
 int wm_launch_row_compact(int nrows, const double *stage, int pitch, const int *np2, int mode, const long long *off, double *out,
                           cudaStream_t st);
+
+// wm_init.cu: seeded initial conditions on the GPU (generator tags in wm_rng.cuh)
+#define WM_PI 3.14159265358979311599796346854418516
+struct WmInitArgs {
+    unsigned tag;           // WM_RNG_WEIBEL, _HARRIS or _SHOCK
+    int n_row;              // particles per row and species
+    unsigned long long seed;
+    double delx, c;
+    double vth_e, vth_i;
+    double ud;              // weibel: beam four-velocity
+    int ibg;                // harris: background particles per row
+    double lcs, x0, y0, tanh_edge, b0, e1, ncs, nbg, f1, f2;   // harris
+    double v0, l_damp_ini, nxgs_delx, xrs, xre, bx, by, bz;   // shock
+};
+int wm_launch_init_particles(const WmGeom &g, const WmInitArgs &a, double *stage, cudaStream_t st);
+int wm_launch_init_fields(const WmGeom &g, const WmInitArgs &a, FView<6, false> uf, cudaStream_t st);

@@ -73,7 +73,8 @@ extern "C" int wm_deposit_current_noalloc(const double *up, const double *gp, co
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return WM_ERR_UNSUPPORTED;
     WM_TRY(noalloc_setup(dev));
 
-    WmGeom g;
+    WmGeom g{};
+    g.bc = WM_BC_PERIODIC;  // field__fdtd_i's current fold of the periodic module
     g.ndim = ndim;
     g.np = np;
     g.nsp = nsp;

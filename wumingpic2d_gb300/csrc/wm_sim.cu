@@ -12,11 +12,13 @@
 //   and one gather B->A into the new cell-sorted order.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "wm_launch.cuh"
 #include "wm_pio.cuh"
+#include "wm_rng.cuh"
 
 namespace {
 
@@ -56,12 +58,45 @@ __global__ void k_pack(WmGeom g, SoAView src, const int *__restrict__ np2, int p
     }
 }
 
+// Pitched copy by the SMs, 16 bytes per access (width and pitches multiples of 16, bases
+// 16-byte aligned).  Between device memory and mapped page-locked host memory on a Grace host
+// the SMs' loads and stores reach the link's rate, about twice what a pitched copy-engine
+// transfer of the same rows gave (rows of a few MB, thousands of rows).
+__global__ void k_copy2d(uint4 *__restrict__ dst, size_t dpitch16, const uint4 *__restrict__ src, size_t spitch16, size_t width16,
+                         int rows)
+{
+    for (int r = blockIdx.y; r < rows; r += gridDim.y) {
+        const uint4 *s = src + (size_t)r * spitch16;
+        uint4 *d = dst + (size_t)r * dpitch16;
+        for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < width16; i += (size_t)gridDim.x * blockDim.x) d[i] = s[i];
+    }
+}
+
 struct Mark {
     const char *name;
     cudaEvent_t ev;
 };
 
 }  // namespace
+
+// dst/src pitched rows where one side is host memory: with the SMs when the host buffer is
+// mapped into the device's address space (wm_host_alloc, or registered page-locked memory) and
+// every size is a multiple of 16 bytes, else with cudaMemcpy2DAsync.
+static int copy_rows(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int rows, bool to_host, cudaStream_t st)
+{
+    void *host = to_host ? dst : (void *)src;
+    void *mapped = nullptr;
+    const bool aligned = ((dpitch | spitch | width | (uintptr_t)dst | (uintptr_t)src) & 15) == 0;
+    if (aligned && width > 0 && rows > 0 && cudaHostGetDevicePointer(&mapped, host, 0) == cudaSuccess && mapped == host) {
+        const size_t w16 = width / 16;
+        dim3 grid((unsigned)std::min<size_t>((w16 + 255) / 256, 16), (unsigned)std::min(rows, 65535));
+        k_copy2d<<<grid, 256, 0, st>>>((uint4 *)dst, dpitch / 16, (const uint4 *)src, spitch / 16, w16, rows);
+        return wm_check_launch("k_copy2d");
+    }
+    cudaGetLastError();  // a failed mapping query is not an error of this call
+    WM_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice, st));
+    return WM_OK;
+}
 
 struct wm_sim {
     WmGeom g{};
@@ -293,13 +328,16 @@ struct wm_sim {
 
     // Upload a reference-layout particle array (np slots per row, np2 used) into set S.
     // up: host rows of `host_pitch` slots (6 doubles each); the reference layout has np slots
+    // up == nullptr: the rows are already in `stage` with pitch = the largest row count
     int upload_particles(const double *up, const int *np2_h, DevBuf *S, int host_pitch)
     {
         const int maxc = std::max(1, *std::max_element(np2_h, np2_h + g.nrows));
         if (maxc > g.np || maxc > host_pitch) return WM_ERR_BAD_ARG;
-        WM_TRY(stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
-        WM_CUDA(cudaMemcpy2DAsync(stage.p, sizeof(double) * 6 * maxc, up, sizeof(double) * 6 * host_pitch, sizeof(double) * 6 * maxc,
-                                  g.nrows, cudaMemcpyHostToDevice, st));
+        if (up) {
+            WM_TRY(stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
+            WM_TRY(copy_rows(stage.p, sizeof(double) * 6 * maxc, up, sizeof(double) * 6 * host_pitch, sizeof(double) * 6 * maxc,
+                             g.nrows, false, st));
+        }
         pmark("copy_in_h2d");
         WM_CUDA(cudaMemcpyAsync(np2[cur].p, np2_h, sizeof(int) * g.nrows, cudaMemcpyHostToDevice, st));
         WM_TRY(wm_launch_rowbase(g.nrows, np2[cur].as<int>(), rowbase[cur].as<long long>(), st));
@@ -493,10 +531,9 @@ int wm_sim_destroy(wm_sim *s)
     return WM_OK;
 }
 
-static int sim_load_common(wm_sim *s, const double *up, const double *uf, const int *np2_h, const int *cumcnt_h,
-                           int host_pitch = -1)
+// Check the row counts of a state about to be loaded and size the device buffers for it.
+static int sim_prepare(wm_sim *s, const int *np2_h)
 {
-    if (host_pitch < 0) host_pitch = s->g.np;
     const WmGeom &g = s->g;
     long long ntot = 0;
     for (int r = 0; r < g.nrows; ++r) {
@@ -508,6 +545,28 @@ static int sim_load_common(wm_sim *s, const double *up, const double *uf, const 
     if (s->cap_req > cap) cap = s->cap_req;
     if (!s->loaded || cap > s->cap) WM_TRY(s->alloc(cap));
     s->ntot = ntot;
+    return WM_OK;
+}
+
+static int sim_finish_load(wm_sim *s)
+{
+    const WmGeom &g = s->g;
+    if (!s->loaded) {
+        const size_t nf = (size_t)g.nxw * g.nyw;
+        WM_CUDA(cudaMemsetAsync(s->f_df.p, 0, sizeof(double) * 6 * nf, s->st));
+        WM_CUDA(cudaMemsetAsync(s->f_uj.p, 0, sizeof(double) * 3 * nf, s->st));
+    }
+    s->loaded = true;
+    WM_CUDA(cudaStreamSynchronize(s->st));
+    return WM_OK;
+}
+
+static int sim_load_common(wm_sim *s, const double *up, const double *uf, const int *np2_h, const int *cumcnt_h,
+                           int host_pitch = -1)
+{
+    if (host_pitch < 0) host_pitch = s->g.np;
+    const WmGeom &g = s->g;
+    WM_TRY(sim_prepare(s, np2_h));
     if (cumcnt_h) {  // already sorted: upload straight into A
         WM_TRY(s->upload_particles(up, np2_h, s->A, host_pitch));
         s->pid_cur = 0;
@@ -518,14 +577,96 @@ static int sim_load_common(wm_sim *s, const double *up, const double *uf, const 
     }
     WM_TRY(s->upload_fields(uf));
     s->pmark("copy_in_fields");
-    if (!s->loaded) {
+    return sim_finish_load(s);
+}
+
+// A generated state: rows of n_row particles per species written into the stage by
+// k_init_particles, unpacked and cell-sorted on the device; fields by k_init_fields (or zero).
+static int sim_init_generated(wm_sim *s, WmInitArgs &a, bool fields)
+{
+    const WmGeom &g = s->g;
+    if (a.n_row < 1 || a.n_row > g.np) return WM_ERR_BAD_ARG;
+    std::vector<int> np2_h(g.nrows, a.n_row);
+    WM_TRY(sim_prepare(s, np2_h.data()));
+    a.delx = s->k.delx;
+    a.c = s->k.c;
+    WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)a.n_row * g.nrows));
+    WM_TRY(wm_launch_init_particles(g, a, s->stage.as<double>(), s->st));
+    WM_TRY(s->upload_particles(nullptr, np2_h.data(), s->B, a.n_row));
+    WM_TRY(s->sort_B_into_A());
+    if (fields) {
+        WM_TRY(wm_launch_init_fields(g, a, s->uf(), s->st));
+    } else {
+        WM_CUDA(cudaMemsetAsync(s->f_uf.p, 0, sizeof(double) * 6 * (size_t)g.nxw * g.nyw, s->st));
+    }
+    if (s->loaded) {  // a fresh state: the CG starts from zero as after a first load
         const size_t nf = (size_t)g.nxw * g.nyw;
         WM_CUDA(cudaMemsetAsync(s->f_df.p, 0, sizeof(double) * 6 * nf, s->st));
         WM_CUDA(cudaMemsetAsync(s->f_uj.p, 0, sizeof(double) * 3 * nf, s->st));
     }
-    s->loaded = true;
-    WM_CUDA(cudaStreamSynchronize(s->st));
-    return WM_OK;
+    return sim_finish_load(s);
+}
+
+int wm_sim_init_weibel(wm_sim *s, int ppc, double v_drift, double vth_e, double vth_i, uint64_t seed)
+{
+    if (!s || ppc < 1 || !(fabs(v_drift) < 1.0) || s->g.nsp != 2) return WM_ERR_BAD_ARG;
+    WmInitArgs a{};
+    a.tag = WM_RNG_WEIBEL;
+    a.n_row = (int)std::min<long long>((long long)ppc * s->g.nx, 1LL << 30);
+    a.seed = seed;
+    a.vth_e = vth_e;
+    a.vth_i = vth_i;
+    a.ud = v_drift / sqrt(1.0 - v_drift * v_drift);
+    return sim_init_generated(s, a, false);
+}
+
+int wm_sim_init_harris(wm_sim *s, int nbg, int ncs, double lcs, double b0, double e1, double vte, double vti, double rtemp,
+                       uint64_t seed)
+{
+    if (!s || nbg < 0 || ncs < 0 || !(lcs > 0) || s->g.nsp != 2 || s->g.bc != WM_BC_RECONNECTION) return WM_ERR_BAD_ARG;
+    const WmGeom &g = s->g;
+    const double delx = s->k.delx;
+    WmInitArgs a{};
+    a.tag = WM_RNG_HARRIS;
+    a.n_row = (int)(nbg * (g.nx - 1) + ncs * 2 * lcs);  // proj/reconnection/app.f90:309
+    a.seed = seed;
+    a.vth_e = vte;
+    a.vth_i = vti;
+    a.ibg = nbg * (g.nxge - g.nxgs - 2);
+    a.lcs = lcs;
+    a.x0 = 0.5 * (g.nxge + g.nxgs) * delx;
+    a.y0 = 0.5 * (g.nyge - g.nygs) * delx;
+    a.tanh_edge = tanh(0.5 * (g.nxge - g.nxgs - 2) * delx / lcs);
+    a.b0 = b0;
+    a.e1 = e1;
+    a.ncs = ncs;
+    a.nbg = nbg;
+    a.f1 = 1.0 / ((1.0 + rtemp) * s->k.q[0]);
+    a.f2 = rtemp / ((1.0 + rtemp) * s->k.q[1]);
+    return sim_init_generated(s, a, true);
+}
+
+int wm_sim_init_shock(wm_sim *s, int n0, double u0, double vth_e, double vth_i, double b0, double theta_bn, double phi_bn,
+                      double l_damp_ini, double xrs, double xre, uint64_t seed)
+{
+    if (!s || n0 < 1 || s->g.nsp != 2 || s->g.bc != WM_BC_SHOCK) return WM_ERR_BAD_ARG;
+    const WmGeom &g = s->g;
+    const double c = s->k.c;
+    WmInitArgs a{};
+    a.tag = WM_RNG_SHOCK;
+    a.n_row = n0 * (g.nxge - g.nxgs - 1);  // np2 = n0*(nxe-nxs-1), proj/shock/app.f90:335, nxs = nxgs, nxe = nxge
+    a.seed = seed;
+    a.vth_e = vth_e;
+    a.vth_i = vth_i;
+    a.v0 = u0 / sqrt(1 + (u0 * u0) / (c * c));
+    a.l_damp_ini = l_damp_ini;
+    a.nxgs_delx = g.nxgs * s->k.delx;
+    a.xrs = xrs;
+    a.xre = xre;
+    a.bx = b0 * cos(theta_bn);
+    a.by = b0 * sin(theta_bn) * cos(phi_bn);
+    a.bz = b0 * sin(theta_bn) * sin(phi_bn);
+    return sim_init_generated(s, a, true);
 }
 
 int wm_sim_load(wm_sim *s, const double *up, const double *uf, const int *np2_h)
@@ -571,8 +712,8 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
     if (up) {
         WM_TRY(sim_pack_stage(s, maxc));
         s->pmark("copy_out_pack");
-        WM_CUDA(cudaMemcpy2DAsync(up, sizeof(double) * 6 * g.np, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * maxc,
-                                  g.nrows, cudaMemcpyDeviceToHost, s->st));
+        WM_TRY(copy_rows(up, sizeof(double) * 6 * g.np, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * maxc, g.nrows, true,
+                         s->st));
         s->pmark("copy_out_d2h");
     }
     if (uf) {
@@ -1052,7 +1193,7 @@ int wm_host_alloc(void **ptr, size_t bytes)
 {
     if (!ptr) return WM_ERR_BAD_ARG;
     *ptr = nullptr;
-    WM_CUDA(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocPortable));
+    WM_CUDA(cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocPortable | cudaHostAllocMapped));
     return WM_OK;
 }
 

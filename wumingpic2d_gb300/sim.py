@@ -104,6 +104,22 @@ class Simulation:
         check(lib().wm_sim_moments(self._h, mom.ctypes.data), "wm_sim_moments")
         return mom
 
+    # ------------------------------------------------ initial conditions generated on the GPU
+    def init_weibel(self, ppc: int, v_drift: float, vth_e: float, vth_i: float, seed: int) -> None:
+        """The two-beam Weibel state (ppc per cell and species), generated and sorted on the GPU."""
+        check(lib().wm_sim_init_weibel(self._h, int(ppc), float(v_drift), float(vth_e), float(vth_i), int(seed)),
+              "wm_sim_init_weibel")
+
+    def init_harris(self, cfg) -> None:
+        """The reconnection application's Harris sheet for a harris.HarrisConfig."""
+        vte, vti, wpe, wpi, q, b0, lcs = cfg.plasma()
+        check(lib().wm_sim_init_harris(self._h, cfg.nbg, cfg.ncs, lcs, b0, cfg.e1, vte, vti, cfg.rtemp, int(cfg.seed)),
+              "wm_sim_init_harris")
+
+    def init_shock(self, cfg) -> None:
+        """The shock application's upstream plasma for a shock.ShockConfig (full box)."""
+        check(lib().wm_sim_init_shock(self._h, *cfg.init_args()), "wm_sim_init_shock")
+
     # ------------------------------------------------------- files (common/paraio.f90 format)
     @staticmethod
     def _dir(d: str) -> bytes:
