@@ -175,15 +175,16 @@ def ncu_traffic():
 # ------------------------------------------------------------------ CPU baseline
 def cpu_sample(args, steps: int):
     """The CPU restatement (OpenMP, every host core) on a strip of the workload."""
+    from oracle import init as I
     from oracle import oracle as O
-    from wumingpic2d_gb300.weibel import WeibelConfig, weibel_particles
+    from wumingpic2d_gb300.weibel import WeibelConfig
 
     cfg = WeibelConfig(nx=args.nx, ny=args.cpu_rows, ppc=args.ppc, seed=args.seed + 7, slack=1.2)
     d = cfg.dims()
     threads = os.cpu_count() or 1
     O.set_threads(threads)
     par = O.make_par(d, cfg.delt, cfg.charge, cfg.mass)
-    up0, np2 = weibel_particles(cfg)
+    up0, _, np2 = I.weibel(d, cfg.ppc, cfg.v_drift, cfg.vth_e, cfg.vth_i, cfg.seed)  # the GPU generator's state
     up, cum = d.alloc_up(), d.alloc_cumcnt()
     assert O.sort_bucket(par, d, up, up0, cum, np2) == 0
     del up0
@@ -202,25 +203,22 @@ def cpu_sample(args, steps: int):
 
 # ---------------------------------------------------------------------- GB300 arm
 def make_state(args, dist: Dist):
-    from wumingpic2d_gb300.weibel import WeibelConfig, weibel_particles
+    """The workload's parameters; the particles are generated on the GPU (wm_sim_init_weibel)."""
+    from wumingpic2d_gb300.weibel import WeibelConfig
 
-    cfg = WeibelConfig(nx=args.nx, ny=args.ny, ppc=args.ppc, seed=args.seed + dist.rank, slack=1.1)
-    t0 = time.perf_counter()
-    up0, np2 = weibel_particles(cfg)
-    return cfg, up0, np2, time.perf_counter() - t0
+    return WeibelConfig(nx=args.nx, ny=args.ny, ppc=args.ppc, seed=args.seed + dist.rank, slack=1.1)
 
 
 def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
     from wumingpic2d_gb300.sim import Simulation, pinned_zeros, set_device
 
     set_device(dist.local)
-    cfg, up0, np2, t_init = state
+    cfg = state
     d = cfg.dims()
-    uf = d.alloc_uf()
     t0 = time.perf_counter()
     sim = Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision=precision)
-    sim.load(up0, uf, np2)
-    t_init += time.perf_counter() - t0
+    sim.init_weibel(cfg.ppc, cfg.v_drift, cfg.vth_e, cfg.vth_i, cfg.seed)
+    t_init = time.perf_counter() - t0
     ntot, dev_bytes = sim.info()
     sim.step(args.warmup)
     sim.set_timing(True)
@@ -368,7 +366,7 @@ def main():
             "metric": METRIC, "value": res["value"], "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": res["ms"] / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32 particles + f64 fields",
-            "data": "synthetic (seeded Philox Weibel beams)",
+            "data": "synthetic (seeded Philox4x32-10 Weibel beams generated on the GPU)",
             "config": {"workload": workload, "nx": d.nx, "ny": d.ny, "ppc": args.ppc, "particles": res["ntot"],
                        "precision": head, "parallelism": f"replicas x{dist.world}",
                        "l2": f"inputs larger than L2 ({res['ntot'] * 48 / 1e9:.1f} GB of particles vs 129 MB)",
