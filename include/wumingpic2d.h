@@ -172,7 +172,8 @@ typedef struct wm_sim_config {
     double cg_err;        /* relative CG tolerance (field.f90:339 uses 1e-6) */
     int cg_itemax;        /* CG iteration limit (field.f90:337 uses 100) */
     int precision;        /* WM_PREC_FP64 or WM_PREC_MIXED */
-    int64_t capacity;     /* particle slots held on the GPU; 0 = 1.05 x loaded count */
+    int64_t capacity;     /* particle slots held on the GPU; 0 = the loaded count (enough unless
+                             particles are injected: see wm_sim_set_injection) */
     int bc;               /* WM_BC_* (the step follows that application's main loop) */
     double u0;            /* WM_BC_SHOCK: upstream four-velocity at the injection boundary */
 } wm_sim_config;
@@ -226,6 +227,21 @@ int wm_sim_init_harris(wm_sim *s, int nbg, int ncs, double lcs, double b0, doubl
                        uint64_t seed);
 int wm_sim_init_shock(wm_sim *s, int n0, double u0, double vth_e, double vth_i, double b0, double theta_bn, double phi_bn,
                       double l_damp_ini, double xrs, double xre, uint64_t seed);
+/* Particle injection of the shock application (proj/shock/app.f90:695-850; bc = WM_BC_SHOCK,
+ * box at full size): every step, after the sort, nginj = int(pflux) particles per species (one
+ * more with probability frac(pflux)), pflux = n0 |v0| dt dx ny, v0 = u0/gamma0 from the
+ * configuration's u0, enter behind the rows -- nginj/ny per row, one more in nginj mod ny rows
+ * drawn at random -- at x = nxe dx + (k+1/2)/n_j |v0| dt moved by (v0 + u_x) dt, Maxwellian
+ * (vth_e, vth_i) boosted by vprofile (l_damp_ini), ids negative after the species' count; np2 and
+ * cumcnt(nxe) grow by the row's count (the row total with them), and the upstream field (b0,
+ * theta_bn, phi_bn) is set in columns nxe-1 and nxe.  The draws are keyed by `seed` and counted by
+ * the step number (wm_sim_set_step / wm_sim_get_step; generated states start at 0, a snapshot at
+ * its own step).  on = 0 switches the injection off.  A step whose injection would exceed the
+ * capacity injects nothing and returns WM_ERR_OVERFLOW. */
+int wm_sim_set_injection(wm_sim *s, int on, int n0, double vth_e, double vth_i, double b0, double theta_bn, double phi_bn,
+                         double l_damp_ini, uint64_t seed);
+int wm_sim_set_step(wm_sim *s, int64_t it);
+int wm_sim_get_step(wm_sim *s, int64_t *it);
 int wm_sim_write_moments(wm_sim *s, const char *dir, int it);
 int wm_sim_write_particles(wm_sim *s, const char *dir, int it, int tracers_only);
 /* CG iterations per component of the last step. */

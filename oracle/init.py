@@ -158,7 +158,9 @@ def shock(d, n0, u0, vth_e, vth_i, b0, theta_bn, phi_bn, l_damp_ini, xrs, xre, s
     gam0 = math.sqrt(1 + u0 * u0 / (c * c))
     v0 = u0 / gam0
     _, uy = uniform2(seed, idx, 0, t)
-    x = np.broadcast_to((nxs + (nxe - nxs) * (i + 0.5) / n_row) * delx, (n_row, d.ny))
+    # over the cells nxs+1..nxe-1 that np2 and the initial cumcnt fill (app.f90:335-349), not
+    # [nxs, nxe) as app.f90:437 writes it (that puts a few particles behind the wall at nxs+1)
+    x = np.broadcast_to(((nxs + 1) + (nxe - nxs - 1) * (i + 0.5) / n_row) * delx, (n_row, d.ny))
     y = (d.nys + jr + uy) * delx
     y = np.minimum(y, np.nextafter((d.nys + jr + 1.0) * delx, 0.0))
     n1, n2 = normal2(seed, idx, 1, t)
@@ -190,3 +192,72 @@ def shock(d, n0, u0, vth_e, vth_i, b0, theta_bn, phi_bn, l_damp_ini, xrs, xre, s
     uf[4] = +vp * bz / c
     uf[5] = -vp * by / c
     return up, uf, np2
+
+
+def inject_counts(seed, it, pflux, ny):
+    """Particles entering each row this step (proj/shock/app.f90:722-754, one rank): int(pflux),
+    one more with probability frac(pflux); nginj // ny per row and one more in nginj % ny rows
+    drawn at random (the rows whose Philox key ranks lowest)."""
+    t = TAG["inject"] + 1
+    u, _ = uniform2(seed, np.array([int(it) << 32]), 0, t)
+    nginj = int(pflux) + (1 if u[0] < pflux - int(pflux) else 0)
+    j = np.arange(ny, dtype=np.uint64)
+    keys = philox4x32_10(j, np.full(ny, it, np.uint64), np.ones(ny, np.uint64), np.full(ny, t, np.uint64),
+                         seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF)[0]
+    order = np.lexsort((np.arange(ny), keys))
+    rank = np.empty(ny, np.int64)
+    rank[order] = np.arange(ny)
+    return (nginj // ny + (rank < nginj % ny)).astype(np.int64)
+
+
+def inject(d, up, uf, np2, cumcnt, it, seed, n0, u0, vth_e, vth_i, b0, theta_bn, phi_bn, l_damp_ini, delt, c=1.0, delx=1.0):
+    """proj/shock/app.f90:695-850 on reference-layout arrays, in place: the new particles behind each
+    row, np2 and cumcnt(nxe) advanced (the row total column is left as the Fortran leaves it),
+    the upstream field at columns nxe-1 and nxe."""
+    nxe = d.nxge
+    gam0 = math.sqrt(1 + u0 * u0 / (c * c))
+    v0 = u0 / gam0
+    pflux = n0 * abs(v0) * delt * delx * (d.nyge - d.nygs + 1)
+    x0 = abs(v0) * delt
+    inj = inject_counts(seed, it, pflux, d.ny)
+    ninc = np.concatenate(([0], np.cumsum(inj)[:-1]))
+    nptot = [int(np2[:, isp].sum()) for isp in range(d.nsp)]
+    t = TAG["inject"]
+    for jr in range(d.ny):
+        n = int(inj[jr])
+        if n == 0:
+            continue
+        k = np.arange(n, dtype=np.int64)
+        q = ninc[jr] + k
+        uy_draw, _ = uniform2(seed, q, 4 * it + 0, t)
+        n1, n2 = normal2(seed, q, 4 * it + 1, t)
+        n3, n4 = normal2(seed, q, 4 * it + 2, t)
+        n5, n6 = normal2(seed, q, 4 * it + 3, t)
+        xb = nxe * delx + (k + 0.5) / n * x0
+        y = (d.nys + jr + uy_draw) * delx
+        for isp, sd, u in ((0, vth_i, (n1, n2, n3)), (1, vth_e, (n4, n5, n6))):
+            ux, uyy, uz = sd * u[0], sd * u[1], sd * u[2]
+            x = xb + (v0 + ux) * delt
+            v1 = vprofile(x, v0, l_damp_ini, d.nxgs, delx)
+            gam1 = 1 / np.sqrt(1 - (v1 / c) ** 2)
+            gamp = np.sqrt(1 + (ux ** 2 + uyy ** 2 + uz ** 2) / c ** 2)
+            s0 = int(np2[jr, isp])
+            up[0, s0:s0 + n, jr, isp] = x
+            up[1, s0:s0 + n, jr, isp] = y
+            up[2, s0:s0 + n, jr, isp] = gam1 * (ux + v1 * gamp)
+            up[3, s0:s0 + n, jr, isp] = uyy
+            up[4, s0:s0 + n, jr, isp] = uz
+            up[5, s0:s0 + n, jr, isp] = (-(k + 1 + ninc[jr] + nptot[isp])).view(np.float64)
+    for isp in range(d.nsp):
+        np2[:, isp] += inj.astype(np2.dtype)
+        cumcnt[nxe - d.nxgs, :, isp] += inj.astype(cumcnt.dtype)
+    by0 = b0 * math.sin(theta_bn) * math.cos(phi_bn)
+    bz0 = b0 * math.sin(theta_bn) * math.sin(phi_bn)
+    i1, i2 = nxe - 1 - (d.nxgs - 2), nxe - (d.nxgs - 2)
+    uf[1, i1, :] = by0
+    uf[2, i1, :] = bz0
+    uf[4, i1, :] = +v0 * bz0 / c
+    uf[5, i1, :] = -v0 * by0 / c
+    uf[1, i2, :] = by0
+    uf[2, i2, :] = bz0
+    return inj

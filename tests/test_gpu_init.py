@@ -79,7 +79,9 @@ def test_shock_on_device(gpu, precision):
     q = cfg.charge
     args = cfg.init_args()
     want = sorted_oracle(d, q, cfg.mass, I.shock(d, *args[:-1], seed=args[-1]))
-    with Simulation(d, cfg.delt, q, cfg.mass, bc="shock", u0=cfg.u0, precision=precision) as sim:
+    # room for the particles the application injects every step
+    with Simulation(d, cfg.delt, q, cfg.mass, bc="shock", u0=cfg.u0, precision=precision,
+                    capacity=2 * cfg.n_ppc * d.nx * d.ny) as sim:
         sim.init_shock(cfg)
         compare(d, sim, want, False, precision)
         sim.step(2)

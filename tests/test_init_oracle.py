@@ -82,7 +82,9 @@ def test_shock_state():
     n = int(np2[0, 0])
     assert n == cfg.n_ppc * (d.nxge - d.nxgs - 1)
     x = up[0, :n, 0, 0]
-    assert np.all(np.diff(x) > 0) and x[0] >= d.nxgs and x[-1] < d.nxge
+    assert np.all(np.diff(x) > 0) and x[0] >= d.nxgs + 1 and x[-1] < d.nxge
+    counts = np.bincount(x.astype(int) - d.nxgs, minlength=d.nx)
+    assert counts[0] == 0 and (counts[1:d.nx - 1] == cfg.n_ppc).all() and counts[d.nx - 1] == 0
     pid = up[5, :n, 0, 0].view(np.int64)
     inside = (x >= 20.0) & (x <= 30.0)
     assert (pid[inside] > 0).all() and (pid[~inside] < 0).all()

@@ -31,13 +31,14 @@ __device__ __forceinline__ void put(double *a, double x, double y, double ux, do
 
 __device__ __forceinline__ double below(double v, double hi) { return fmin(v, nextafter(hi, 0.0)); }
 
-__device__ __forceinline__ double vprofile(double x, const WmInitArgs &a)
+// proj/shock/app.f90:881-891
+__device__ __forceinline__ double vprofile(double x, double v0, double l_damp_ini, double nxgs_delx)
 {
-    // proj/shock/app.f90:881-891
-    const double x0 = a.l_damp_ini + a.nxgs_delx;
-    const double xs = a.l_damp_ini * 0.1;
-    return 0.5 * a.v0 * (1 + tanh((x - x0) / xs));
+    const double x0 = l_damp_ini + nxgs_delx;
+    const double xs = l_damp_ini * 0.1;
+    return 0.5 * v0 * (1 + tanh((x - x0) / xs));
 }
+__device__ __forceinline__ double vprofile(double x, const WmInitArgs &a) { return vprofile(x, a.v0, a.l_damp_ini, a.nxgs_delx); }
 
 __global__ void k_init_particles(WmGeom g, WmInitArgs a, double *__restrict__ stage)
 {
@@ -82,7 +83,10 @@ __global__ void k_init_particles(WmGeom g, WmInitArgs a, double *__restrict__ st
         put(s1, x, y, sde * n4, sde * n5, sde * n6 + a.f2 * drift, -(1 + idx));
     } else {  // shock
         const int nxs = g.nxgs, nxe = g.nxge;
-        const double x = (nxs + (nxe - nxs) * (i + 0.5) / a.n_row) * delx;
+        // evenly over the cells nxs+1..nxe-1 that np2 = n0 (nxe-nxs-1) and the initial cumcnt
+        // (app.f90:335-349) give n0 each; app.f90:437 spreads them over [nxs, nxe), which puts a
+        // few behind the wall at nxs+1, where the first reflection moves them by more than a cell
+        const double x = ((nxs + 1) + (nxe - nxs - 1) * (i + 0.5) / a.n_row) * delx;
         const double y = below((jrow + ub) * delx, (jrow + 1.0) * delx);
         const double v1 = vprofile(x, a);
         const double gam1 = 1 / sqrt(1 - (v1 / a.c) * (v1 / a.c));
@@ -138,4 +142,183 @@ int wm_launch_init_fields(const WmGeom &g, const WmInitArgs &a, FView<6, false> 
 {
     k_init_fields<<<wm_div_up((long long)g.nxw * g.nyw, 256), 256, 0, st>>>(g, a, uf);
     return wm_check_launch("k_init_fields");
+}
+
+// ============================================================ shock injection
+// proj/shock/app.f90:695-850 for one rank: nginj = int(pflux) (+1 with probability frac(pflux))
+// particles per species enter each step, nginj / ny per row and one more in nginj mod ny rows
+// drawn at random; row j's particles sit at x = nxe dx + (k + 1/2)/n_j x0, y = (j + U) dx, then
+// move by (v0 + u_x) dt and are boosted by vprofile; ids continue after the species' count.
+namespace {
+
+__global__ void k_inject_counts(WmGeom g, WmInjectArgs a, const int *__restrict__ np2, int *__restrict__ inj,
+                                long long *__restrict__ ninc, long long *__restrict__ nptot, unsigned *status)
+{
+    extern __shared__ unsigned keys[];  // [ny]
+    __shared__ unsigned long long tot[2];
+    __shared__ long long s_nginj;
+    const int ny = g.ny;
+    if (threadIdx.x < 2) tot[threadIdx.x] = 0;
+    __syncthreads();
+    unsigned long long t0 = 0, t1 = 0;
+    for (int r = threadIdx.x; r < ny; r += blockDim.x) {
+        t0 += np2[r];
+        t1 += np2[ny + r];
+        keys[r] = wm_philox4x32_10((uint32_t)r, (uint32_t)a.it, 1u, WM_RNG_INJECT_COUNT, (uint32_t)a.seed, (uint32_t)(a.seed >> 32)).v[0];
+    }
+    atomicAdd(&tot[0], t0);
+    atomicAdd(&tot[1], t1);
+    if (threadIdx.x == 0) {
+        double u, unused;
+        wm_rng_uniform2(a.seed, (long long)a.it << 32, 0u, WM_RNG_INJECT_COUNT, u, unused);
+        long long n = (long long)a.pflux;
+        if (u < a.pflux - (double)(long long)a.pflux) ++n;
+        s_nginj = n;
+    }
+    __syncthreads();
+    long long nginj = s_nginj;
+    if ((long long)(tot[0] + tot[1]) + 2 * nginj > a.cap) {  // no room: nothing enters, the step reports it
+        if (threadIdx.x == 0) atomicOr(status, (unsigned)WMDEV_OVERFLOW);
+        nginj = 0;
+    }
+    const long long base = nginj / ny, nlmod = nginj % ny;
+    for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+        const unsigned kj = keys[j];
+        int rank = 0;
+        for (int k = 0; k < ny; ++k) rank += (keys[k] < kj) || (keys[k] == kj && k < j);
+        inj[j] = (int)(base + (rank < nlmod ? 1 : 0));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long c = 0;
+        for (int j = 0; j < ny; ++j) {
+            ninc[j] = c;
+            c += inj[j];
+        }
+        nptot[0] = (long long)tot[0];
+        nptot[1] = (long long)tot[1];
+    }
+}
+
+__global__ void k_inject_reserve(WmGeom g, const int *__restrict__ np2, const int *__restrict__ inj, int *__restrict__ tmp)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r < g.nrows) tmp[r] = np2[r] + inj[r % g.ny];
+}
+
+__device__ __forceinline__ void put_particle(const SoAView &v, long long p, const WmGeom &, int, int, double x, double y, double ux, double uy,
+                                             double uz, long long pid)
+{
+    v.X(p) = x;
+    v.Y(p) = y;
+    v.UX(p) = ux;
+    v.UY(p) = uy;
+    v.UZ(p) = uz;
+    v.setpid(p, pid);
+}
+
+// mixed sets: offsets against the cell the particle is counted in (may reach past 1 for a
+// particle beyond nxe, as the FP64 shape offset does in the reference)
+__device__ __forceinline__ void put_particle(const MixedView &v, long long p, const WmGeom &g, int cell, int jr, double x, double y,
+                                             double ux, double uy, double uz, long long pid)
+{
+    v.X(p) = (float)(x - (double)(g.nxgs + cell));
+    float oy = (float)(y - (double)(g.nys + jr));
+    if (oy >= 1.f) oy = 0x1.fffffep-1f;
+    v.Y(p) = oy;
+    v.UX(p) = (float)ux;
+    v.UY(p) = (float)uy;
+    v.UZ(p) = (float)uz;
+    v.setpid(p, pid);
+}
+
+template <class PV>
+__global__ void k_inject_particles(WmGeom g, WmInjectArgs a, PV dst, const int *__restrict__ np2, const int *__restrict__ inj,
+                                   const long long *__restrict__ ninc, const long long *__restrict__ nptot)
+{
+    const int jr = blockIdx.y;
+    const int n = inj[jr];
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const long long q = ninc[jr] + k;  // this step's injection index
+        double uy_draw, unused, n1, n2, n3, n4, n5, n6;
+        wm_rng_uniform2(a.seed, q, (uint32_t)(4 * a.it + 0), WM_RNG_INJECT, uy_draw, unused);
+        wm_rng_normal2(a.seed, q, (uint32_t)(4 * a.it + 1), WM_RNG_INJECT, n1, n2);
+        wm_rng_normal2(a.seed, q, (uint32_t)(4 * a.it + 2), WM_RNG_INJECT, n3, n4);
+        wm_rng_normal2(a.seed, q, (uint32_t)(4 * a.it + 3), WM_RNG_INJECT, n5, n6);
+        const double delx = a.delx;
+        const double xb = a.xe + (k + 0.5) / n * a.x0;
+        const double y = (g.nys + jr + uy_draw) * delx;
+        const double c2 = a.c * a.c;
+        for (int isp = 0; isp < 2; ++isp) {
+            const double sd = isp == 0 ? a.vth_i : a.vth_e;
+            const double ux = sd * (isp == 0 ? n1 : n4), uy = sd * (isp == 0 ? n2 : n5), uz = sd * (isp == 0 ? n3 : n6);
+            const double x = xb + (a.v0 + ux) * a.delt;
+            const double v1 = vprofile(x, a.v0, a.l_damp_ini, a.nxgs_delx);
+            const double gam1 = 1 / sqrt(1 - (v1 / a.c) * (v1 / a.c));
+            const double gamp = sqrt(1 + (ux * ux + uy * uy + uz * uz) / c2);
+            const int row = isp * g.ny + jr;
+            const long long p = dst.idx(row, np2[row] + k);
+            put_particle(dst, p, g, a.cell, jr, x, y, gam1 * (ux + v1 * gamp), uy, uz, -(k + 1 + ninc[jr] + nptot[isp]));
+        }
+    }
+}
+
+__global__ void k_inject_finish(WmGeom g, WmInjectArgs a, int *__restrict__ np2, int *__restrict__ cumcnt, const int *__restrict__ inj)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.nrows) return;
+    const int n = inj[r % g.ny];
+    np2[r] += n;
+    int *cc = cumcnt + (long long)r * (g.nx + 1);
+    cc[a.cell + 1] += n;  // cumcnt(nxe): the new particles count in cell nxe-1 (app.f90:837)
+    for (int ci = a.cell + 2; ci <= g.nx; ++ci) cc[ci] += n;  // and the row total with it
+}
+
+__global__ void k_inject_fields(WmGeom g, WmInjectArgs a, FView<6, false> uf)
+{
+    const int iy = blockIdx.x * blockDim.x + threadIdx.x;
+    if (iy >= g.nyw) return;
+    const int i1 = a.cell + 2, i2 = a.cell + 3;  // ghosted columns of nxe-1 and nxe
+    uf(1, i1, iy) = a.by0;
+    uf(2, i1, iy) = a.bz0;
+    uf(4, i1, iy) = +a.v0 * a.bz0 / a.c;
+    uf(5, i1, iy) = -a.v0 * a.by0 / a.c;
+    uf(1, i2, iy) = a.by0;
+    uf(2, i2, iy) = a.bz0;
+}
+
+}  // namespace
+
+int wm_launch_inject_counts(const WmGeom &g, const WmInjectArgs &a, const int *np2, int *inj, long long *ninc, long long *nptot,
+                            unsigned *status, cudaStream_t st)
+{
+    if (g.ny > WM_INJECT_MAX_ROWS) return WM_ERR_UNSUPPORTED;
+    k_inject_counts<<<1, 1024, sizeof(unsigned) * g.ny, st>>>(g, a, np2, inj, ninc, nptot, status);
+    return wm_check_launch("k_inject_counts");
+}
+
+int wm_launch_inject_reserve(const WmGeom &g, const int *np2, const int *inj, int *tmp, cudaStream_t st)
+{
+    k_inject_reserve<<<wm_div_up(g.nrows, 256), 256, 0, st>>>(g, np2, inj, tmp);
+    return wm_check_launch("k_inject_reserve");
+}
+
+template <class PV>
+int wm_launch_inject_particles(const WmGeom &g, const WmInjectArgs &a, PV dst, int *np2, int *cumcnt, const int *inj,
+                               const long long *ninc, const long long *nptot, cudaStream_t st)
+{
+    k_inject_particles<PV><<<dim3(1, g.ny), 128, 0, st>>>(g, a, dst, np2, inj, ninc, nptot);
+    WM_TRY(wm_check_launch("k_inject_particles"));
+    k_inject_finish<<<wm_div_up(g.nrows, 256), 256, 0, st>>>(g, a, np2, cumcnt, inj);
+    return wm_check_launch("k_inject_finish");
+}
+template int wm_launch_inject_particles<SoAView>(const WmGeom &, const WmInjectArgs &, SoAView, int *, int *, const int *,
+                                                 const long long *, const long long *, cudaStream_t);
+template int wm_launch_inject_particles<MixedView>(const WmGeom &, const WmInjectArgs &, MixedView, int *, int *, const int *,
+                                                   const long long *, const long long *, cudaStream_t);
+
+int wm_launch_inject_fields(const WmGeom &g, const WmInjectArgs &a, FView<6, false> uf, cudaStream_t st)
+{
+    k_inject_fields<<<wm_div_up(g.nyw, 128), 128, 0, st>>>(g, a, uf);
+    return wm_check_launch("k_inject_fields");
 }

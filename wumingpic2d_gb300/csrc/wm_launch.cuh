@@ -144,3 +144,28 @@ struct WmInitArgs {
 };
 int wm_launch_init_particles(const WmGeom &g, const WmInitArgs &a, double *stage, cudaStream_t st);
 int wm_launch_init_fields(const WmGeom &g, const WmInitArgs &a, FView<6, false> uf, cudaStream_t st);
+
+// wm_init.cu: particle injection of the shock application (proj/shock/app.f90:695-850)
+struct WmInjectArgs {
+    unsigned long long seed;
+    int it;                    // step number (the draws' counter)
+    double pflux;              // n0 |v0| dt dx ny: particles per step and species
+    double x0;                 // |v0| dt
+    double xe;                 // nxe dx
+    double v0, delt, c, delx, vth_e, vth_i, l_damp_ini, nxgs_delx;
+    int cell;                  // interior cell the new particles are counted in (nxe-1)
+    long long cap;             // particle capacity of the sets
+    double by0, bz0;           // upstream field
+};
+constexpr int WM_INJECT_MAX_ROWS = 12288;
+// counts per row (inj[ny]), their exclusive prefix (ninc[ny]) and the species totals before the
+// injection (nptot[2]); reads the new row counts np2
+int wm_launch_inject_counts(const WmGeom &g, const WmInjectArgs &a, const int *np2, int *inj, long long *ninc, long long *nptot,
+                            unsigned *status, cudaStream_t st);
+// tmp[row] = np2[row] + inj[row % ny]: row counts with room for the new particles
+int wm_launch_inject_reserve(const WmGeom &g, const int *np2, const int *inj, int *tmp, cudaStream_t st);
+// write the new particles behind each row's sorted ones, then np2 += inj, cumcnt(nxe), total += inj
+template <class PV>
+int wm_launch_inject_particles(const WmGeom &g, const WmInjectArgs &a, PV dst, int *np2, int *cumcnt, const int *inj,
+                               const long long *ninc, const long long *nptot, cudaStream_t st);
+int wm_launch_inject_fields(const WmGeom &g, const WmInjectArgs &a, FView<6, false> uf, cudaStream_t st);

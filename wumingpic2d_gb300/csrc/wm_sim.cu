@@ -109,6 +109,11 @@ struct wm_sim {
     DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out, jtile, fcc, stage2;
     DevBuf cumcnt_alt, mx_cnt9, mx_off9;  // mixed path: new cumcnt, per-cell direction counts and offsets
     DevBuf mom_dev, out_dev, out_cnt;     // moments and the file-ordered data of the paraio outputs
+    // shock application: particles entering at the right boundary every step (off until set)
+    bool inject_on = false;
+    WmInjectArgs inj{};
+    long long it = 0;  // steps taken: the counter of the injection draws
+    DevBuf inj_rows, inj_ninc, inj_nptot, inj_tmp;
     // learned CG guess (off until wm_sim_set_guess)
     DevBuf cnn_params, cnn_wf[WM_CNN_LAYERS], cnn_x, cnn_a0, cnn_a1, cnn_pred, cnn_partial, cnn_scale, guess_cand, guess_stats;
     WmCnnNet net{};
@@ -296,7 +301,7 @@ struct wm_sim {
             B[c].release();
         }
         for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &stage2,
-                          &mom_dev, &out_dev, &out_cnt,
+                          &mom_dev, &out_dev, &out_cnt, &inj_rows, &inj_ninc, &inj_nptot, &inj_tmp,
                           &f_uf, &f_uj, &f_df, &f_pj, &f_b, &f_r, &f_p, &f_ap, &f_partial, &f_ticket, &f_scal, &rb_dir, &rb_ord,
                           &rb_P, &rb_key, &rb_holes, &rb_nup, &rb_ndown, &rb_cellcnt, &rb_pairs, &rb_status})
             b->release();
@@ -392,6 +397,29 @@ struct wm_sim {
 
     // The mixed-precision step: FP32 push + deposit with the wrap, keys and counts fused in one
     // kernel; FP64 current fold, field solve and the same particle_y / sort permutation.
+    // Injection, first half (after the new row counts exist): this step's counts per row and the
+    // new row bases with room behind each row for them.  Without injection: the plain row bases.
+    int rowbases(WmRebinScratch &sc)
+    {
+        if (!inject_on) return wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st);
+        inj.it = (int)it;
+        inj.cap = cap;
+        WM_TRY(wm_launch_inject_counts(g, inj, sc.np2_new, inj_rows.as<int>(), inj_ninc.as<long long>(), inj_nptot.as<long long>(),
+                                       sc.status, st));
+        WM_TRY(wm_launch_inject_reserve(g, sc.np2_new, inj_rows.as<int>(), inj_tmp.as<int>(), st));
+        return wm_launch_rowbase(g.nrows, inj_tmp.as<int>(), sc.rowbase_new, st);
+    }
+    // second half (after the move): the new particles behind the sorted ones, np2 and cumcnt
+    // advanced (proj/shock/app.f90:829-848), and the upstream field at the boundary columns
+    template <class PV>
+    int inject_write(PV dst, int *cumcnt_new, WmRebinScratch &sc)
+    {
+        if (!inject_on) return WM_OK;
+        WM_TRY(wm_launch_inject_particles(g, inj, dst, sc.np2_new, cumcnt_new, inj_rows.as<int>(), inj_ninc.as<long long>(),
+                                          inj_nptot.as<long long>(), st));
+        return wm_launch_inject_fields(g, inj, uf(), st);
+    }
+
     int step_mixed()
     {
         WmRebinScratch sc = scratch();
@@ -415,16 +443,22 @@ struct wm_sim {
         // the new cumcnt (into the second buffer) and row bases, then one move into the new order
         WM_TRY(wm_launch_mixed_incoming(g, mx_cnt9.as<int>(), mx_off9.as<int>(), sc, st));
         WM_TRY(wm_launch_scan_cells(g, sc, cumcnt_alt.as<int>(), sc.np2_new, st));
-        WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
-        nl += 3;
+        WM_TRY(rowbases(sc));
+        nl += inject_on ? 5 : 3;
         mark("scan");
         WM_TRY(wm_launch_mixed_move(g, mview(B, cur, pid_cur), mview(A, 1 - cur, 1 - pid_cur), cumcnt.as<int>(), cumcnt_alt.as<int>(),
                                     mx_off9.as<int>(), sc, st));
         ++nl;
         mark("sort_move");
+        WM_TRY(inject_write(mview(A, 1 - cur, 1 - pid_cur), cumcnt_alt.as<int>(), sc));
+        if (inject_on) {
+            nl += 3;
+            mark("inject");
+        }
         std::swap(cumcnt, cumcnt_alt);
         cur = 1 - cur;
         pid_cur = 1 - pid_cur;
+        ++it;
         launches += nl;
         return check_status();
     }
@@ -458,13 +492,19 @@ struct wm_sim {
         nl += 1;
         mark("classify");
         WM_TRY(wm_launch_scan_cells(g, sc, cumcnt.as<int>(), sc.np2_new, st));
-        WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
-        nl += 2;
+        WM_TRY(rowbases(sc));
+        nl += inject_on ? 4 : 2;
         mark("scan");
         WM_TRY(wm_launch_place_sort(g, vb, view(A, 1 - cur), np2[cur].as<int>(), max_row, cumcnt.as<int>(), sc, st));
         nl += 3;
         mark("sort_move");
+        WM_TRY(inject_write(view(A, 1 - cur), cumcnt.as<int>(), sc));
+        if (inject_on) {
+            nl += 3;
+            mark("inject");
+        }
         cur = 1 - cur;
+        ++it;
         launches += nl;
         return check_status();
     }
@@ -599,6 +639,7 @@ static int sim_init_generated(wm_sim *s, WmInitArgs &a, bool fields)
     } else {
         WM_CUDA(cudaMemsetAsync(s->f_uf.p, 0, sizeof(double) * 6 * (size_t)g.nxw * g.nyw, s->st));
     }
+    s->it = 0;
     if (s->loaded) {  // a fresh state: the CG starts from zero as after a first load
         const size_t nf = (size_t)g.nxw * g.nyw;
         WM_CUDA(cudaMemsetAsync(s->f_df.p, 0, sizeof(double) * 6 * nf, s->st));
@@ -667,6 +708,57 @@ int wm_sim_init_shock(wm_sim *s, int n0, double u0, double vth_e, double vth_i, 
     a.by = b0 * sin(theta_bn) * cos(phi_bn);
     a.bz = b0 * sin(theta_bn) * sin(phi_bn);
     return sim_init_generated(s, a, true);
+}
+
+int wm_sim_set_injection(wm_sim *s, int on, int n0, double vth_e, double vth_i, double b0, double theta_bn, double phi_bn,
+                         double l_damp_ini, uint64_t seed)
+{
+    if (!s) return WM_ERR_BAD_ARG;
+    if (!on) {
+        s->inject_on = false;
+        return WM_OK;
+    }
+    const WmGeom &g = s->g;
+    if (g.bc != WM_BC_SHOCK || g.nsp != 2 || n0 < 1) return WM_ERR_BAD_ARG;
+    if (g.ny > WM_INJECT_MAX_ROWS) return WM_ERR_UNSUPPORTED;
+    const double c = s->k.c, delt = s->k.delt, delx = s->k.delx, u0 = s->u0;
+    WmInjectArgs a{};
+    a.seed = seed;
+    a.v0 = u0 / sqrt(1 + (u0 * u0) / (c * c));  // proj/shock/app.f90:318-319
+    a.delt = delt;
+    a.c = c;
+    a.delx = delx;
+    a.pflux = n0 * fabs(a.v0) * delt * delx * (g.nyge - g.nygs + 1);  // app.f90:725
+    a.x0 = fabs(a.v0) * delt;
+    a.xe = g.nxge * delx;
+    a.vth_e = vth_e;
+    a.vth_i = vth_i;
+    a.l_damp_ini = l_damp_ini;
+    a.nxgs_delx = g.nxgs * delx;
+    a.cell = g.nx - 2;  // nxe-1 with nxe = nxge
+    a.by0 = b0 * sin(theta_bn) * cos(phi_bn);
+    a.bz0 = b0 * sin(theta_bn) * sin(phi_bn);
+    WM_TRY(s->inj_rows.ensure(sizeof(int) * g.ny));
+    WM_TRY(s->inj_ninc.ensure(sizeof(long long) * g.ny));
+    WM_TRY(s->inj_nptot.ensure(sizeof(long long) * 2));
+    WM_TRY(s->inj_tmp.ensure(sizeof(int) * g.nrows));
+    s->inj = a;
+    s->inject_on = true;
+    return WM_OK;
+}
+
+int wm_sim_set_step(wm_sim *s, int64_t it)
+{
+    if (!s || it < 0) return WM_ERR_BAD_ARG;
+    s->it = it;
+    return WM_OK;
+}
+
+int wm_sim_get_step(wm_sim *s, int64_t *it)
+{
+    if (!s || !it) return WM_ERR_BAD_ARG;
+    *it = s->it;
+    return WM_OK;
 }
 
 int wm_sim_load(wm_sim *s, const double *up, const double *uf, const int *np2_h)
@@ -952,6 +1044,7 @@ int wm_sim_read_snapshot(wm_sim *s, const char *dir, const char *filename, int *
     }
     if (st == WM_OK) st = sim_load_common(s, up_h, uf_h.data(), np2_h.data(), nullptr, maxc);
     cudaFreeHost(up_h);
+    if (st == WM_OK) s->it = *it;
     return st;
 }
 

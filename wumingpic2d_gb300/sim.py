@@ -116,9 +116,29 @@ class Simulation:
         check(lib().wm_sim_init_harris(self._h, cfg.nbg, cfg.ncs, lcs, b0, cfg.e1, vte, vti, cfg.rtemp, int(cfg.seed)),
               "wm_sim_init_harris")
 
-    def init_shock(self, cfg) -> None:
-        """The shock application's upstream plasma for a shock.ShockConfig (full box)."""
+    def init_shock(self, cfg, inject: bool = True) -> None:
+        """The shock application's upstream plasma for a shock.ShockConfig (full box), with the
+        application's particle injection at the right boundary switched on (inject=True)."""
         check(lib().wm_sim_init_shock(self._h, *cfg.init_args()), "wm_sim_init_shock")
+        self.set_injection(cfg if inject else None)
+
+    def set_injection(self, cfg) -> None:
+        """Inject the upstream plasma of a shock.ShockConfig every step (None: off)."""
+        if cfg is None:
+            check(lib().wm_sim_set_injection(self._h, 0, 0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0), "wm_sim_set_injection")
+            return
+        a = cfg.init_args()  # n0, u0, vth_e, vth_i, b0, theta, phi, l_damp, xrs, xre, seed
+        check(lib().wm_sim_set_injection(self._h, 1, a[0], a[2], a[3], a[4], a[5], a[6], a[7], a[10]), "wm_sim_set_injection")
+
+    @property
+    def step_number(self) -> int:
+        v = ctypes.c_int64()
+        check(lib().wm_sim_get_step(self._h, ctypes.byref(v)), "wm_sim_get_step")
+        return v.value
+
+    @step_number.setter
+    def step_number(self, it: int) -> None:
+        check(lib().wm_sim_set_step(self._h, int(it)), "wm_sim_set_step")
 
     # ------------------------------------------------------- files (common/paraio.f90 format)
     @staticmethod
