@@ -97,9 +97,11 @@ int wm_launch_mixed_incoming(const WmGeom &g, const int *cnt9, int *off9, const 
 int wm_launch_mixed_move(const WmGeom &g, MixedView src, MixedView dst, const int *cumcnt_old, const int *cumcnt_new, const int *off9,
                          const WmRebinScratch &sc, cudaStream_t st);
 int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> uj, cudaStream_t st);
+// rows row0 .. row0+nrows-1 of the stage (nrows < 0: to the last row)
 int wm_launch_mixed_unpack(const WmGeom &g, const double *stage, int pitch, const int *np2, MixedView dst, const WmRebinScratch &sc,
-                           cudaStream_t st);
-int wm_launch_mixed_pack(const WmGeom &g, MixedView src, const int *np2, const int *cumcnt, int pitch, double *stage, cudaStream_t st);
+                           cudaStream_t st, int row0 = 0, int nrows = -1);
+int wm_launch_mixed_pack(const WmGeom &g, MixedView src, const int *np2, const int *cumcnt, int pitch, double *stage, cudaStream_t st,
+                         int row0 = 0, int nrows = -1);
 
 // wm_cnn.cu: the learned-guess network inside the solve (layer shapes are padded channel counts)
 constexpr int WM_CNN_LAYERS = 6;

@@ -30,6 +30,8 @@ constexpr int MX_TW = MX_THREADS / MX_LPC;  // cells per tile (one row, one spec
 constexpr int MX_JW = MX_TW + 4;            // node columns a tile deposits on
 constexpr int MX_FS = 60;                   // floats per cell of staged stencil: 9 x 6 used; 60 keeps 128-bit reads conflict-free
 constexpr int MX_PW = MX_TW + 8;            // per-cell partial rows: 4 zero cells on each side
+constexpr int MX_CB = 6;                    // bits of the tile cell in a move code: rank << 10 | cell << 4 | direction
+static_assert(MX_TW <= (1 << MX_CB), "a tile's cells fit the move code");
 constexpr unsigned FULL = 0xffffffffu;
 
 struct MxConst {
@@ -53,11 +55,13 @@ __device__ __forceinline__ void mirror(int w2, int &cn, float &off)
     }
 }
 
+// The TSC weights at centred offset h: 0.5 (0.5 + h)^2 = h (h/2 + 1/2) + 1/8 and
+// 0.5 (0.5 - h)^2 = that - h, 3/4 - h^2: four instructions.
 __device__ __forceinline__ void shape3(float h, float &a0, float &a1, float &a2)
 {
-    a0 = 0.5f * (0.5f - h) * (0.5f - h);
-    a1 = 0.75f - h * h;
-    a2 = 0.5f * (0.5f + h) * (0.5f + h);
+    a2 = fmaf(h, fmaf(0.5f, h, 0.5f), 0.125f);
+    a0 = a2 - h;
+    a1 = fmaf(-h, h, 0.75f);
 }
 
 // Two FP32 values in one 64-bit register pair, and the packed FMA of sm_100+ on such pairs.
@@ -128,8 +132,11 @@ __global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__
 // a lane past the end of its cell runs on a zero particle with zero deposit weights and its stores
 // switched off.  Each lane's next particle is copied into shared memory (cp.async) while the
 // current one is pushed.
+#ifndef WM_MX_MINB
+#define WM_MX_MINB (512 / MX_THREADS)  // resident CTAs per SM the register budget is sized for
+#endif
 template <int BC>  // WM_BC_*: the walls' code is compiled only where it runs
-__global__ void __launch_bounds__(MX_THREADS, 512 / MX_THREADS)
+__global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const float *__restrict__ fcc, const int *__restrict__ cumcnt,
                          unsigned *__restrict__ code, int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status)
 {
@@ -388,8 +395,8 @@ __global__ void __launch_bounds__(MX_THREADS, 512 / MX_THREADS)
         const int rank = base + __popc(peers & lanemask_lt());
         if (lane == leader && valid) dcnt[c][d] = base + __popc(peers);
         __syncwarp();
-        bad |= valid & (rank >= (1 << 27));
-        store_particle(b, p, nx1, ny1, u1, u2, u3, code, ((unsigned)rank << 4) | (unsigned)d, valid);
+        bad |= valid & (rank >= (1 << (28 - MX_CB)));
+        store_particle(b, p, nx1, ny1, u1, u2, u3, code, ((unsigned)rank << (4 + MX_CB)) | ((unsigned)c << 4) | (unsigned)d, valid);
     }
     if (bad) atomicOr(status, (unsigned)WMDEV_CELL);
     // this tile's per-cell direction counts (the cells of a warp are its own)
@@ -470,36 +477,38 @@ __global__ void k_mixed_incoming(WmGeom g, const int *__restrict__ cnt9, int *__
 }
 
 // Move every pushed particle (src: the push output in the old order) to its slot in the new
-// cell-sorted order (dst), ids included.  One CTA per (tile, row, species) of source cells.
+// cell-sorted order (dst), ids included.  One CTA per (tile, row, species) of source cells.  The
+// slot of the first particle each tile cell sends in each direction is set up once per tile; a
+// particle's code (rank << 10 | tile cell << 4 | direction) then gives its slot directly.
 __global__ void __launch_bounds__(MX_THREADS) k_mixed_move(WmGeom g, MixedView src, MixedView dst, const int *__restrict__ cumcnt_old,
                                                            const int *__restrict__ cumcnt_new, const int *__restrict__ off9,
                                                            const unsigned *__restrict__ code)
 {
-    __shared__ int cc[MX_TW + 1];
+    __shared__ long long base9[MX_TW][9];
+    __shared__ int span[2];
     const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
     const int row = isp * g.ny + jr;
     const int c0 = tile * MX_TW;
     const int ncell = min(MX_TW, g.nx - c0);
     const int *ccrow = cumcnt_old + (long long)(g.nx + 1) * row;
-    for (int e = threadIdx.x; e <= ncell; e += MX_THREADS) cc[e] = ccrow[c0 + e];
-    __syncthreads();
-    const long long rb = src.rowbase[row];
-    for (int s = cc[0] + threadIdx.x; s < cc[ncell]; s += MX_THREADS) {
-        int lo = 0, hi = ncell - 1;  // source cell: the last c with cc[c] <= s
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (cc[mid] <= s) lo = mid;
-            else hi = mid - 1;
-        }
-        const long long p = rb + s;
-        const unsigned cv = code[p];
-        const int d = (int)(cv & 15u), rank = (int)(cv >> 4);
-        int dr = jr + d / 3 - 1, dc = c0 + lo + d % 3 - 1;
+    for (int e = threadIdx.x; e < ncell * 9; e += MX_THREADS) {
+        const int c = e / 9, d = e % 9;
+        int dr = jr + d / 3 - 1, dc = c0 + c + d % 3 - 1;
         dr += dr < 0 ? g.ny : (dr >= g.ny ? -g.ny : 0);
         dc += dc < 0 ? g.nx : (dc >= g.nx ? -g.nx : 0);
         const int drow = isp * g.ny + dr;
-        const long long q = dst.rowbase[drow] + cumcnt_new[(long long)(g.nx + 1) * drow + dc] +
-                            off9[((long long)drow * g.nx + dc) * 9 + (8 - d)] + rank;
+        base9[c][d] = dst.rowbase[drow] + cumcnt_new[(long long)(g.nx + 1) * drow + dc] + off9[((long long)drow * g.nx + dc) * 9 + (8 - d)];
+    }
+    if (threadIdx.x == 0) {
+        span[0] = ccrow[c0];
+        span[1] = ccrow[c0 + ncell];
+    }
+    __syncthreads();
+    const long long rb = src.rowbase[row];
+    for (int s = span[0] + threadIdx.x; s < span[1]; s += MX_THREADS) {
+        const long long p = rb + s;
+        const unsigned cv = code[p];
+        const long long q = base9[(cv >> 4) & ((1u << MX_CB) - 1)][cv & 15u] + (cv >> (4 + MX_CB));
         copy_particle(dst, q, src, p);
     }
 }
@@ -533,9 +542,9 @@ __global__ void k_mixed_jfold(WmGeom g, int ntiles, const float *__restrict__ jt
 // FP64 reference-layout staging (pitch slots per row) -> mixed set; key = row * nx + cell for the
 // load-time sort.  Offsets are taken against the particle's own cell int(x) and its row.
 __global__ void k_mixed_unpack(WmGeom g, const double *__restrict__ stage, int pitch, const int *__restrict__ np2, MixedView dst,
-                               int *__restrict__ key, int *__restrict__ cellcnt, unsigned *status)
+                               int *__restrict__ key, int *__restrict__ cellcnt, unsigned *status, int row0)
 {
-    const int row = blockIdx.y;
+    const int row = row0 + blockIdx.y;
     const int jr = row % g.ny;
     const int n = np2[row];
     unsigned bad = 0;
@@ -566,32 +575,59 @@ __global__ void k_mixed_unpack(WmGeom g, const double *__restrict__ stage, int p
 }
 
 // mixed set -> FP64 reference-layout staging; the cell of each particle comes from cumcnt.
-__global__ void k_mixed_pack(WmGeom g, MixedView src, const int *__restrict__ np2, const int *__restrict__ cumcnt, int pitch,
-                             double *__restrict__ stage)
+constexpr int PACK_TW = 64;       // cells per pack CTA
+constexpr int PACK_THREADS = 256;
+
+// One CTA per (64-cell tile, row) writes the tile's particles, in slot order, as reference-layout
+// records (x, y, ux, uy, uz, id as 6 doubles) -- the cell comes from cumcnt, searched in shared
+// memory -- through a shared-memory buffer, so the stage is written in 16-byte vectors; the CTA
+// past the last tile zeroes the row's slots from np2 to the pitch.
+__global__ void __launch_bounds__(PACK_THREADS) k_mixed_pack(WmGeom g, MixedView src, const int *__restrict__ np2,
+                                                             const int *__restrict__ cumcnt, int pitch, double *__restrict__ stage, int row0)
 {
-    const int row = blockIdx.y;
+    __shared__ int cc[PACK_TW + 1];
+    __shared__ __align__(16) double buf[PACK_THREADS * 6];
+    const int row = row0 + blockIdx.y;
     const int jr = row % g.ny;
-    const int n = np2[row];
-    const int *cc = cumcnt + (long long)(g.nx + 1) * row;
-    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < pitch; s += gridDim.x * blockDim.x) {
-        double *a = stage + 6 * ((long long)row * pitch + s);
-        if (s < n) {
-            int lo = 0, hi = g.nx - 1;
+    const long long rs = (long long)row * pitch;  // the row's first slot in the stage
+    const int ntile = (g.nx + PACK_TW - 1) / PACK_TW;
+    if ((int)blockIdx.x == ntile) {  // zero tail
+        const int n = np2[row];
+        uint4 *z = reinterpret_cast<uint4 *>(stage + 6 * (rs + n));
+        const long long nv = 3LL * (pitch - n);
+        for (long long e = threadIdx.x; e < nv; e += PACK_THREADS) z[e] = make_uint4(0u, 0u, 0u, 0u);
+        return;
+    }
+    const int c0 = blockIdx.x * PACK_TW, ncell = min(PACK_TW, g.nx - c0);
+    const int *ccrow = cumcnt + (long long)(g.nx + 1) * row;
+    for (int e = threadIdx.x; e <= ncell; e += PACK_THREADS) cc[e] = ccrow[c0 + e];
+    __syncthreads();
+    const int beg = cc[0], end = cc[ncell];
+    const long long rb = src.rowbase[row];
+    for (int s0 = beg; s0 < end; s0 += PACK_THREADS) {
+        const int s = s0 + threadIdx.x;
+        if (s < end) {
+            int lo = 0, hi = ncell - 1;  // the last cell whose start is <= s
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
                 if (cc[mid] <= s) lo = mid;
                 else hi = mid - 1;
             }
-            const long long p = src.idx(row, s);
-            a[0] = (double)(g.nxgs + lo) + (double)src.X(p);
+            const long long p = rb + s;
+            double *a = buf + 6 * threadIdx.x;
+            a[0] = (double)(g.nxgs + c0 + lo) + (double)src.X(p);
             a[1] = (double)(g.nys + jr) + (double)src.Y(p);
             a[2] = src.UX(p);
             a[3] = src.UY(p);
             a[4] = src.UZ(p);
             a[5] = __longlong_as_double(src.getpid(p));
-        } else {
-            for (int k = 0; k < 6; ++k) a[k] = 0.0;
         }
+        __syncthreads();
+        const int nv = 3 * min(PACK_THREADS, end - s0);  // 16-byte words of this chunk
+        const uint4 *b = reinterpret_cast<const uint4 *>(buf);
+        uint4 *d = reinterpret_cast<uint4 *>(stage + 6 * (rs + s0));
+        for (int e = threadIdx.x; e < nv; e += PACK_THREADS) d[e] = b[e];
+        __syncthreads();
     }
 }
 
@@ -668,17 +704,20 @@ int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> u
 }
 
 int wm_launch_mixed_unpack(const WmGeom &g, const double *stage, int pitch, const int *np2, MixedView dst, const WmRebinScratch &sc,
-                           cudaStream_t st)
+                           cudaStream_t st, int row0, int nrows)
 {
-    WM_CUDA(cudaMemsetAsync(sc.cellcnt, 0, sizeof(int) * (size_t)g.nrows * g.nx, st));
-    dim3 grid(std::min(wm_div_up(std::max(pitch, 1), 256), 64u), g.nrows);
-    k_mixed_unpack<<<grid, 256, 0, st>>>(g, stage, pitch, np2, dst, sc.key, sc.cellcnt, sc.status);
+    if (nrows < 0) nrows = g.nrows - row0;
+    if (row0 == 0) WM_CUDA(cudaMemsetAsync(sc.cellcnt, 0, sizeof(int) * (size_t)g.nrows * g.nx, st));
+    dim3 grid(std::min(wm_div_up(std::max(pitch, 1), 256), 64u), nrows);
+    k_mixed_unpack<<<grid, 256, 0, st>>>(g, stage, pitch, np2, dst, sc.key, sc.cellcnt, sc.status, row0);
     return wm_check_launch("k_mixed_unpack");
 }
 
-int wm_launch_mixed_pack(const WmGeom &g, MixedView src, const int *np2, const int *cumcnt, int pitch, double *stage, cudaStream_t st)
+int wm_launch_mixed_pack(const WmGeom &g, MixedView src, const int *np2, const int *cumcnt, int pitch, double *stage, cudaStream_t st,
+                         int row0, int nrows)
 {
-    dim3 grid(std::min(wm_div_up(std::max(pitch, 1), 256), 64u), g.nrows);
-    k_mixed_pack<<<grid, 256, 0, st>>>(g, src, np2, cumcnt, pitch, stage);
+    if (nrows < 0) nrows = g.nrows - row0;
+    dim3 grid((g.nx + PACK_TW - 1) / PACK_TW + 1, nrows);
+    k_mixed_pack<<<grid, PACK_THREADS, 0, st>>>(g, src, np2, cumcnt, pitch, stage, row0);
     return wm_check_launch("k_mixed_pack");
 }

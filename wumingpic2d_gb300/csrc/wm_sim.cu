@@ -22,9 +22,9 @@
 
 namespace {
 
-__global__ void k_unpack(WmGeom g, const double *__restrict__ stage, int pitch, const int *__restrict__ np2, SoAView dst)
+__global__ void k_unpack(WmGeom g, const double *__restrict__ stage, int pitch, const int *__restrict__ np2, SoAView dst, int row0)
 {
-    const int row = blockIdx.y;
+    const int row = row0 + blockIdx.y;
     const int n = np2[row];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         const double *a = stage + 6 * ((long long)row * pitch + s);
@@ -38,9 +38,9 @@ __global__ void k_unpack(WmGeom g, const double *__restrict__ stage, int pitch, 
     }
 }
 
-__global__ void k_pack(WmGeom g, SoAView src, const int *__restrict__ np2, int pitch, double *__restrict__ stage)
+__global__ void k_pack(WmGeom g, SoAView src, const int *__restrict__ np2, int pitch, double *__restrict__ stage, int row0)
 {
-    const int row = blockIdx.y;
+    const int row = row0 + blockIdx.y;
     const int n = np2[row];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < pitch; s += gridDim.x * blockDim.x) {
         double *a = stage + 6 * ((long long)row * pitch + s);
@@ -82,18 +82,32 @@ struct Mark {
 // dst/src pitched rows where one side is host memory: with the SMs when the host buffer is
 // mapped into the device's address space (wm_host_alloc, or registered page-locked memory) and
 // every size is a multiple of 16 bytes, else with cudaMemcpy2DAsync.
-static int copy_rows(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int rows, bool to_host, cudaStream_t st)
+static bool rows_mapped(const void *host, const void *dst, size_t dpitch, const void *src, size_t spitch, size_t width)
 {
-    void *host = to_host ? dst : (void *)src;
     void *mapped = nullptr;
     const bool aligned = ((dpitch | spitch | width | (uintptr_t)dst | (uintptr_t)src) & 15) == 0;
-    if (aligned && width > 0 && rows > 0 && cudaHostGetDevicePointer(&mapped, host, 0) == cudaSuccess && mapped == host) {
-        const size_t w16 = width / 16;
-        dim3 grid((unsigned)std::min<size_t>((w16 + 255) / 256, 16), (unsigned)std::min(rows, 65535));
-        k_copy2d<<<grid, 256, 0, st>>>((uint4 *)dst, dpitch / 16, (const uint4 *)src, spitch / 16, w16, rows);
-        return wm_check_launch("k_copy2d");
-    }
-    cudaGetLastError();  // a failed mapping query is not an error of this call
+    if (aligned && width > 0 && cudaHostGetDevicePointer(&mapped, (void *)host, 0) == cudaSuccess && mapped == host) return true;
+    cudaGetLastError();  // a failed mapping query is not an error of the caller
+    return false;
+}
+
+// k_copy2d over `rows` rows with up to gx x gy CTAs.  Measured on the 2048^2 x 64 ppc state:
+// host -> device chunks of 256 rows with 16 x 256 CTAs overlapped with the unpack took 125 ms
+// (one full-grid copy then the unpack: 134 ms); device -> host, one full-grid copy after the pack
+// took 149 ms, chunks overlapped with the pack 154-158 ms at every grid size tried.
+static int launch_copy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int rows, cudaStream_t st, int gx = 16,
+                         int gy = 65535)
+{
+    if (rows <= 0) return WM_OK;
+    const size_t w16 = width / 16;
+    dim3 grid((unsigned)std::min<size_t>((w16 + 255) / 256, gx), (unsigned)std::min(rows, gy));
+    k_copy2d<<<grid, 256, 0, st>>>((uint4 *)dst, dpitch / 16, (const uint4 *)src, spitch / 16, w16, rows);
+    return wm_check_launch("k_copy2d");
+}
+
+static int copy_rows(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, int rows, bool to_host, cudaStream_t st)
+{
+    if (rows > 0 && rows_mapped(to_host ? dst : src, dst, dpitch, src, spitch, width)) return launch_copy2d(dst, dpitch, src, spitch, width, rows, st);
     WM_CUDA(cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, rows, to_host ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice, st));
     return WM_OK;
 }
@@ -114,6 +128,18 @@ struct wm_sim {
     WmInjectArgs inj{};
     long long it = 0;  // steps taken: the counter of the injection draws
     DevBuf inj_rows, inj_ninc, inj_nptot, inj_tmp;
+    // host -> device particle rows in chunks on a second stream, overlapped with the unpack
+    // kernels on the main one (host buffers mapped into the device's address space)
+    static constexpr int XFER_CHUNKS = 16;
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t xev[XFER_CHUNKS + 1] = {};
+    int xfer_setup()
+    {
+        if (!st2) WM_CUDA(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+        for (cudaEvent_t &e : xev)
+            if (!e) WM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        return WM_OK;
+    }
     // learned CG guess (off until wm_sim_set_guess)
     DevBuf cnn_params, cnn_wf[WM_CNN_LAYERS], cnn_x, cnn_a0, cnn_a1, cnn_pred, cnn_partial, cnn_scale, guess_cand, guess_stats;
     WmCnnNet net{};
@@ -319,6 +345,15 @@ struct wm_sim {
         status_host = nullptr;
         if (st) cudaStreamDestroy(st);
         st = nullptr;
+        if (st2) {
+            cudaStreamSynchronize(st2);
+            cudaStreamDestroy(st2);
+        }
+        st2 = nullptr;
+        for (cudaEvent_t &e : xev) {
+            if (e) cudaEventDestroy(e);
+            e = nullptr;
+        }
     }
 
     int check_status()
@@ -338,25 +373,42 @@ struct wm_sim {
     {
         const int maxc = std::max(1, *std::max_element(np2_h, np2_h + g.nrows));
         if (maxc > g.np || maxc > host_pitch) return WM_ERR_BAD_ARG;
+        const size_t rowb = sizeof(double) * 6 * maxc, hrowb = sizeof(double) * 6 * host_pitch;
+        bool piped = false;
         if (up) {
-            WM_TRY(stage.ensure(sizeof(double) * 6 * (size_t)maxc * g.nrows));
-            WM_TRY(copy_rows(stage.p, sizeof(double) * 6 * maxc, up, sizeof(double) * 6 * host_pitch, sizeof(double) * 6 * maxc,
-                             g.nrows, false, st));
+            WM_TRY(stage.ensure(rowb * g.nrows));
+            piped = rows_mapped(up, stage.p, rowb, up, hrowb, rowb);
+            if (!piped) WM_TRY(copy_rows(stage.p, rowb, up, hrowb, rowb, g.nrows, false, st));
         }
-        pmark("copy_in_h2d");
         WM_CUDA(cudaMemcpyAsync(np2[cur].p, np2_h, sizeof(int) * g.nrows, cudaMemcpyHostToDevice, st));
         WM_TRY(wm_launch_rowbase(g.nrows, np2[cur].as<int>(), rowbase[cur].as<long long>(), st));
-        if (mixed()) {  // offsets against int(x) and the row; also the load-sort keys and counts
-            WmRebinScratch sc = scratch();
-            WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
-            WM_TRY(wm_launch_mixed_unpack(g, stage.as<double>(), maxc, np2[cur].as<int>(), mview(S, cur), sc, st));
+        WmRebinScratch sc = scratch();
+        if (mixed()) WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
+        // mixed: offsets against int(x) and the row, also the load-sort keys and counts
+        auto unpack = [&](int r0, int nr) -> int {
+            if (mixed()) return wm_launch_mixed_unpack(g, stage.as<double>(), maxc, np2[cur].as<int>(), mview(S, cur), sc, st, r0, nr);
+            dim3 grid(std::min(wm_div_up(maxc, 256), 64u), nr);
+            k_unpack<<<grid, 256, 0, st>>>(g, stage.as<double>(), maxc, np2[cur].as<int>(), view(S, cur), r0);
+            return wm_check_launch("k_unpack");
+        };
+        if (piped) {  // chunk c's copy on st2, its unpack on st once the copy is in
+            WM_TRY(xfer_setup());
+            WM_CUDA(cudaEventRecord(xev[XFER_CHUNKS], st));
+            WM_CUDA(cudaStreamWaitEvent(st2, xev[XFER_CHUNKS], 0));
+            const int per = (g.nrows + XFER_CHUNKS - 1) / XFER_CHUNKS;
+            for (int c = 0, r0 = 0; r0 < g.nrows; ++c, r0 += per) {
+                const int nr = std::min(per, g.nrows - r0);
+                WM_TRY(launch_copy2d((char *)stage.p + r0 * rowb, rowb, (const char *)up + r0 * hrowb, hrowb, rowb, nr, st2, 16, 256));
+                WM_CUDA(cudaEventRecord(xev[c], st2));
+                WM_CUDA(cudaStreamWaitEvent(st, xev[c], 0));
+                WM_TRY(unpack(r0, nr));
+            }
         } else {
-            dim3 grid(std::min(wm_div_up(maxc, 256), 64u), g.nrows);
-            k_unpack<<<grid, 256, 0, st>>>(g, stage.as<double>(), maxc, np2[cur].as<int>(), view(S, cur));
-            WM_TRY(wm_check_launch("k_unpack"));
+            pmark("copy_in_h2d");
+            WM_TRY(unpack(0, g.nrows));
         }
         max_row = maxc;
-        pmark("copy_in_unpack");
+        pmark("copy_in_particles");
         return WM_OK;
     }
 
@@ -780,16 +832,21 @@ static int sim_row_counts(wm_sim *s, std::vector<int> &cnt, int &maxc)
 
 // The current particles as reference-layout rows in s->stage: 6 doubles per slot, `pitch` slots
 // per row, slots past a row's count zero.
-static int sim_pack_stage(wm_sim *s, int pitch)
+static int sim_pack_rows(wm_sim *s, int pitch, int r0, int nr)
 {
     const WmGeom &g = s->g;
-    WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)pitch * g.nrows));
     if (s->mixed())
         return wm_launch_mixed_pack(g, s->mview(s->A, s->cur, s->pid_cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), pitch,
-                                    s->stage.as<double>(), s->st);
-    dim3 grid(std::min(wm_div_up(pitch, 256), 64u), g.nrows);
-    k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), pitch, s->stage.as<double>());
+                                    s->stage.as<double>(), s->st, r0, nr);
+    dim3 grid(std::min(wm_div_up(pitch, 256), 64u), nr);
+    k_pack<<<grid, 256, 0, s->st>>>(g, s->view(s->A, s->cur), s->np2[s->cur].as<int>(), pitch, s->stage.as<double>(), r0);
     return wm_check_launch("k_pack");
+}
+
+static int sim_pack_stage(wm_sim *s, int pitch)
+{
+    WM_TRY(s->stage.ensure(sizeof(double) * 6 * (size_t)pitch * s->g.nrows));
+    return sim_pack_rows(s, pitch, 0, s->g.nrows);
 }
 
 int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
@@ -802,10 +859,11 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
     if (maxc > g.np) return WM_ERR_OVERFLOW;
     s->pmark("store_start");
     if (up) {
+        const size_t rowb = sizeof(double) * 6 * maxc, hrowb = sizeof(double) * 6 * g.np;
+        WM_TRY(s->stage.ensure(rowb * g.nrows));
         WM_TRY(sim_pack_stage(s, maxc));
         s->pmark("copy_out_pack");
-        WM_TRY(copy_rows(up, sizeof(double) * 6 * g.np, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * maxc, g.nrows, true,
-                         s->st));
+        WM_TRY(copy_rows(up, hrowb, s->stage.p, rowb, rowb, g.nrows, true, s->st));
         s->pmark("copy_out_d2h");
     }
     if (uf) {
