@@ -61,6 +61,9 @@ def parse():
     p.add_argument("--guess", default=os.path.join(ROOT, "wumingpic2d_gb300", "guess_weibel.npz"),
                    help="trained CG-guess network (wumingpic2d_gb300.train_guess); 'none' skips the learned-guess leg")
     p.add_argument("--cpu-steps", type=int, default=2)
+    p.add_argument("--reconnection-guess", default=os.path.join(ROOT, "wumingpic2d_gb300", "guess_harris.npz"),
+                   help="network trained on Harris-sheet pairs for the reconnection CG leg; 'none' skips the leg")
+    p.add_argument("--reconnection-steps", type=int, default=10)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
@@ -207,6 +210,37 @@ def make_state(args, dist: Dist):
     from wumingpic2d_gb300.weibel import WeibelConfig
 
     return WeibelConfig(nx=args.nx, ny=args.ny, ppc=args.ppc, seed=args.seed + dist.rank, slack=1.1)
+
+
+def reconnection_cg(args):
+    """The reconnection workload (Harris sheet, walls in x, 4096 x 2048 cells, 64 ppc in the sheet
+    centre, mixed path) with the CG tolerance at 1e-10: CG iterations per step (3 components) and
+    time per step from the previous step's dB and from the network trained on Harris pairs."""
+    from wumingpic2d_gb300.harris import HarrisConfig
+    from wumingpic2d_gb300.sim import Simulation
+
+    if args.reconnection_guess == "none" or not os.path.exists(args.reconnection_guess):
+        return None
+    params = np.load(args.reconnection_guess)["params"]
+    cfg = HarrisConfig(nx=4096, ny=2048, seed=args.seed + 11, slack=1.3)
+    d = cfg.dims()
+    out = {"workload": f"Harris sheet {cfg.nx}x{cfg.ny} (walls in x, periodic y), nbg {cfg.nbg} + ncs {cfg.ncs} ppc/species, "
+                       f"mi/me {cfg.mass_ratio:g}, Te/Ti {cfg.rtemp:g}, cg_tol 1e-10, mixed path",
+           "steps": args.reconnection_steps, "weights": os.path.relpath(args.reconnection_guess, ROOT)}
+    for mode in ("previous_step", "learned"):
+        with Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision="mixed", cg_err=1e-10, bc="reconnection") as sim:
+            sim.init_harris(cfg)
+            out["particles"] = sim.info()[0]
+            sim.step(3)
+            if mode == "learned":
+                sim.set_guess(params)
+                sim.step(1)
+            its, ms = [], 0.0
+            for _ in range(args.reconnection_steps):
+                ms += sim.step_timed(1)
+                its.append(int(sim.cg_iters().sum()))
+            out[mode] = {"cg_iters_per_step": round(float(np.mean(its)), 2), "ms_per_step": round(ms / args.reconnection_steps, 3)}
+    return out
 
 
 def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
@@ -383,6 +417,9 @@ def main():
         }
         if res.get("guess") is not None:
             line["learned_guess"] = res["guess"]
+        rc = reconnection_cg(args) if head == "mixed" else None
+        if rc is not None:
+            line["reconnection_cg"] = rc
         if other is not None:
             line["fp64_path"] = {"value": other["value"], "unit": UNIT, "ms_per_step": other["ms"] / args.steps,
                                  "speedup_of_mixed": res["value"] / other["value"],

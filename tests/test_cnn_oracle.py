@@ -110,13 +110,14 @@ def test_network_mask_is_block_diagonal_and_scales_are_per_group():
     assert np.allclose(x1, x2) and np.allclose(y1, y2)
 
 
-def test_shipped_guess_weights_are_block_diagonal():
+@pytest.mark.parametrize("name", ["guess_weibel.npz", "guess_harris.npz"])
+def test_shipped_guess_weights_are_block_diagonal(name):
     import json
     from pathlib import Path
 
     from wumingpic2d_gb300 import cnn
 
-    z = np.load(Path(cnn.__file__).with_name("guess_weibel.npz"))
+    z = np.load(Path(cnn.__file__).with_name(name))
     params = z["params"]
     assert params.shape == (cnn.NPARAMS,) and params.dtype == np.float32 and np.all(np.isfinite(params))
     assert not (params * (1 - cnn.param_mask())).any()

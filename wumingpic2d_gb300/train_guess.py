@@ -1,13 +1,15 @@
 """Train the learned CG initial guess on the GPU and save its parameters.
 
-    python -m wumingpic2d_gb300.train_guess [--out wumingpic2d_gb300/guess_weibel.npz]
+    python -m wumingpic2d_gb300.train_guess [--app weibel|harris] [--out ...npz]
 
-Pairs (E, B at time n; J at n+1/2) -> converged dB come from seeded FP64 Weibel runs on the
-resident simulation (a 128 x 128 box with the benchmark's plasma parameters, whose length scales
--- the skin depth in cells, c dt/dx -- do not depend on the box size): one run sampled every step
-over its first steps, one sampled every 10 steps over a long run that reaches the nonlinear
-phase.  Training runs the library's BF16 tensor-core kernels (cnn.Trainer).  A held-out seed then
-measures CG iterations per step from the previous step's dB and from the network's guess.
+Pairs (E, B at time n; J at n+1/2) -> converged dB come from seeded FP64 runs on the resident
+simulation.  weibel: a 128 x 128 box with the benchmark's plasma parameters (whose length scales
+-- the skin depth in cells, c dt/dx -- do not depend on the box size), one run sampled every step
+over its first steps and one sampled every 10 steps over a long run that reaches the nonlinear
+phase.  harris: the reconnection application's Harris sheet (walls in x) on a 256 x 128 box,
+generated on the GPU (wm_sim_init_harris), sampled the same way.  Training runs the library's
+BF16 tensor-core kernels (cnn.Trainer).  A held-out seed then measures CG iterations per step
+from the previous step's dB and from the network's guess.
 """
 from __future__ import annotations
 
@@ -22,10 +24,19 @@ from . import cnn
 from .sim import Simulation
 from .weibel import WeibelConfig, weibel_particles
 
-DEFAULT_OUT = Path(__file__).resolve().parent / "guess_weibel.npz"
+DEFAULT_OUT = {"weibel": Path(__file__).resolve().parent / "guess_weibel.npz",
+               "harris": Path(__file__).resolve().parent / "guess_harris.npz"}
+APP = {"name": "weibel"}
 
 
 def _sim(seed, nx, ny, ppc, cg_err=1e-6):
+    if APP["name"] == "harris":
+        from .harris import HarrisConfig
+        cfg = HarrisConfig(nx=nx, ny=ny, seed=seed, slack=2.0)
+        d = cfg.dims()
+        sim = Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision="fp64", cg_err=cg_err, bc="reconnection")
+        sim.init_harris(cfg)
+        return sim
     cfg = WeibelConfig(nx=nx, ny=ny, ppc=ppc, seed=seed, slack=2.5)
     d = cfg.dims()
     up, np2 = weibel_particles(cfg)
@@ -67,8 +78,9 @@ def cg_iterations(params, seed, nx, ny, ppc, cg_err, warm, steps):
 
 def main(argv=None):
     p = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    p.add_argument("--out", type=Path, default=DEFAULT_OUT)
-    p.add_argument("--nx", type=int, default=128)
+    p.add_argument("--app", choices=["weibel", "harris"], default="weibel")
+    p.add_argument("--out", type=Path, default=None)
+    p.add_argument("--nx", type=int, default=None)
     p.add_argument("--ny", type=int, default=128)
     p.add_argument("--ppc", type=int, default=16)
     p.add_argument("--early-steps", type=int, default=200)
@@ -79,6 +91,9 @@ def main(argv=None):
     p.add_argument("--lr", type=float, default=3e-3)
     p.add_argument("--seed", type=int, default=7)
     args = p.parse_args(argv)
+    APP["name"] = args.app
+    args.out = args.out or DEFAULT_OUT[args.app]
+    args.nx = args.nx or (256 if args.app == "harris" else 128)
 
     t0 = time.perf_counter()
     xs, ys = collect(args.nx, args.ny, args.ppc, [101], [102], args.early_steps, args.long_steps, args.long_every)
@@ -91,7 +106,7 @@ def main(argv=None):
     t_train = time.perf_counter() - t0
     params = net.host_params()
     evals = {str(e): cg_iterations(params, 103, args.nx, args.ny, args.ppc, e, 20, 40) for e in (1e-6, 1e-10)}
-    meta = {"samples": int(xs.shape[0]), "grid": [args.nx, args.ny], "ppc": args.ppc, "train_steps": args.train_steps,
+    meta = {"app": args.app, "samples": int(xs.shape[0]), "grid": [args.nx, args.ny], "ppc": args.ppc, "train_steps": args.train_steps,
             "batch": args.batch, "lr": args.lr, "loss_history": hist, "seconds_data": round(t_data, 1),
             "seconds_train": round(t_train, 1), "cg_iterations_held_out": evals}
     args.out.parent.mkdir(parents=True, exist_ok=True)
