@@ -17,6 +17,10 @@ e2e      the same metric through the host-buffer entry point (wm_sim_step_host):
 roofline the dominant particle kernel's algorithmic bytes per launch / its event time.
 cpu_baseline  the CPU restatement of the reference step (oracle/, OpenMP on every host core)
          on a bounded sample of the same workload.
+learned_guess, reconnection_cg, shock
+         the Weibel loop with the learned CG guess; the reconnection workload (Harris sheet
+         4096 x 2048, CG to 1e-10) with and without its learned guess; the shock workload
+         (16384 x 1024, 32 ppc, injection every step), all on the mixed path.
 --impl reference times that CPU restatement alone (the reference is Fortran + MPI and no
 Fortran compiler exists on this machine).
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU (the path does
@@ -64,6 +68,7 @@ def parse():
     p.add_argument("--reconnection-guess", default=os.path.join(ROOT, "wumingpic2d_gb300", "guess_harris.npz"),
                    help="network trained on Harris-sheet pairs for the reconnection CG leg; 'none' skips the leg")
     p.add_argument("--reconnection-steps", type=int, default=10)
+    p.add_argument("--shock-steps", type=int, default=5, help="steps of the shock leg (0 skips it)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
@@ -243,6 +248,37 @@ def reconnection_cg(args):
     return out
 
 
+def shock_leg(args):
+    """The shock workload (16384 x 1024 cells, 32 ppc per species upstream, u0 = -0.1c, mi/me 100,
+    sigma_e 0.01, reflecting wall and injection boundary, particles injected every step; the box
+    at full size), mixed path: particle-updates/s over the first steps of the run, and the
+    particles injected meanwhile."""
+    from wumingpic2d_gb300.shock import ShockConfig
+    from wumingpic2d_gb300.sim import Simulation
+
+    if args.shock_steps <= 0:
+        return None
+    cfg = ShockConfig(nx=16384, ny=1024, n_ppc=32, l_damp_ini=64.0, slack=1.0, seed=args.seed + 13)
+    d = cfg.dims()
+    n0 = 2 * cfg.n_ppc * (d.nx - 2) * d.ny
+    with Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision="mixed", bc="shock", u0=cfg.u0,
+                    capacity=int(n0 * 1.02)) as sim:
+        t0 = time.perf_counter()
+        sim.init_shock(cfg)
+        t_init = time.perf_counter() - t0
+        sim.step(2)
+        n_start = sim.info()[0]
+        ms = sim.step_timed(args.shock_steps)
+        n_end = sim.info()[0]
+        iters = sim.cg_iters().tolist()
+    return {"workload": f"shock {cfg.nx}x{cfg.ny}, {cfg.n_ppc} ppc/species upstream, u0 {cfg.u0:g}c, mi/me {cfg.mass_ratio:g}, "
+                        f"sigma_e {cfg.sigma_e:g}, wall + injection boundary, injection every step, mixed path",
+            "value": (n_start + n_end) / 2 * args.shock_steps / (ms / 1e3), "unit": UNIT,
+            "ms_per_step": round(ms / args.shock_steps, 3), "steps": args.shock_steps, "particles": n_end,
+            "injected_per_step": round((n_end - n_start) / args.shock_steps, 1), "setup_s": round(t_init, 2),
+            "cg_iters_last_step": iters}
+
+
 def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
     from wumingpic2d_gb300.sim import Simulation, pinned_zeros, set_device
 
@@ -420,6 +456,9 @@ def main():
         rc = reconnection_cg(args) if head == "mixed" else None
         if rc is not None:
             line["reconnection_cg"] = rc
+        sh = shock_leg(args) if head == "mixed" else None
+        if sh is not None:
+            line["shock"] = sh
         if other is not None:
             line["fp64_path"] = {"value": other["value"], "unit": UNIT, "ms_per_step": other["ms"] / args.steps,
                                  "speedup_of_mixed": res["value"] / other["value"],

@@ -310,6 +310,7 @@ JVal &Writer::entry(JVal *&group, const char *grp, const char *name, const char 
     for (long long s : shape) sh.arr.push_back(JVal::integer(s));
     e.add("shape", std::move(sh));
     e.add("description", JVal::str(desc));
+    end_ = disp_ + n * elem;
     return group->add(name, std::move(e));
 }
 
@@ -363,7 +364,7 @@ int Writer::dataset(const char *name, const char *dt, const std::vector<long lon
 int Writer::close()
 {
     if (!raw_) return WM_ERR_IO;
-    const bool ok = fclose(raw_) == 0;
+    const bool ok = fclose(raw_) == 0 && disp_ == end_;
     raw_ = nullptr;
     if (!ok) return WM_ERR_IO;
     FILE *f = fopen(json_path_.c_str(), "w");

@@ -89,6 +89,7 @@ class Writer {
     JVal *att_ = nullptr, *ds_ = nullptr;
     FILE *raw_ = nullptr;
     long long disp_ = 0;
+    long long end_ = 0;  // where the last entry's bytes end: close() checks they were all written
     std::string json_path_;
     JVal &entry(JVal *&group, const char *grp, const char *name, const char *dt, const std::vector<long long> &shape,
                 long long elem, const char *desc);

@@ -1219,6 +1219,14 @@ int wm_sim_launches(wm_sim *s, int64_t *count)
 int wm_sim_info(wm_sim *s, int64_t *nparticles, int64_t *device_bytes)
 {
     if (!s) return WM_ERR_BAD_ARG;
+    if (nparticles && s->loaded && s->inject_on) {  // the count grows every step: read the rows
+        std::vector<int> cnt;
+        int maxc;
+        WM_TRY(sim_row_counts(s, cnt, maxc));
+        long long n = 0;
+        for (int c : cnt) n += c;
+        s->ntot = n;
+    }
     if (nparticles) *nparticles = s->ntot;
     if (device_bytes) *device_bytes = (int64_t)s->device_bytes();
     return WM_OK;
