@@ -38,3 +38,23 @@ def test_div_e_of_a_uniform_field_is_zero():
     uf[3] = 0.7
     uf[4] = -0.2
     assert np.max(np.abs(div_e(d, uf))) == 0.0
+
+
+def test_strip_gauss_residual_matches_the_full_grid():
+    """The row-strip Gauss residual of the long-run check equals the full-grid one on its rows."""
+    from oracle import oracle as O
+    from wumingpic2d_gb300.diagnostics import gauss_residual
+    from wumingpic2d_gb300.validate import strip_gauss
+    from wumingpic2d_gb300.weibel import WeibelConfig, weibel_particles
+
+    cfg = WeibelConfig(nx=16, ny=12, ppc=4, seed=3, slack=2)
+    d = cfg.dims()
+    up0, np2 = weibel_particles(cfg)
+    par = O.make_par(d, cfg.delt, cfg.charge, cfg.mass)
+    up, cc = d.alloc_up(), d.alloc_cumcnt()
+    assert O.sort_bucket(par, d, up, up0, cc, np2) == 0
+    uf = d.alloc_uf()
+    uf[:] = np.random.default_rng(1).standard_normal(uf.shape)
+    full = gauss_residual(d, up, uf, np2, cfg.charge)
+    for j0, k in ((0, 4), (5, 3), (9, 3)):
+        assert np.allclose(strip_gauss(d, up, uf, np2, cfg.charge, j0, k), full[:, j0:j0 + k], rtol=0, atol=1e-12)
