@@ -362,6 +362,24 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
 # writes x, y, u; the deposit reads old x, y and new x, y, u; the sort moves 6 components).  Mixed:
 # the fused push+deposit reads and writes 5 FP32 components and writes the 4-byte move code; the
 # move reads the code and moves 5 FP32 components and the i64 pid.
+# FP64 operations per particle of the FP64 path's compute-bound kernels, counted from the
+# reference's code (particle.f90:96-161: ~215 plus 2 square roots and 3 divisions; field.f90:224-298:
+# ~570 plus a square root and a division); GB300's FP64 rate is 1.25 TFLOP/s nominal.
+FP64_FLOP = {"push": 215, "deposit": 570}
+FP64_PEAK_TFLOPS = 1.25
+
+
+def fp64_rooflines(res, args):
+    out = {}
+    for name, f in FP64_FLOP.items():
+        t = res["ktimes"].get(name)
+        if t:
+            tf = f * res["ntot"] / (t / args.steps / 1e3) / 1e12
+            out[name] = {"flop_per_particle": f, "achieved_tflops": round(tf, 3), "frac": round(tf / FP64_PEAK_TFLOPS, 3)}
+    out["peak"] = {"tflops": FP64_PEAK_TFLOPS, "source": "nominal FP64 rate (MEASURED_PEAKS.json has no FP64 figure)"}
+    return out
+
+
 ALGO_BYTES = {"fp64": {"push": 80, "deposit": 56, "sort_move": 96},
               "mixed": {"push_deposit": 44, "sort_move": 60}}
 
@@ -464,7 +482,8 @@ def main():
                                  "speedup_of_mixed": res["value"] / other["value"],
                                  "cg_iters_last_step": other["iters"],
                                  "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in other["ktimes"].items()},
-                                 "roofline": roofline(other, args), "gpu_launches": other["launches"],
+                                 "roofline": roofline(other, args), "roofline_fp64": fp64_rooflines(other, args),
+                                 "gpu_launches": other["launches"],
                                  "clocks": other["clocks"]}
         print(json.dumps(line), flush=True)
     dist.close()
