@@ -359,9 +359,13 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
 
 
 # Algorithmic bytes per particle of the particle kernels.  FP64: 8 B per component (push reads and
-# writes x, y, u; the deposit reads old x, y and new x, y, u; the sort moves 6 components).  Mixed:
-# the fused push+deposit reads and writes 5 FP32 components and writes the 4-byte move code; the
-# move reads the code and moves 5 FP32 components and the i64 pid.
+# writes x, y, u; the deposit reads old x, y and new x, y, u; the sort moves 6 components).  Mixed,
+# with the rebin as a permutation (the default): the fused push+deposit reads its particle's slot
+# in the permutation (4 B), reads and writes 5 FP32 components (20 + 20 B) and writes the 4-byte
+# move code; the permutation kernel reads the code and the id permutation and writes both
+# permutations (4 x 4 B; the ids themselves stay put).  With the move rebin the push reads and
+# writes the 5 components and the code (44 B) and the move reads the code and moves 5 FP32
+# components and the i64 id (60 B).
 # FP64 operations per particle of the FP64 path's compute-bound kernels, counted from the
 # reference's code (particle.f90:96-161: ~215 plus 2 square roots and 3 divisions; field.f90:224-298:
 # ~570 plus a square root and a division); GB300's FP64 rate is 1.25 TFLOP/s nominal.
@@ -381,7 +385,8 @@ def fp64_rooflines(res, args):
 
 
 ALGO_BYTES = {"fp64": {"push": 80, "deposit": 56, "sort_move": 96},
-              "mixed": {"push_deposit": 44, "sort_move": 60}}
+              "mixed": {"push_deposit": 48, "sort_perm": 16},
+              "mixed_move": {"push_deposit": 44, "sort_move": 60}}
 
 
 def all_rooflines(res, args):

@@ -257,6 +257,14 @@ int wm_sim_launches(wm_sim *s, int64_t *count);
 int wm_sim_info(wm_sim *s, int64_t *nparticles, int64_t *device_bytes);
 /* Block until every launched step has finished. */
 int wm_sim_sync(wm_sim *s);
+/* Rebin of the mixed-precision step (no reference counterpart: the reference sorts its FP64
+ * particles in place, sort.f90:36-82).  WM_REBIN_PERMUTE (the default) records the new cell order
+ * as a slot permutation that the next push reads through, so the particles move once per step,
+ * inside the push; the cell-sorted order is written out only when a call needs it (store, energy,
+ * moments, files).  WM_REBIN_MOVE moves them into cell order after every step.  Both give the
+ * same particles in the same order, bit for bit.  Steps with injection always move. */
+enum { WM_REBIN_PERMUTE = 0, WM_REBIN_MOVE = 1 };
+int wm_sim_set_rebin(wm_sim *s, int mode);
 /* wm_sim_step bracketed by CUDA events on the simulation's stream: *ms = GPU time of the
  * nsteps steps (host synchronisations inside the step loop included). */
 int wm_sim_step_timed(wm_sim *s, int nsteps, double *ms);

@@ -89,6 +89,7 @@ SIGNATURES = {
     "wm_sim_launches": [_P, ctypes.POINTER(ctypes.c_int64)],
     "wm_sim_info": [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
     "wm_sim_sync": [_P],
+    "wm_sim_set_rebin": [_P, _I],
     "wm_sim_get_work": [_P, _P, _P],
     "wm_sim_set_work": [_P, _P],
     "wm_sim_step_timed": [_P, _I, ctypes.POINTER(_D)],

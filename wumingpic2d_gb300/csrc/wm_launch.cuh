@@ -88,14 +88,25 @@ int wm_mixed_ntiles(const WmGeom &g);
 size_t wm_mixed_jtile_floats(const WmGeom &g);
 size_t wm_mixed_fcc_floats(const WmGeom &g);
 int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cudaStream_t st);
-// sc.key receives each particle's move code (rank << 4 | direction), cnt9 [cells][9] the per-cell
-// direction counts; k_mixed_incoming turns them into destination counts (sc.cellcnt) and offsets
-// off9 [cells][9]; k_mixed_move writes the new cell-sorted order.
-int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const float *fcc,
+// sc.key receives each particle's move code (rank << 10 | tile cell << 4 | direction), cnt9
+// [cells][9] the per-cell direction counts; k_mixed_incoming turns them into destination counts
+// (sc.cellcnt) and offsets off9 [cells][9]; k_mixed_move writes the new cell-sorted order, or
+// k_mixed_perm records it as a slot permutation that the next push reads through (perm != null:
+// the particle of slot p is at slot perm[p] of a; the push leaves the ids alone, and k_mixed_perm
+// composes the permutation of the id array, idperm, instead).
+int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const unsigned *perm, const float *fcc,
                                  const int *cumcnt, const WmRebinScratch &sc, int *cnt9, float *jtile, cudaStream_t st);
 int wm_launch_mixed_incoming(const WmGeom &g, const int *cnt9, int *off9, const WmRebinScratch &sc, cudaStream_t st);
 int wm_launch_mixed_move(const WmGeom &g, MixedView src, MixedView dst, const int *cumcnt_old, const int *cumcnt_new, const int *off9,
                          const WmRebinScratch &sc, cudaStream_t st);
+// perm[q] = p and idperm_new[q] = idperm_old[p] (idperm_old = null: p) for the push output slot p
+// that lands on slot q of the new order
+int wm_launch_mixed_perm(const WmGeom &g, const long long *rowbase_src, const long long *rowbase_dst, const int *cumcnt_old,
+                         const int *cumcnt_new, const int *off9, const WmRebinScratch &sc, unsigned *perm, const unsigned *idperm_old,
+                         unsigned *idperm_new, cudaStream_t st);
+// dst slot p <- src slot perm[p] over the np2 slots of every row, the id from src slot idperm[p]
+int wm_launch_mixed_gather(const WmGeom &g, MixedView src, MixedView dst, const unsigned *perm, const unsigned *idperm, const int *np2, int max_row,
+                           cudaStream_t st);
 int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> uj, cudaStream_t st);
 // rows row0 .. row0+nrows-1 of the stage (nrows < 0: to the last row)
 int wm_launch_mixed_unpack(const WmGeom &g, const double *stage, int pitch, const int *np2, MixedView dst, const WmRebinScratch &sc,

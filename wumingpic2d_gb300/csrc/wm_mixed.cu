@@ -33,6 +33,12 @@ constexpr int MX_PW = MX_TW + 8;            // per-cell partial rows: 4 zero cel
 constexpr int MX_CB = 6;                    // bits of the tile cell in a move code: rank << 10 | cell << 4 | direction
 static_assert(MX_TW <= (1 << MX_CB), "a tile's cells fit the move code");
 constexpr unsigned FULL = 0xffffffffu;
+#ifndef WM_MX_PFD
+#define WM_MX_PFD 2  // particles each lane has in flight (cp.async) ahead of the one it pushes (2: 2 % faster than 1)
+#endif
+constexpr int MX_PFD = WM_MX_PFD;
+constexpr int MX_NBUF = MX_PFD + 1;
+constexpr int MX_PR = MX_PFD + 2;  // perm entries each lane holds (GATHER): iterations it+MX_PFD .. it+2 MX_PFD+1
 
 struct MxConst {
     float fac1[WM_MAX_SP], txxx[WM_MAX_SP], fac2[WM_MAX_SP], mqdd[WM_MAX_SP], q[WM_MAX_SP];
@@ -96,7 +102,8 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src, unsigned
                  : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // The pushed particle's five components and its move code, stored only by lanes that hold a
 // particle (one predicate for the six stores: the loop body has no branches).
@@ -135,17 +142,21 @@ __global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__
 #ifndef WM_MX_MINB
 #define WM_MX_MINB (512 / MX_THREADS)  // resident CTAs per SM the register budget is sized for
 #endif
-template <int BC>  // WM_BC_*: the walls' code is compiled only where it runs
+// GATHER: the particle of cell-sorted slot p is at slot perm[p] of set a (the previous step's push
+// output, see k_mixed_perm); otherwise it is at slot p.  The push does not touch the ids.
+template <int BC, bool GATHER>  // BC = WM_BC_*: the walls' code is compiled only where it runs
 __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
-    k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const float *__restrict__ fcc, const int *__restrict__ cumcnt,
-                         unsigned *__restrict__ code, int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status)
+    k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const unsigned *__restrict__ perm, const float *__restrict__ fcc,
+                         const int *__restrict__ cumcnt, unsigned *__restrict__ code, int *__restrict__ cnt9, float *__restrict__ jtile,
+                         unsigned *status)
 {
     __shared__ int dcnt[MX_TW][9];  // per cell: particles so far that move in direction d
     __shared__ __align__(16) float fcell[MX_TW][MX_FS];  // [cell][(b*3 + a)*6 + m]
     __shared__ float cellpj[65][MX_PW];                   // per-cell partials; first holds the node rows
     __shared__ int cc[MX_TW + 1];
     __shared__ float spc[5];
-    __shared__ float pbuf[2][5][MX_THREADS];  // each lane's next particle, double-buffered
+    __shared__ float pbuf[MX_NBUF][5][MX_THREADS];  // each lane's next particles, MX_PFD ahead
+    __shared__ unsigned permring[GATHER ? MX_PR : 1][MX_THREADS];
     float(*tmp)[3][MX_TW + 2] = reinterpret_cast<float(*)[3][MX_TW + 2]>(&cellpj[0][0]);
     static_assert(6 * 3 * (MX_TW + 2) <= 65 * MX_PW, "node rows fit in the partials buffer");
     const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
@@ -229,27 +240,56 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
             az[jp][ip] = 0.f;
         }
     unsigned bad = 0;
-    // lane's particle of iteration it -> pbuf[it & 1]; a lane past its cell copies zeros
-    auto prefetch = [&](int it) {
+    // lane's particle of iteration it (at slot q of set a) -> pbuf[slot]; a lane past its cell copies zeros.
+    // GATHER: the perm entry of iteration j travels in the copy group of iteration j - MX_PFD - 1
+    // (into permring[j % MX_PR]), so it is in shared memory when iteration j's particle is fetched.
+    auto canon = [&](int it) { return rbase + s_beg + sub + (long long)it * MX_LPC; };
+    auto prefetch = [&](int it, int slot, long long q, int jperm) {
         const bool v = it < nmine;
-        const long long q = v ? rbase + s_beg + sub + (long long)it * MX_LPC : 0;
         const unsigned nb = v ? 4u : 0u;
-        float(*dst)[MX_THREADS] = pbuf[it & 1];
+        float(*dst)[MX_THREADS] = pbuf[slot];
         cp_async4(&dst[0][tid], a.x + q, nb);
         cp_async4(&dst[1][tid], a.y + q, nb);
         cp_async4(&dst[2][tid], a.ux + q, nb);
         cp_async4(&dst[3][tid], a.uy + q, nb);
         cp_async4(&dst[4][tid], a.uz + q, nb);
+        if (GATHER && jperm >= 0) {  // (the first MX_PFD groups carry no perm entry)
+            const bool vp = jperm < nmine;
+            cp_async4(reinterpret_cast<float *>(&permring[jperm % MX_PR][tid]), reinterpret_cast<const float *>(perm + (vp ? canon(jperm) : 0)),
+                      vp ? 4u : 0u);
+        }
         cp_async_commit();
     };
-    if (nwarp > 0) prefetch(0);
+    // the slot of set a that holds iteration it's particle
+    auto source = [&](int it) -> long long {
+        if constexpr (GATHER) return it < nmine ? (long long)permring[it % MX_PR][tid] : 0LL;
+        else return it < nmine ? canon(it) : 0LL;
+    };
+    // iterations 0 .. MX_PFD-1 are fetched before the loop, their perm entries read directly;
+    // those of iterations MX_PFD .. 2 MX_PFD go into the ring directly too
+    auto direct = [&](int j) -> long long {
+        if constexpr (GATHER) return j < nmine ? (long long)__ldg(perm + canon(j)) : 0LL;
+        else return j < nmine ? canon(j) : 0LL;
+    };
+    if constexpr (GATHER) {
+#pragma unroll
+        for (int j = MX_PFD; j <= 2 * MX_PFD; ++j) permring[j % MX_PR][tid] = (unsigned)direct(j);
+    }
+#pragma unroll
+    for (int i = 0; i < MX_PFD; ++i) {
+        if (i < nwarp) prefetch(i, i, direct(i), -1);
+        else cp_async_commit();  // empty groups keep the wait count uniform
+    }
+    int rslot = 0, wslot = MX_PFD;  // slot read this iteration, slot the next prefetch fills
     for (int it = 0; it < nwarp; ++it) {
         const bool valid = it < nmine;
-        const long long p = rbase + s_beg + sub + (long long)it * MX_LPC;
-        if (it + 1 < nwarp) prefetch(it + 1);
-        else cp_async_commit();  // an empty group keeps the wait count uniform
-        cp_async_wait1();
-        const float(*src)[MX_THREADS] = pbuf[it & 1];
+        const long long p = canon(it);
+        if (it + MX_PFD < nwarp) prefetch(it + MX_PFD, wslot, source(it + MX_PFD), it + 2 * MX_PFD + 1);
+        else cp_async_commit();
+        cp_async_wait<MX_PFD>();
+        const float(*src)[MX_THREADS] = pbuf[rslot];
+        rslot = rslot + 1 == MX_NBUF ? 0 : rslot + 1;
+        wslot = wslot + 1 == MX_NBUF ? 0 : wslot + 1;
         const float dx = src[0][tid], dy = src[1][tid];
         float u1 = src[2][tid], u2 = src[3][tid], u3 = src[4][tid];
         float sx0, sx1, sx2, sy0, sy1, sy2;
@@ -513,6 +553,67 @@ __global__ void __launch_bounds__(MX_THREADS) k_mixed_move(WmGeom g, MixedView s
     }
 }
 
+// The rebin as a permutation: instead of moving the pushed particles (k_mixed_move), record for
+// every slot q of the new cell-sorted order the slot p of the push output that holds its particle,
+// perm[q] = p (same slots as k_mixed_move computes).  The next push reads its particles through
+// perm, which moves them into cell order as a side effect of the step's own reads and writes.
+// The ids are not moved at all: idperm maps a cell-sorted slot to the slot of the id array that
+// holds its particle's id, idperm_new[q] = idperm_old[p] (idperm_old = null: the identity).
+__global__ void __launch_bounds__(MX_THREADS) k_mixed_perm(WmGeom g, const long long *__restrict__ rowbase_src,
+                                                           const long long *__restrict__ rowbase_dst, const int *__restrict__ cumcnt_old,
+                                                           const int *__restrict__ cumcnt_new, const int *__restrict__ off9,
+                                                           const unsigned *__restrict__ code, unsigned *__restrict__ perm,
+                                                           const unsigned *__restrict__ idperm_old, unsigned *__restrict__ idperm_new)
+{
+    __shared__ long long base9[MX_TW][9];
+    __shared__ int span[2];
+    const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
+    const int row = isp * g.ny + jr;
+    const int c0 = tile * MX_TW;
+    const int ncell = min(MX_TW, g.nx - c0);
+    const int *ccrow = cumcnt_old + (long long)(g.nx + 1) * row;
+    for (int e = threadIdx.x; e < ncell * 9; e += MX_THREADS) {
+        const int c = e / 9, d = e % 9;
+        int dr = jr + d / 3 - 1, dc = c0 + c + d % 3 - 1;
+        dr += dr < 0 ? g.ny : (dr >= g.ny ? -g.ny : 0);
+        dc += dc < 0 ? g.nx : (dc >= g.nx ? -g.nx : 0);
+        const int drow = isp * g.ny + dr;
+        base9[c][d] = rowbase_dst[drow] + cumcnt_new[(long long)(g.nx + 1) * drow + dc] + off9[((long long)drow * g.nx + dc) * 9 + (8 - d)];
+    }
+    if (threadIdx.x == 0) {
+        span[0] = ccrow[c0];
+        span[1] = ccrow[c0 + ncell];
+    }
+    __syncthreads();
+    const long long rb = rowbase_src[row];
+    for (int s = span[0] + threadIdx.x; s < span[1]; s += MX_THREADS) {
+        const long long p = rb + s;
+        const unsigned cv = code[p];
+        const long long q = base9[(cv >> 4) & ((1u << MX_CB) - 1)][cv & 15u] + (cv >> (4 + MX_CB));
+        perm[q] = (unsigned)p;
+        idperm_new[q] = idperm_old ? idperm_old[p] : (unsigned)p;
+    }
+}
+
+// dst slot p = src slot perm[p] for the np2[row] slots of every row, the id from slot idperm[p]
+// of src's id array: the cell-sorted state that the other kernels and the host copies read.
+__global__ void k_mixed_gather(WmGeom g, MixedView src, MixedView dst, const unsigned *__restrict__ perm, const unsigned *__restrict__ idperm,
+                               const int *__restrict__ np2)
+{
+    const int row = blockIdx.y;
+    const int n = np2[row];
+    const long long rb = dst.rowbase[row];
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+        const long long p = rb + s, q = perm[p];
+        dst.X(p) = src.X(q);
+        dst.Y(p) = src.Y(q);
+        dst.UX(p) = src.UX(q);
+        dst.UY(p) = src.UY(q);
+        dst.UZ(p) = src.UZ(q);
+        dst.setpid(p, src.getpid((long long)idperm[p]));
+    }
+}
+
 // uj(k, ix, iy) over the ghosted grid = sum of the tile currents that cover the node, in the
 // order (species, cell row, tile), accumulated in FP64.
 __global__ void k_mixed_jfold(WmGeom g, int ntiles, const float *__restrict__ jtile, FView<3, false> uj)
@@ -645,7 +746,7 @@ int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cuda
     return wm_check_launch("k_mixed_fields");
 }
 
-int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const float *fcc,
+int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const unsigned *perm, const float *fcc,
                                  const int *cumcnt, const WmRebinScratch &sc, int *cnt9, float *jtile, cudaStream_t st)
 {
     MxConst kc;
@@ -670,12 +771,18 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
     }
     dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
     unsigned *code = reinterpret_cast<unsigned *>(sc.key);
-    if (g.bc == WM_BC_RECONNECTION)
-        k_mixed_push_deposit<WM_BC_RECONNECTION><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, code, cnt9, jtile, sc.status);
-    else if (g.bc == WM_BC_SHOCK)
-        k_mixed_push_deposit<WM_BC_SHOCK><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, code, cnt9, jtile, sc.status);
-    else
-        k_mixed_push_deposit<WM_BC_PERIODIC><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, fcc, cumcnt, code, cnt9, jtile, sc.status);
+#define WM_MX_PUSH(BCV, GV) k_mixed_push_deposit<BCV, GV><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, perm, fcc, cumcnt, code, cnt9, jtile, sc.status)
+    if (g.bc == WM_BC_RECONNECTION) {
+        if (perm) WM_MX_PUSH(WM_BC_RECONNECTION, true);
+        else WM_MX_PUSH(WM_BC_RECONNECTION, false);
+    } else if (g.bc == WM_BC_SHOCK) {
+        if (perm) WM_MX_PUSH(WM_BC_SHOCK, true);
+        else WM_MX_PUSH(WM_BC_SHOCK, false);
+    } else {
+        if (perm) WM_MX_PUSH(WM_BC_PERIODIC, true);
+        else WM_MX_PUSH(WM_BC_PERIODIC, false);
+    }
+#undef WM_MX_PUSH
     return wm_check_launch("k_mixed_push_deposit");
 }
 
@@ -693,6 +800,24 @@ int wm_launch_mixed_move(const WmGeom &g, MixedView src, MixedView dst, const in
     dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
     k_mixed_move<<<grid, MX_THREADS, 0, st>>>(g, src, dst, cumcnt_old, cumcnt_new, off9, reinterpret_cast<const unsigned *>(sc.key));
     return wm_check_launch("k_mixed_move");
+}
+
+int wm_launch_mixed_perm(const WmGeom &g, const long long *rowbase_src, const long long *rowbase_dst, const int *cumcnt_old,
+                         const int *cumcnt_new, const int *off9, const WmRebinScratch &sc, unsigned *perm, const unsigned *idperm_old,
+                         unsigned *idperm_new, cudaStream_t st)
+{
+    dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
+    k_mixed_perm<<<grid, MX_THREADS, 0, st>>>(g, rowbase_src, rowbase_dst, cumcnt_old, cumcnt_new, off9, reinterpret_cast<const unsigned *>(sc.key),
+                                              perm, idperm_old, idperm_new);
+    return wm_check_launch("k_mixed_perm");
+}
+
+int wm_launch_mixed_gather(const WmGeom &g, MixedView src, MixedView dst, const unsigned *perm, const unsigned *idperm, const int *np2, int max_row,
+                           cudaStream_t st)
+{
+    dim3 grid(std::min(wm_div_up(std::max(max_row, 1), 256), 64u), g.nrows);
+    k_mixed_gather<<<grid, 256, 0, st>>>(g, src, dst, perm, idperm, np2);
+    return wm_check_launch("k_mixed_gather");
 }
 
 int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> uj, cudaStream_t st)

@@ -122,6 +122,14 @@ struct wm_sim {
     DevBuf A[6], B[6];
     DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out, jtile, fcc, stage2;
     DevBuf cumcnt_alt, mx_cnt9, mx_off9;  // mixed path: new cumcnt, per-cell direction counts and offsets
+    // Mixed path, rebin by permutation (the default): after a step, set A holds the push output
+    // and slot p of the cell-sorted order is at slot mx_perm[p] of A ("permuted"), its id at slot
+    // mx_idperm[idp][p] of A[5] (the ids do not move while permuted); the next push reads through
+    // mx_perm, and materialize() writes the cell-sorted order out when anything else needs it.
+    // rebin_move = true moves the particles every step instead (k_mixed_move).
+    DevBuf mx_perm, mx_idperm[2];
+    int idp = 0;
+    bool permuted = false, rebin_move = false;
     DevBuf mom_dev, out_dev, out_cnt;     // moments and the file-ordered data of the paraio outputs
     // shock application: particles entering at the right boundary every step (off until set)
     bool inject_on = false;
@@ -275,7 +283,12 @@ struct wm_sim {
             WM_TRY(cumcnt_alt.ensure(sizeof(int) * (size_t)(g.nx + 1) * g.nrows));
             WM_TRY(mx_cnt9.ensure(sizeof(int) * 9 * (size_t)g.nx * g.nrows));
             WM_TRY(mx_off9.ensure(sizeof(int) * 9 * (size_t)g.nx * g.nrows));
+            if (cap < (1LL << 32)) {
+                WM_TRY(mx_perm.ensure(sizeof(unsigned) * (size_t)cap));
+                for (DevBuf &b : mx_idperm) WM_TRY(b.ensure(sizeof(unsigned) * (size_t)cap));
+            }
         }
+        permuted = false;
         for (int c = 0; c < 2; ++c) {
             WM_TRY(rowbase[c].ensure(sizeof(long long) * (g.nrows + 1)));
             WM_TRY(np2[c].ensure(sizeof(int) * g.nrows));
@@ -312,7 +325,7 @@ struct wm_sim {
     {
         size_t t = 0;
         for (int c = 0; c < 6; ++c) t += A[c].bytes + B[c].bytes;
-        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &f_uf, &f_uj, &f_df, &f_pj,
+        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &mx_perm, &mx_idperm[0], &mx_idperm[1], &f_uf, &f_uj, &f_df, &f_pj,
                                 &f_b, &f_r, &f_p, &f_ap, &f_partial, &rb_dir, &rb_ord, &rb_P, &rb_key, &rb_holes, &rb_nup,
                                 &rb_ndown, &rb_cellcnt, &rb_pairs})
             t += b->bytes;
@@ -326,7 +339,7 @@ struct wm_sim {
             A[c].release();
             B[c].release();
         }
-        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &stage2,
+        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &mx_perm, &mx_idperm[0], &mx_idperm[1], &stage2,
                           &mom_dev, &out_dev, &out_cnt, &inj_rows, &inj_ninc, &inj_nptot, &inj_tmp,
                           &f_uf, &f_uj, &f_df, &f_pj, &f_b, &f_r, &f_p, &f_ap, &f_partial, &f_ticket, &f_scal, &rb_dir, &rb_ord,
                           &rb_P, &rb_key, &rb_holes, &rb_nup, &rb_ndown, &rb_cellcnt, &rb_pairs, &rb_status})
@@ -373,6 +386,7 @@ struct wm_sim {
     {
         const int maxc = std::max(1, *std::max_element(np2_h, np2_h + g.nrows));
         if (maxc > g.np || maxc > host_pitch) return WM_ERR_BAD_ARG;
+        permuted = false;  // the state is replaced
         const size_t rowb = sizeof(double) * 6 * maxc, hrowb = sizeof(double) * 6 * host_pitch;
         bool piped = false;
         if (up) {
@@ -472,8 +486,24 @@ struct wm_sim {
         return wm_launch_inject_fields(g, inj, uf(), st);
     }
 
+    // The cell-sorted state in set A again (ids in A[5]): gather the push output through mx_perm
+    // and the ids through mx_idperm into set B and exchange the two sets.
+    int materialize()
+    {
+        if (!permuted) return WM_OK;
+        WM_TRY(wm_launch_mixed_gather(g, mview(A, cur), mview(B, cur), mx_perm.as<unsigned>(), mx_idperm[idp].as<unsigned>(), np2[cur].as<int>(),
+                                      max_row, st));
+        ++launches;
+        for (int c = 0; c < 6; ++c) std::swap(A[c], B[c]);
+        permuted = false;
+        pid_cur = 0;
+        return WM_OK;
+    }
+
     int step_mixed()
     {
+        if (!rebin_move && !inject_on && cap < (1LL << 32)) return step_mixed_perm();
+        WM_TRY(materialize());
         WmRebinScratch sc = scratch();
         long long nl = 0;
         WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
@@ -482,7 +512,7 @@ struct wm_sim {
         WM_TRY(wm_launch_mixed_fields(g, uf(), fcc.as<float>(), st));
         ++nl;
         mark("fields");
-        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, fcc.as<float>(), cumcnt.as<int>(), sc, mx_cnt9.as<int>(), jtile.as<float>(), st));
+        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, nullptr, fcc.as<float>(), cumcnt.as<int>(), sc, mx_cnt9.as<int>(), jtile.as<float>(), st));
         ++nl;
         mark("push_deposit");
         WM_TRY(wm_launch_mixed_jfold(g, jtile.as<float>(), uj(), st));
@@ -510,6 +540,58 @@ struct wm_sim {
         std::swap(cumcnt, cumcnt_alt);
         cur = 1 - cur;
         pid_cur = 1 - pid_cur;
+        ++it;
+        launches += nl;
+        return check_status();
+    }
+
+    // The same step with the rebin as a permutation: the push reads its particles through mx_perm
+    // (when the state is permuted) and writes them to set B in the cell order of the step's start;
+    // k_mixed_perm records where each particle of the new order is (and where its id is: the ids
+    // stay in A[5]); the position sets then exchange roles.  The particles, their order and every
+    // result are those of the move.
+    int step_mixed_perm()
+    {
+        WmRebinScratch sc = scratch();
+        long long nl = 0;
+        WM_CUDA(cudaMemsetAsync(sc.status, 0, sizeof(unsigned), st));
+        mark("start");
+        if (pid_cur != 0) {  // the ids of the current order live with the positions in set A
+            std::swap(A[5], B[5]);
+            pid_cur = 0;
+        }
+        const bool gather = permuted;
+        MixedView va = mview(A, cur), vb = mview(B, cur);
+        WM_TRY(wm_launch_mixed_fields(g, uf(), fcc.as<float>(), st));
+        ++nl;
+        mark("fields");
+        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, gather ? mx_perm.as<unsigned>() : nullptr, fcc.as<float>(), cumcnt.as<int>(), sc,
+                                            mx_cnt9.as<int>(), jtile.as<float>(), st));
+        ++nl;
+        mark("push_deposit");
+        WM_TRY(wm_launch_mixed_jfold(g, jtile.as<float>(), uj(), st));
+        ++nl;
+        mark("deposit");
+        WmFieldWork w = work();
+        const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl, guess());
+        if (s != WM_OK) return s;
+        WM_TRY(wm_launch_mixed_incoming(g, mx_cnt9.as<int>(), mx_off9.as<int>(), sc, st));
+        WM_TRY(wm_launch_scan_cells(g, sc, cumcnt_alt.as<int>(), sc.np2_new, st));
+        WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
+        nl += 3;
+        mark("scan");
+        WM_TRY(wm_launch_mixed_perm(g, rowbase[cur].as<long long>(), sc.rowbase_new, cumcnt.as<int>(), cumcnt_alt.as<int>(), mx_off9.as<int>(),
+                                    sc, mx_perm.as<unsigned>(), gather ? mx_idperm[idp].as<unsigned>() : nullptr,
+                                    mx_idperm[1 - idp].as<unsigned>(), st));
+        ++nl;
+        mark("sort_perm");
+        // set B now holds the pushed particles in the old cell order: it becomes set A (the ids
+        // stay in A[5], reached through the new idperm)
+        for (int c = 0; c < 5; ++c) std::swap(A[c], B[c]);
+        idp = 1 - idp;
+        std::swap(cumcnt, cumcnt_alt);
+        cur = 1 - cur;
+        permuted = true;
         ++it;
         launches += nl;
         return check_status();
@@ -835,6 +917,7 @@ static int sim_row_counts(wm_sim *s, std::vector<int> &cnt, int &maxc)
 static int sim_pack_rows(wm_sim *s, int pitch, int r0, int nr)
 {
     const WmGeom &g = s->g;
+    WM_TRY(s->materialize());
     if (s->mixed())
         return wm_launch_mixed_pack(g, s->mview(s->A, s->cur, s->pid_cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), pitch,
                                     s->stage.as<double>(), s->st, r0, nr);
@@ -946,6 +1029,7 @@ int wm_sim_energy(wm_sim *s, double *out)
     const WmGeom &g = s->g;
     const int nb = 304;
     double *part = s->energy_partial.as<double>();
+    WM_TRY(s->materialize());
     if (s->mixed())
         WM_TRY(wm_launch_energy_particles(g, s->k, s->mview(s->A, s->cur), s->np2[s->cur].as<int>(), part, nb, s->st));
     else
@@ -969,6 +1053,7 @@ static int sim_moments_device(wm_sim *s)
     const WmGeom &g = s->g;
     const size_t nm = (size_t)7 * (g.nx + 2) * (g.ny + 2) * g.nsp;
     WM_TRY(s->mom_dev.ensure(sizeof(double) * nm));
+    WM_TRY(s->materialize());
     if (s->mixed()) {
         // moment steps are rare: expand the mixed state to FP64 rows (pitch = largest row) and run
         // the FP64 half-step push and moment deposit on that copy
@@ -1229,6 +1314,14 @@ int wm_sim_info(wm_sim *s, int64_t *nparticles, int64_t *device_bytes)
     }
     if (nparticles) *nparticles = s->ntot;
     if (device_bytes) *device_bytes = (int64_t)s->device_bytes();
+    return WM_OK;
+}
+
+int wm_sim_set_rebin(wm_sim *s, int mode)
+{
+    if (!s || (mode != WM_REBIN_PERMUTE && mode != WM_REBIN_MOVE)) return WM_ERR_BAD_ARG;
+    if (mode == WM_REBIN_MOVE) WM_TRY(s->materialize());
+    s->rebin_move = mode == WM_REBIN_MOVE;
     return WM_OK;
 }
 

@@ -93,6 +93,11 @@ class Simulation:
     def sync(self) -> None:
         check(lib().wm_sim_sync(self._h), "wm_sim_sync")
 
+    def set_rebin(self, mode: str) -> None:
+        """Mixed path: 'permute' (default; the next push reads through the new order) or 'move'
+        (the particles are moved into cell order after every step).  Same results bit for bit."""
+        check(lib().wm_sim_set_rebin(self._h, {"permute": 0, "move": 1}[mode]), "wm_sim_set_rebin")
+
     # ------------------------------------------------------------ diagnostics
     def energy(self) -> np.ndarray:
         out = np.zeros(self.dims.nsp + 2)
