@@ -262,7 +262,7 @@ int wm_sim_sync(wm_sim *s);
  * as a slot permutation that the next push reads through, so the particles move once per step,
  * inside the push; the cell-sorted order is written out only when a call needs it (store, energy,
  * moments, files).  WM_REBIN_MOVE moves them into cell order after every step.  Both give the
- * same particles in the same order, bit for bit.  Steps with injection always move. */
+ * same particles in the same order, bit for bit (injected particles included). */
 enum { WM_REBIN_PERMUTE = 0, WM_REBIN_MOVE = 1 };
 int wm_sim_set_rebin(wm_sim *s, int mode);
 /* wm_sim_step bracketed by CUDA events on the simulation's stream: *ms = GPU time of the

@@ -200,3 +200,27 @@ def test_mixed_rebin_permutation_equals_move(gpu, bc, shape):
         assert np.array_equal(x.view(np.uint64) if x.dtype == np.float64 else x, y.view(np.uint64) if y.dtype == np.float64 else y)
     assert np.array_equal(ea5, eb5) and np.array_equal(ea, eb)
     assert np.array_equal(ia5, ib5) and np.array_equal(ia, ib)
+
+
+def test_mixed_rebin_permutation_equals_move_with_injection(gpu):
+    """The same with the shock application's particle injection every step: the new particles take
+    fresh slots past the push output and the permutations point at them."""
+    from wumingpic2d_gb300.shock import ShockConfig
+
+    cfg = ShockConfig(nx=96, ny=16, n_ppc=8, l_damp_ini=8.0, slack=3.0, seed=23, tracer_window=(30.0, 50.0))
+    d = cfg.dims()
+    outs = {}
+    for mode in ("move", "permute"):
+        with Simulation(d, cfg.delt, cfg.charge, cfg.mass, bc="shock", u0=cfg.u0, precision="mixed",
+                        capacity=int(4 * cfg.n_ppc * d.nx * d.ny)) as sim:
+            sim.set_rebin(mode)
+            sim.init_shock(cfg)
+            sim.step(4)
+            e4 = sim.energy()
+            sim.step(5)
+            outs[mode] = (sim.store(up=d.alloc_up()), e4, sim.energy(), sim.info()[0])
+    (a, ea4, ea, na), (b, eb4, eb, nb) = outs["move"], outs["permute"]
+    assert na == nb and na > cfg.n_ppc * (d.nx - 2) * d.ny * 2
+    for x, y in zip(a, b):
+        assert np.array_equal(x.view(np.uint64) if x.dtype == np.float64 else x, y.view(np.uint64) if y.dtype == np.float64 else y)
+    assert np.array_equal(ea4, eb4) and np.array_equal(ea, eb)

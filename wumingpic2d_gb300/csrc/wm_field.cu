@@ -170,6 +170,32 @@ __global__ void k_soa_to_aos(long long npts, const double *__restrict__ s, doubl
     }
 }
 
+// Grid-stride walk over the elements e = r * n + c of an (rows x n) grid: the column and row
+// advance by the stride's quotient and remainder, so the loop divides only once per thread.
+struct GridCell {
+    long long e, stride;
+    int c, r, dc, dr, n;
+    __device__ explicit GridCell(int n_) : n(n_)
+    {
+        e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        stride = (long long)gridDim.x * blockDim.x;
+        c = (int)(e % n);
+        r = (int)(e / n);
+        dc = (int)(stride % n);
+        dr = (int)(stride / n);
+    }
+    __device__ __forceinline__ void next()
+    {
+        e += stride;
+        c += dc;
+        r += dr;
+        if (c >= n) {
+            c -= n;
+            ++r;
+        }
+    }
+};
+
 // ------------------------------------------------------------- reductions
 __device__ __forceinline__ void block_sum3(double &a, double &b, double &c)
 {
@@ -264,8 +290,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_rhs(WmGeom g, FieldK fk, FV6 
 {
     const long long ncell = (long long)g.nx * g.ny;
     double a0 = 0.0, a1 = 0.0, a2 = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+    for (GridCell q(g.nx); q.e < ncell; q.next()) {
+        const long long e = q.e;
+        const int ci = q.c, cj = q.r;
         const int x = ci + 2, y = cj + 2;
         const double g1 = +fk.f2 * (+uf(0, x, y - 1) + uf(0, x - 1, y) - 4. * uf(0, x, y) + uf(0, x + 1, y) + uf(0, x, y + 1)
                                     + fk.f3 * (-uj(2, x, y - 1) + uj(2, x, y)))
@@ -301,8 +328,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_resid(WmGeom g, FieldK fk, FV
 {
     const long long ncell = (long long)g.nx * g.ny;
     double acc[3] = {0.0, 0.0, 0.0};
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+    for (GridCell q(g.nx); q.e < ncell; q.next()) {
+        const long long e = q.e;
+        const int ci = q.c, cj = q.r;
         const int ym = wrapm(cj - 1, g.ny) + 2, yp = wrapm(cj + 1, g.ny) + 2, x = ci + 2, y = cj + 2;
 #pragma unroll
         for (int l = 0; l < 3; ++l) {
@@ -342,8 +370,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_guess_resid(WmGeom g, FieldK fk,
 {
     const long long ncell = (long long)g.nx * g.ny;
     double acc[3] = {0.0, 0.0, 0.0};
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+    for (GridCell q(g.nx); q.e < ncell; q.next()) {
+        const long long e = q.e;
+        const int ci = q.c, cj = q.r;
         const int ym = wrapm(cj - 1, g.ny) + 2, yp = wrapm(cj + 1, g.ny) + 2, xx = ci + 2, yy = cj + 2;
 #pragma unroll
         for (int l = 0; l < 3; ++l) {
@@ -370,8 +399,9 @@ __global__ void k_guess_pick(WmGeom g, FV6 df, const double *__restrict__ cand, 
         stats[6 + threadIdx.x] = take[threadIdx.x] ? 1.0 : 0.0;
         stats[9 + threadIdx.x] = scal[threadIdx.x].sum_g;
     }
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-        const int ix = (int)(e % g.nx) + 2, iy = (int)(e / g.nx) + 2;
+    for (GridCell q(g.nx); q.e < ncell; q.next()) {
+        const long long e = q.e;
+        const int ix = q.c + 2, iy = q.r + 2;
 #pragma unroll
         for (int l = 0; l < 3; ++l)
             if (take[l]) df(l, ix, iy) = cand[l * ncell + e];
@@ -386,8 +416,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_ap(WmGeom g, FieldK fk, const
     const bool act[3] = {scal[0].active != 0, scal[1].active != 0, scal[2].active != 0};
     if (!act[0] && !act[1] && !act[2]) return;  // uniform across the grid: no CTA takes a ticket
     double acc[3] = {0.0, 0.0, 0.0};
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+    for (GridCell q(g.nx); q.e < ncell; q.next()) {
+        const long long e = q.e;
+        const int ci = q.c, cj = q.r;
         const long long row = (long long)cj * g.nx;
         const long long es = (long long)wrapm(cj - 1, g.ny) * g.nx + ci, en = (long long)wrapm(cj + 1, g.ny) * g.nx + ci;
 #pragma unroll
@@ -424,8 +455,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_update(WmGeom g, FieldK fk, F
     if (!act[0] && !act[1] && !act[2]) return;
     const double av[3] = {scal[0].av, scal[1].av, scal[2].av};
     double acc[3] = {0.0, 0.0, 0.0};
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-        const int ci = (int)(e % g.nx), cj = (int)(e / g.nx);
+    for (GridCell q(g.nx); q.e < ncell; q.next()) {
+        const long long e = q.e;
+        const int ci = q.c, cj = q.r;
 #pragma unroll
         for (int l = 0; l < 3; ++l) {
             if (!act[l]) continue;
@@ -474,8 +506,8 @@ template <class FV6, class FV3>
 __global__ void k_efield(WmGeom g, FieldK fk, FV6 df, FV6 uf, FV3 uj)
 {
     const long long ncell = (long long)g.nx * g.ny;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(e % g.nx) + 2, y = (int)(e / g.nx) + 2;
+    for (GridCell q(g.nx); q.e < ncell; q.next()) {
+        const int x = q.c + 2, y = q.r + 2;
         df(3, x, y) = +fk.f1 * (+fk.gfac * (-df(2, x, y) + df(2, x, y + 1)) + (-uf(2, x, y) + uf(2, x, y + 1))) - fk.pi4dt * uj(0, x, y);
         df(4, x, y) = -fk.f1 * (+fk.gfac * (-df(2, x, y) + df(2, x + 1, y)) + (-uf(2, x, y) + uf(2, x + 1, y))) - fk.pi4dt * uj(1, x, y);
         df(5, x, y) = +fk.f1 * (+fk.gfac * (-df(1, x, y) + df(1, x + 1, y) + df(0, x, y) - df(0, x, y + 1))
@@ -489,8 +521,8 @@ template <class FV6>
 __global__ void k_field_add(WmGeom g, FV6 uf, FV6 df)
 {
     const long long n = (long long)g.nxw * g.nyw;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int ix = (int)(e % g.nxw), iy = (int)(e / g.nxw);
+    for (GridCell q(g.nxw); q.e < n; q.next()) {
+        const int ix = q.c, iy = q.r;
 #pragma unroll
         for (int k = 0; k < 6; ++k) uf(k, ix, iy) = uf(k, ix, iy) + df(k, ix, iy);
     }
@@ -502,8 +534,8 @@ __global__ void __launch_bounds__(CG_THREADS) k_energy_fields(WmGeom g, FV6 uf, 
 {
     const long long ncell = (long long)g.nx * g.ny;
     double be = 0.0, ee = 0.0, z = 0.0;
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(e % g.nx) + 2, y = (int)(e / g.nx) + 2;
+    for (GridCell q(g.nx); q.e < ncell; q.next()) {
+        const int x = q.c + 2, y = q.r + 2;
         be += uf(0, x, y) * uf(0, x, y) + uf(1, x, y) * uf(1, x, y) + uf(2, x, y) * uf(2, x, y);
         ee += uf(3, x, y) * uf(3, x, y) + uf(4, x, y) * uf(4, x, y) + uf(5, x, y) * uf(5, x, y);
     }

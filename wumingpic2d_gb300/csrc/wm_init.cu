@@ -232,12 +232,17 @@ __device__ __forceinline__ void put_particle(const MixedView &v, long long p, co
     v.setpid(p, pid);
 }
 
+// perm != null (the mixed path's permuted state): the new particle of row slot np2+k goes to the
+// fresh slot *phys0 + isp * (this step's count) + (its injection index) of dst's arrays -- past
+// the slots the push output and the ids occupy -- and perm / idperm of its cell-sorted slot point there.
 template <class PV>
 __global__ void k_inject_particles(WmGeom g, WmInjectArgs a, PV dst, const int *__restrict__ np2, const int *__restrict__ inj,
-                                   const long long *__restrict__ ninc, const long long *__restrict__ nptot)
+                                   const long long *__restrict__ ninc, const long long *__restrict__ nptot, unsigned *__restrict__ perm,
+                                   unsigned *__restrict__ idperm, const long long *__restrict__ phys0)
 {
     const int jr = blockIdx.y;
     const int n = inj[jr];
+    const long long step_total = ninc[g.ny - 1] + inj[g.ny - 1];
     for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const long long q = ninc[jr] + k;  // this step's injection index
         double uy_draw, unused, n1, n2, n3, n4, n5, n6;
@@ -257,7 +262,13 @@ __global__ void k_inject_particles(WmGeom g, WmInjectArgs a, PV dst, const int *
             const double gam1 = 1 / sqrt(1 - (v1 / a.c) * (v1 / a.c));
             const double gamp = sqrt(1 + (ux * ux + uy * uy + uz * uz) / c2);
             const int row = isp * g.ny + jr;
-            const long long p = dst.idx(row, np2[row] + k);
+            long long p = dst.idx(row, np2[row] + k);
+            if (perm) {
+                const long long ph = *phys0 + isp * step_total + q;
+                perm[p] = (unsigned)ph;
+                idperm[p] = (unsigned)ph;
+                p = ph;
+            }
             put_particle(dst, p, g, a.cell, jr, x, y, gam1 * (ux + v1 * gamp), uy, uz, -(k + 1 + ninc[jr] + nptot[isp]));
         }
     }
@@ -305,17 +316,20 @@ int wm_launch_inject_reserve(const WmGeom &g, const int *np2, const int *inj, in
 
 template <class PV>
 int wm_launch_inject_particles(const WmGeom &g, const WmInjectArgs &a, PV dst, int *np2, int *cumcnt, const int *inj,
-                               const long long *ninc, const long long *nptot, cudaStream_t st)
+                               const long long *ninc, const long long *nptot, cudaStream_t st, unsigned *perm, unsigned *idperm,
+                               const long long *phys0)
 {
-    k_inject_particles<PV><<<dim3(1, g.ny), 128, 0, st>>>(g, a, dst, np2, inj, ninc, nptot);
+    k_inject_particles<PV><<<dim3(1, g.ny), 128, 0, st>>>(g, a, dst, np2, inj, ninc, nptot, perm, idperm, phys0);
     WM_TRY(wm_check_launch("k_inject_particles"));
     k_inject_finish<<<wm_div_up(g.nrows, 256), 256, 0, st>>>(g, a, np2, cumcnt, inj);
     return wm_check_launch("k_inject_finish");
 }
 template int wm_launch_inject_particles<SoAView>(const WmGeom &, const WmInjectArgs &, SoAView, int *, int *, const int *,
-                                                 const long long *, const long long *, cudaStream_t);
+                                                 const long long *, const long long *, cudaStream_t, unsigned *, unsigned *,
+                                                 const long long *);
 template int wm_launch_inject_particles<MixedView>(const WmGeom &, const WmInjectArgs &, MixedView, int *, int *, const int *,
-                                                   const long long *, const long long *, cudaStream_t);
+                                                   const long long *, const long long *, cudaStream_t, unsigned *, unsigned *,
+                                                   const long long *);
 
 int wm_launch_inject_fields(const WmGeom &g, const WmInjectArgs &a, FView<6, false> uf, cudaStream_t st)
 {

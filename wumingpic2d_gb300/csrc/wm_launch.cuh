@@ -177,8 +177,11 @@ int wm_launch_inject_counts(const WmGeom &g, const WmInjectArgs &a, const int *n
                             unsigned *status, cudaStream_t st);
 // tmp[row] = np2[row] + inj[row % ny]: row counts with room for the new particles
 int wm_launch_inject_reserve(const WmGeom &g, const int *np2, const int *inj, int *tmp, cudaStream_t st);
-// write the new particles behind each row's sorted ones, then np2 += inj, cumcnt(nxe), total += inj
+// write the new particles behind each row's sorted ones, then np2 += inj, cumcnt(nxe), total += inj;
+// with perm (a permuted mixed state): the particles go to fresh slots from *phys0 on and perm /
+// idperm of their cell-sorted slots point there
 template <class PV>
 int wm_launch_inject_particles(const WmGeom &g, const WmInjectArgs &a, PV dst, int *np2, int *cumcnt, const int *inj,
-                               const long long *ninc, const long long *nptot, cudaStream_t st);
+                               const long long *ninc, const long long *nptot, cudaStream_t st, unsigned *perm = nullptr,
+                               unsigned *idperm = nullptr, const long long *phys0 = nullptr);
 int wm_launch_inject_fields(const WmGeom &g, const WmInjectArgs &a, FView<6, false> uf, cudaStream_t st);

@@ -614,26 +614,58 @@ __global__ void k_mixed_gather(WmGeom g, MixedView src, MixedView dst, const uns
     }
 }
 
+// FP32 -> FP64 by moving the exponent and mantissa bits (integer instructions; GB300's FP64 pipe
+// runs about 2 operations per clock per SM, and the conversion instruction would be one of them).
+// Exact, as the conversion is: zeros keep their sign, denormals, infinities and NaNs take the
+// conversion instruction.
+__device__ __forceinline__ double f2d_exact(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+    if ((u & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sign);
+    if (ex == 0u || ex == 0xffu) return (double)f;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
 // uj(k, ix, iy) over the ghosted grid = sum of the tile currents that cover the node, in the
-// order (species, cell row, tile), accumulated in FP64.
+// order (species, cell row, tile), accumulated in FP64.  A node is covered by the tiles of at most
+// 5 cell rows (iy-4 .. iy) and 2 tiles (ix/64 - 1 and ix/64); all of a species' loads are issued
+// before the sums (predicated off where the row or tile does not exist).
 __global__ void k_mixed_jfold(WmGeom g, int ntiles, const float *__restrict__ jtile, FView<3, false> uj)
 {
     const long long n = (long long)g.nxw * g.nyw;
+    const long long tstride = 3LL * 5 * MX_JW;  // floats per tile
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
         const int ix = (int)(e % g.nxw), iy = (int)(e / g.nxw);
+        const int th = min(ntiles - 1, ix / MX_TW);
+        const int lx1 = ix - th * MX_TW, lx0 = lx1 + MX_TW;  // column in tile th and in tile th-1
+        const bool t0ok = th >= 1 && lx0 < MX_JW, t1ok = lx1 < MX_JW;
         double s[3] = {0.0, 0.0, 0.0};
-        const int t_lo = max(0, (ix - MX_JW + 1 + MX_TW - 1) / MX_TW), t_hi = min(ntiles - 1, ix / MX_TW);
-        for (int isp = 0; isp < g.nsp; ++isp)
-            for (int cj = max(0, iy - 4); cj <= min(g.ny - 1, iy); ++cj) {
-                const int ly = iy - cj;
-                for (int t = t_lo; t <= t_hi; ++t) {
-                    const int lx = ix - t * MX_TW;
-                    if (lx < 0 || lx >= MX_JW) continue;
-                    const float *base = jtile + ((((long long)isp * g.ny + cj) * ntiles + t) * 3) * 5 * MX_JW;
+        for (int isp = 0; isp < g.nsp; ++isp) {
+            float v[5][2][3];
 #pragma unroll
-                    for (int k = 0; k < 3; ++k) s[k] += (double)base[(k * 5 + ly) * MX_JW + lx];
+            for (int r = 0; r < 5; ++r) {
+                const int cj = iy - 4 + r, ly = 4 - r;
+                const bool rok = cj >= 0 && cj < g.ny;
+                const float *row = jtile + (((long long)isp * g.ny + (rok ? cj : 0)) * ntiles + th) * tstride + ly * MX_JW;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    v[r][0][k] = (rok && t0ok) ? __ldg(row - tstride + k * 5 * MX_JW + lx0) : 0.f;
+                    v[r][1][k] = (rok && t1ok) ? __ldg(row + k * 5 * MX_JW + lx1) : 0.f;
                 }
             }
+#pragma unroll
+            for (int r = 0; r < 5; ++r) {
+                const int cj = iy - 4 + r;
+                const bool rok = cj >= 0 && cj < g.ny;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    if (rok && t0ok) s[k] += f2d_exact(v[r][0][k]);
+                    if (rok && t1ok) s[k] += f2d_exact(v[r][1][k]);
+                }
+            }
+        }
         uj(0, ix, iy) = s[0];
         uj(1, ix, iy) = s[1];
         uj(2, ix, iy) = s[2];

@@ -502,7 +502,7 @@ struct wm_sim {
 
     int step_mixed()
     {
-        if (!rebin_move && !inject_on && cap < (1LL << 32)) return step_mixed_perm();
+        if (!rebin_move && cap < (1LL << 32)) return step_mixed_perm();
         WM_TRY(materialize());
         WmRebinScratch sc = scratch();
         long long nl = 0;
@@ -577,14 +577,22 @@ struct wm_sim {
         if (s != WM_OK) return s;
         WM_TRY(wm_launch_mixed_incoming(g, mx_cnt9.as<int>(), mx_off9.as<int>(), sc, st));
         WM_TRY(wm_launch_scan_cells(g, sc, cumcnt_alt.as<int>(), sc.np2_new, st));
-        WM_TRY(wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st));
-        nl += 3;
+        WM_TRY(rowbases(sc));
+        nl += inject_on ? 5 : 3;
         mark("scan");
         WM_TRY(wm_launch_mixed_perm(g, rowbase[cur].as<long long>(), sc.rowbase_new, cumcnt.as<int>(), cumcnt_alt.as<int>(), mx_off9.as<int>(),
                                     sc, mx_perm.as<unsigned>(), gather ? mx_idperm[idp].as<unsigned>() : nullptr,
                                     mx_idperm[1 - idp].as<unsigned>(), st));
         ++nl;
         mark("sort_perm");
+        if (inject_on) {  // the new particles past the push output (positions in B, ids in A[5]), their slots in the permutations
+            WM_TRY(wm_launch_inject_particles(g, inj, mview(B, 1 - cur, 0), sc.np2_new, cumcnt_alt.as<int>(), inj_rows.as<int>(),
+                                              inj_ninc.as<long long>(), inj_nptot.as<long long>(), st, mx_perm.as<unsigned>(),
+                                              mx_idperm[1 - idp].as<unsigned>(), rowbase[cur].as<long long>() + g.nrows));
+            WM_TRY(wm_launch_inject_fields(g, inj, uf(), st));
+            nl += 3;
+            mark("inject");
+        }
         // set B now holds the pushed particles in the old cell order: it becomes set A (the ids
         // stay in A[5], reached through the new idperm)
         for (int c = 0; c < 5; ++c) std::swap(A[c], B[c]);
