@@ -69,6 +69,8 @@ def parse():
                    help="network trained on Harris-sheet pairs for the reconnection CG leg; 'none' skips the leg")
     p.add_argument("--reconnection-steps", type=int, default=10)
     p.add_argument("--shock-steps", type=int, default=5, help="steps of the shock leg (0 skips it)")
+    p.add_argument("--rebin", default="permute", choices=["permute", "move"],
+                   help="mixed path: the next push reads through the new order (permute) or the particles are moved every step")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
@@ -287,6 +289,8 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
     d = cfg.dims()
     t0 = time.perf_counter()
     sim = Simulation(d, cfg.delt, cfg.charge, cfg.mass, precision=precision)
+    if precision == "mixed":
+        sim.set_rebin(args.rebin)
     sim.init_weibel(cfg.ppc, cfg.v_drift, cfg.vth_e, cfg.vth_i, cfg.seed)
     t_init = time.perf_counter() - t0
     ntot, dev_bytes = sim.info()
@@ -389,11 +393,15 @@ ALGO_BYTES = {"fp64": {"push": 80, "deposit": 56, "sort_move": 96},
               "mixed_move": {"push_deposit": 44, "sort_move": 60}}
 
 
+def prec_key(res, args):
+    return "mixed_move" if res["precision"] == "mixed" and args.rebin == "move" else res["precision"]
+
+
 def all_rooflines(res, args):
     """achieved GB/s and fraction of the measured HBM peak for every particle kernel"""
     peaks, _ = measured_peaks()
     out = {}
-    for name, b in ALGO_BYTES[res["precision"]].items():
+    for name, b in ALGO_BYTES[prec_key(res, args)].items():
         t = res["ktimes"].get(name)
         if t:
             gbs = b * res["ntot"] / (t / args.steps / 1e3) / 1e9
@@ -407,14 +415,14 @@ def roofline(res, args, name=None):
     kt = res["ktimes"]
     steps = args.steps
     ntot = res["ntot"]
-    algo = ALGO_BYTES[res["precision"]]
+    algo = ALGO_BYTES[prec_key(res, args)]
     cand = {k: v for k, v in kt.items() if k in algo}
     if not cand:
         return None
     name = name or max(cand, key=cand.get)
     t = cand[name] / steps / 1e3
     achieved = algo[name] * ntot / t / 1e9
-    tr = ncu_traffic().get(f"{res['precision']}:{name}")
+    tr = ncu_traffic().get(f"{prec_key(res, args)}:{name}")
     return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
             "traffic": (tr * ntot if tr else None), "bytes_per_particle_algorithmic": algo[name],
@@ -461,7 +469,8 @@ def main():
             "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32 particles + f64 fields",
             "data": "synthetic (seeded Philox4x32-10 Weibel beams generated on the GPU)",
             "config": {"workload": workload, "nx": d.nx, "ny": d.ny, "ppc": args.ppc, "particles": res["ntot"],
-                       "precision": head, "parallelism": f"replicas x{dist.world}",
+                       "precision": head, "rebin": args.rebin if head == "mixed" else None,
+                       "parallelism": f"replicas x{dist.world}",
                        "l2": f"inputs larger than L2 ({res['ntot'] * 48 / 1e9:.1f} GB of particles vs 129 MB)",
                        "cg_iters_last_step": res["iters"], "cg_tol": 1e-6},
             "roofline": roofline(res, args),
