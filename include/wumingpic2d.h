@@ -348,6 +348,11 @@ enum { WM_CNN_FWD_TRAIN = 0, WM_CNN_FWD_INFER = 1, WM_CNN_FWD_LINEAR = 2, WM_CNN
  * over three groups of 16 channels, as in the learned guess, and only the diagonal blocks are
  * computed (the other weights must be zero; their gradient is returned as zero). */
 enum { WM_CNN_GROUPED = 16 };
+/* The forward modes (FWD_TRAIN, FWD_INFER) of the layers with cout = 48 run on the 5th-generation
+ * tensor cores (tcgen05.mma, accumulators in tensor memory) when h is a multiple of 16 and w of 8;
+ * OR-ing WM_CNN_MMA_SYNC into the mode selects the warp-level mma.sync kernel instead (the one the
+ * other modes and shapes use). */
+enum { WM_CNN_MMA_SYNC = 32 };
 
 /* One 3x3 convolution, (cin, cout) in {(16, 48), (48, 48), (48, 8)}.  Modes:
  *   FWD_TRAIN  out = GELU(conv + bias) BF16 and zout = conv + bias BF16;
@@ -357,6 +362,10 @@ enum { WM_CNN_GROUPED = 16 };
  *              transposed weights of the next layer this is the pre-activation gradient. */
 int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, int cout, int mode, int nimg, int h, int wd, void *out,
                    void *zout, const void *zprev, void *stream);
+/* WM_ERR_CUDA if a tensor-core convolution of the calls above gave up waiting for its MMAs (a
+ * bounded wait; the output of that call is not valid), else WM_OK; clear != 0 resets the flag.
+ * Call it after the stream's work has finished. */
+int wm_cnn_status(int clear);
 /* Weight and bias gradients dw[9][cout][cin] (FP32), db[cout] from the layer input x [.][cin] and
  * the pre-activation gradient dz [.][coutp], (cin, coutp) in {(16, 48), (48, 48), (48, 16)},
  * cout <= coutp.  scratch: at least 9*coutp*cin + coutp floats per CTA used (up to 304 CTAs). */

@@ -146,3 +146,52 @@ def test_learned_guess_saves_cg_iterations(gpu, trained, cg_err):
     # the answer does not depend on the guess beyond the solver tolerance
     e_prev, e_net = runs["prev"][2], runs["net"][2]
     assert abs(e_net.sum() - e_prev.sum()) <= 1e-6 * e_prev.sum()
+
+
+@pytest.mark.parametrize("cin,grouped", [(16, False), (48, True), (48, False)])
+@pytest.mark.parametrize("train", [False, True])
+def test_tensor_core_conv_matches_mma_sync_and_exact_sums(gpu, cin, grouped, train):
+    """The forward convolutions with 48 outputs run on tcgen05 (accumulators in tensor memory).
+    Against the warp-level mma.sync kernel on the same BF16 operands, and against exact float64
+    sums of those operands: the BF16 outputs agree to 1e-2 normwise (only the FP32 accumulation
+    order differs, which moves a few roundings by one unit), and the kernel reports no timeout."""
+    import ctypes
+
+    from wumingpic2d_gb300._native import check, lib
+
+    rng = np.random.default_rng(cin + 7 * grouped + 3 * train)
+    n, H, W = 2, 32, 48
+    xb = C.bf16(rng.standard_normal((n, H, W, cin)))
+    w = C.bf16(0.2 * rng.standard_normal((9, 48, cin)))
+    if grouped:
+        for go in range(3):
+            for gi in range(3):
+                if go != gi:
+                    w[:, 16 * go:16 * go + 16, 16 * gi:16 * gi + 16] = 0.0
+    b = (0.1 * rng.standard_normal(48)).astype(np.float32)
+    x_d = torch.tensor(xb, dtype=torch.float32).to("cuda", torch.bfloat16)
+    w_d = torch.tensor(w, dtype=torch.float32).to("cuda", torch.bfloat16)
+    b_d = torch.tensor(b, device="cuda")
+    outs = {}
+    for legacy in (False, True):
+        out = torch.empty((n, H, W, 48), dtype=torch.bfloat16, device="cuda")
+        z = torch.empty_like(out)
+        mode = (cnn.FWD_TRAIN if train else cnn.FWD_INFER) | (cnn.GROUPED if grouped else 0) | (32 if legacy else 0)
+        check(lib().wm_cnn_conv3x3(ctypes.c_void_p(x_d.data_ptr()), ctypes.c_void_p(w_d.data_ptr()), ctypes.c_void_p(b_d.data_ptr()),
+                                   cin, 48, mode, n, H, W, ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(z.data_ptr()), None, None),
+              "wm_cnn_conv3x3")
+        torch.cuda.synchronize()
+        outs[legacy] = (out.float().cpu().numpy(), z.float().cpu().numpy())
+    check(lib().wm_cnn_status(1), "wm_cnn_status")
+    # exact pre-activation from the same BF16 operands
+    zx = np.zeros((n, H, W, 48))
+    for tap in range(9):
+        dy, dx = tap // 3 - 1, tap % 3 - 1
+        zx += np.einsum("nhwc,oc->nhwo", np.roll(xb, (-dy, -dx), axis=(1, 2)).astype(np.float64), w[tap].astype(np.float64))
+    zx += b
+    gx = 0.5 * zx * (1 + np.vectorize(__import__("math").erf)(zx / np.sqrt(2)))
+    (a_tc, z_tc), (a_mma, z_mma) = outs[False], outs[True]
+    print(f"\ntcgen05 vs mma.sync {rel_err(a_tc, a_mma):.2e}, vs exact {rel_err(a_tc, gx):.2e} (mma.sync vs exact {rel_err(a_mma, gx):.2e})")
+    assert rel_err(a_tc, a_mma) <= 1e-2 and rel_err(a_tc, gx) <= 1e-2
+    if train:
+        assert rel_err(z_tc, zx) <= 1e-2 and rel_err(z_tc, z_mma) <= 1e-2

@@ -120,6 +120,7 @@ SIGNATURES = {
     "wm_paraio_ptcl": [_P, _P, _P, _I],
     "wm_paraio_orb": [_P, _P, _P, _I],
     "wm_cnn_conv3x3": [_P, _P, _P, _I, _I, _I, _I, _I, _I, _P, _P, _P, _P],
+    "wm_cnn_status": [_I],
     "wm_cnn_conv3x3_wgrad": [_P, _P, _I, _I, _I, _I, _I, _I, _I, _P, _P, _P, ctypes.c_int64, _P],
     "wm_cnn_mse": [_P, _P, ctypes.c_int64, _P, _P, _I, _P, _P],
     "wm_cnn_adam": [_P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _I, _P],

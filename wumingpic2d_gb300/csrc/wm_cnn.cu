@@ -27,6 +27,15 @@
 namespace {
 
 constexpr int TH = 8, TWD = 16;  // output tile: 8 rows x 16 pixels
+
+// Status word of the public entry points' tensor-core kernels (WMDEV_TIMEOUT when a bounded wait
+// ran out); read and cleared by wm_cnn_status.
+__device__ unsigned g_cnn_status;
+unsigned *cnn_status_word()
+{
+    void *p = nullptr;
+    return cudaGetSymbolAddress(&p, g_cnn_status) == cudaSuccess ? static_cast<unsigned *>(p) : nullptr;
+}
 constexpr int HALO_H = TH + 2, HALO_W = TWD + 2;
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -485,7 +494,7 @@ int wm_cnn_net_prepare(WmCnnNet &net, cudaStream_t st)
 }
 
 int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf, FView<3, false> uj, const WmCnnWork &w, double *cand,
-                       cudaStream_t st)
+                       cudaStream_t st, unsigned *status)
 {
     if (!shape_ok(1, g.ny, g.nx)) return WM_ERR_BAD_ARG;
     const long long ncell = (long long)g.nx * g.ny;
@@ -499,9 +508,13 @@ int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf,
     const void *in = w.x;
     void *bufs[2] = {w.a0, w.a1};
     for (int l = 0; l < WM_CNN_LAYERS - 1; ++l) {
-        const int grp = (wm_cnn_cin[l] == 48 && wm_cnn_cout[l] == 48) ? WM_CNN_GROUPED : 0;
-        WM_TRY(wm_cnn_conv3x3(in, net.wf[l], net.bias[l], wm_cnn_cin[l], wm_cnn_cout[l], WM_CNN_FWD_INFER | grp, 1, g.ny, g.nx,
-                              bufs[l & 1], nullptr, nullptr, st));
+        if (wm_cnn_cout[l] == 48 && wm_cnn_tc_shape_ok(1, g.ny, g.nx)) {  // tensor cores (tcgen05)
+            WM_TRY(wm_cnn_conv3x3_tc(in, net.wf[l], net.bias[l], wm_cnn_cin[l], false, 1, g.ny, g.nx, bufs[l & 1], nullptr, status, st));
+        } else {
+            const int grp = (wm_cnn_cin[l] == 48 && wm_cnn_cout[l] == 48) ? WM_CNN_GROUPED : 0;
+            WM_TRY(wm_cnn_conv3x3(in, net.wf[l], net.bias[l], wm_cnn_cin[l], wm_cnn_cout[l], WM_CNN_FWD_INFER | grp | WM_CNN_MMA_SYNC, 1,
+                                  g.ny, g.nx, bufs[l & 1], nullptr, nullptr, st));
+        }
         in = bufs[l & 1];
     }
     const int L = WM_CNN_LAYERS - 1;
@@ -518,8 +531,14 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
 {
     if (!in || !w || !out || !shape_ok(nimg, h, wd)) return WM_ERR_BAD_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const bool grouped = (mode & WM_CNN_GROUPED) != 0;
-    mode &= ~WM_CNN_GROUPED;
+    const bool grouped = (mode & WM_CNN_GROUPED) != 0, legacy = (mode & WM_CNN_MMA_SYNC) != 0;
+    mode &= ~(WM_CNN_GROUPED | WM_CNN_MMA_SYNC);
+    if (!legacy && cout == 48 && (cin == 16 || cin == 48) && (mode == WM_CNN_FWD_TRAIN || mode == WM_CNN_FWD_INFER) &&
+        wm_cnn_tc_shape_ok(nimg, h, wd)) {
+        unsigned *status = cnn_status_word();
+        if (!status) return WM_ERR_CUDA;
+        return wm_cnn_conv3x3_tc(in, w, bias, cin, mode == WM_CNN_FWD_TRAIN, nimg, h, wd, out, zout, status, st);
+    }
     if (mode != WM_CNN_BWD && !bias) return WM_ERR_BAD_ARG;
     if (mode == WM_CNN_FWD_TRAIN && !zout) return WM_ERR_BAD_ARG;
     if (mode == WM_CNN_BWD && !zprev) return WM_ERR_BAD_ARG;
@@ -539,6 +558,17 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
         if (mode == WM_CNN_FWD_LINEAR) return launch_conv<48, 8, EPI_LINEAR>(in, w, bias, nimg, h, wd, out, zout, zprev, st);
     }
     return WM_ERR_UNSUPPORTED;
+}
+
+int wm_cnn_status(int clear)
+{
+    unsigned v = 0;
+    WM_CUDA(cudaMemcpyFromSymbol(&v, g_cnn_status, sizeof v));
+    if (clear) {
+        const unsigned z = 0;
+        WM_CUDA(cudaMemcpyToSymbol(g_cnn_status, &z, sizeof z));
+    }
+    return (v & WMDEV_TIMEOUT) ? WM_ERR_CUDA : WM_OK;
 }
 
 int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int cout, int nimg, int h, int wd, int flags, float *dw,

@@ -1,0 +1,220 @@
+// wm_cnn_tc.cu -- the forward 3x3 convolutions of the learned CG guess (cout = 48) on the
+// 5th-generation tensor cores: tcgen05.mma with both operands in shared memory and the FP32
+// accumulator in tensor memory (TMEM), read back with tcgen05.ld for the bias + GELU epilogue.
+//
+// Implicit GEMM per CTA tile of 16 rows x 8 pixels: M = 128 pixels, N = 48 output channels,
+// K = 9 taps x cin, one tcgen05.mma (M128 N48 K16) per tap and 16 input channels.  The tile's
+// periodic halo (18 x 10 pixels) is stored in shared memory as 16-byte core-matrix rows,
+// [channel group of 8][halo pixel][8 channels]: eight consecutive pixels of a halo row form one
+// 8 x 16-byte core matrix, the next tile row is one halo row (160 bytes) further on and the next
+// channel group one plane further on.  So the A operand of every tap is the same no-swizzle
+// K-major layout with its start address moved by (dy, dx) -- no data is copied per tap.  The
+// weights are stored [tap][channel group][cout][8 channels], the B operand of the same form.
+// One thread issues the 27 (cin 48) or 9 (cin 16) MMAs of a tile and commits them to an mbarrier;
+// the four warps then read their 32 TMEM lanes (pixels) and write the activations.
+//
+// The network and its arithmetic are those of wm_cnn.cu (BF16 operands, FP32 accumulation); block
+// diagonal (grouped) weights are multiplied as they are, zeros included, which gives the grouped
+// result exactly.  Waits on the mbarrier are bounded: on a timeout the kernel records
+// WMDEV_TIMEOUT in its status word, waits (bounded) once more, frees its TMEM and returns.
+#include <algorithm>
+#include <cstdint>
+
+#include <cuda_bf16.h>
+
+#include "wm_launch.cuh"
+
+namespace {
+
+constexpr int TC_TH = 16, TC_TW = 8;                  // output tile: 16 rows x 8 pixels (M = 128)
+constexpr int TC_HW = TC_TW + 2, TC_HPIX = (TC_TH + 2) * TC_HW;  // halo 18 x 10 pixels
+constexpr int TC_N = 48;                              // output channels (N)
+constexpr uint32_t TC_TMEM_COLS = 64;                 // FP32 accumulator columns (power of 2 >= N)
+constexpr uint32_t TC_SPIN = 1u << 22;                // mbarrier polls before giving up
+
+// no-swizzle K-major shared-memory matrix descriptor: start address, leading (K-direction) and
+// stride (M/N-direction) byte offsets between 8 x 16-byte core matrices, descriptor version 1
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
+           (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N and M
+constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+                 "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < TC_SPIN; ++i) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]),
+                   "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float gelu_tc(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+
+// EPI: 0 = TRAIN (out = GELU(z), zout = z), 1 = INFER (out = GELU(z)); z = conv + bias, BF16.
+template <int CIN, int EPI>
+__global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ wk,
+                                                    const float *__restrict__ bias, int nimg, int H, int W, __nv_bfloat16 *__restrict__ out,
+                                                    __nv_bfloat16 *__restrict__ zout, unsigned *status)
+{
+    constexpr int KG = CIN / 8;  // channel groups of 8 (16 bytes)
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __nv_bfloat16 *w_s = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [9][KG][48][8]
+    __nv_bfloat16 *x_s = w_s + 9 * KG * TC_N * 8;                      // [KG][180][8]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(x_s + KG * TC_HPIX * 8);
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+    __shared__ int give_up;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (int e = tid; e < 9 * TC_N * KG; e += blockDim.x) {
+        const int kg = e % KG, co = (e / KG) % TC_N, tap = e / (KG * TC_N);
+        *reinterpret_cast<uint4 *>(w_s + ((tap * KG + kg) * TC_N + co) * 8) =
+            *reinterpret_cast<const uint4 *>(wk + ((long long)tap * TC_N + co) * CIN + kg * 8);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)), "r"(TC_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        give_up = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+    const uint32_t bar_a = saddr(bar);
+    const uint32_t xs_a = saddr(x_s), ws_a = saddr(w_s);
+
+    const int ntx = W / TC_TW, nty = H / TC_TH;
+    const long long ntiles = (long long)nimg * nty * ntx;
+    uint32_t phase = 0;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int n = (int)(tile / ((long long)nty * ntx));
+        const int rem = (int)(tile % ((long long)nty * ntx));
+        const int y0 = (rem / ntx) * TC_TH, x0 = (rem % ntx) * TC_TW;
+        // the tile's periodic halo in core-matrix rows
+        for (int e = tid; e < TC_HPIX * KG; e += blockDim.x) {
+            const int kg = e % KG, pix = e / KG, hy = pix / TC_HW, hx = pix % TC_HW;
+            int yy = y0 - 1 + hy, xx = x0 - 1 + hx;
+            yy += (yy < 0) ? H : (yy >= H ? -H : 0);
+            xx += (xx < 0) ? W : (xx >= W ? -W : 0);
+            *reinterpret_cast<uint4 *>(x_s + (kg * TC_HPIX + pix) * 8) =
+                *reinterpret_cast<const uint4 *>(in + (((long long)n * H + yy) * W + xx) * CIN + kg * 8);
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the halo stores, seen by the tensor core
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+#pragma unroll
+            for (int tap = 0; tap < 9; ++tap) {
+                const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+#pragma unroll
+                for (int ks = 0; ks < KG / 2; ++ks) {
+                    const uint64_t ad = smem_desc(xs_a + (uint32_t)((2 * ks * TC_HPIX + (dy + 1) * TC_HW + dx + 1) * 16), TC_HPIX * 16, TC_HW * 16);
+                    const uint64_t bd = smem_desc(ws_a + (uint32_t)(((tap * KG + 2 * ks) * TC_N) * 16), TC_N * 16, 8 * 16);
+                    mma_f16(tmem, ad, bd, (tap | ks) != 0 ? 1u : 0u);
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_a) : "memory");
+        }
+        if (!mbar_wait(bar_a, phase)) give_up = 1;
+        phase ^= 1u;
+        __syncthreads();
+        if (give_up) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        // epilogue: warp w holds TMEM lanes 32w..32w+31 = MMA rows m = 8 r + c
+        const int m = 32 * warp + lane, r = m >> 3, c = m & 7;
+        float v[TC_N];
+#pragma unroll
+        for (int q = 0; q < TC_N / 16; ++q) {
+            float t[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * q), t);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[16 * q + i] = t[i];
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        const long long p = ((long long)n * H + y0 + r) * W + x0 + c;
+#pragma unroll
+        for (int q = 0; q < TC_N / 8; ++q) {
+            uint32_t za[4], ga[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float z0 = v[8 * q + 2 * i] + bias[8 * q + 2 * i], z1 = v[8 * q + 2 * i + 1] + bias[8 * q + 2 * i + 1];
+                const __nv_bfloat162 zz = __floats2bfloat162_rn(z0, z1), gg = __floats2bfloat162_rn(gelu_tc(z0), gelu_tc(z1));
+                za[i] = *reinterpret_cast<const uint32_t *>(&zz);
+                ga[i] = *reinterpret_cast<const uint32_t *>(&gg);
+            }
+            if constexpr (EPI == 0) *reinterpret_cast<uint4 *>(zout + p * TC_N + 8 * q) = make_uint4(za[0], za[1], za[2], za[3]);
+            *reinterpret_cast<uint4 *>(out + p * TC_N + 8 * q) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();  // TMEM read and the halo consumed before the next tile's MMAs and stores
+    }
+    if (give_up) {
+        if (tid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
+        mbar_wait(bar_a, phase ^ 1u);  // the MMAs still in flight, if any (bounded)
+    }
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+}
+
+template <int CIN, int EPI>
+int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H, int W, void *out, void *zout, unsigned *status,
+              cudaStream_t st)
+{
+    constexpr int KG = CIN / 8;
+    const size_t smem = 16 * (size_t)(9 * KG * TC_N + KG * TC_HPIX) + 16;
+    WM_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<CIN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const long long ntiles = (long long)nimg * (H / TC_TH) * (W / TC_TW);
+    // resident CTAs per SM: 3 (registers), 3 x 64 TMEM columns of 512, within the shared memory
+    const int per_sm = std::max(1, std::min(3, (int)(200000 / smem)));
+    const int grid = (int)std::min<long long>(ntiles, 152LL * per_sm);
+    k_conv3x3_tc<CIN, EPI><<<grid, 128, smem, st>>>(static_cast<const __nv_bfloat16 *>(in), static_cast<const __nv_bfloat16 *>(wk), bias, nimg, H,
+                                                    W, static_cast<__nv_bfloat16 *>(out), static_cast<__nv_bfloat16 *>(zout), status);
+    return wm_check_launch("k_conv3x3_tc");
+}
+
+}  // namespace
+
+bool wm_cnn_tc_shape_ok(int nimg, int H, int W) { return nimg > 0 && H >= TC_TH && W >= TC_TW && H % TC_TH == 0 && W % TC_TW == 0; }
+
+int wm_cnn_conv3x3_tc(const void *in, const void *w, const float *bias, int cin, bool train, int nimg, int h, int wd, void *out, void *zout,
+                      unsigned *status, cudaStream_t st)
+{
+    if (!wm_cnn_tc_shape_ok(nimg, h, wd) || !status || (train && !zout)) return WM_ERR_BAD_ARG;
+    if (cin == 16) return train ? launch_tc<16, 0>(in, w, bias, nimg, h, wd, out, zout, status, st)
+                                : launch_tc<16, 1>(in, w, bias, nimg, h, wd, out, zout, status, st);
+    if (cin == 48) return train ? launch_tc<48, 0>(in, w, bias, nimg, h, wd, out, zout, status, st)
+                                : launch_tc<48, 1>(in, w, bias, nimg, h, wd, out, zout, status, st);
+    return WM_ERR_BAD_ARG;
+}

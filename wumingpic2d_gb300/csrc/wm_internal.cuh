@@ -104,7 +104,7 @@ struct FView {
 
 // ------------------------------------------------------------- device status
 // Bits OR-ed into a device status word by kernels that detect bad input.
-enum { WMDEV_CELL = 1, WMDEV_OVERFLOW = 2, WMDEV_ROWJUMP = 4 };
+enum { WMDEV_CELL = 1, WMDEV_OVERFLOW = 2, WMDEV_ROWJUMP = 4, WMDEV_TIMEOUT = 8 };
 
 // ------------------------------------------------------------------ host side
 #define WM_CUDA(call)                                                                                       \

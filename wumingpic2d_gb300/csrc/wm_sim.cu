@@ -236,7 +236,7 @@ struct wm_sim {
     {
         wm_sim *s = static_cast<wm_sim *>(ctx);
         const WmCnnWork w{s->cnn_x.p, s->cnn_a0.p, s->cnn_a1.p, s->cnn_pred.as<float>(), s->cnn_partial.as<double>(), s->cnn_scale.as<double>()};
-        return wm_cnn_infer_guess(s->g, s->net, s->uf(), s->uj(), w, s->guess_cand.as<double>(), stream);
+        return wm_cnn_infer_guess(s->g, s->net, s->uf(), s->uj(), w, s->guess_cand.as<double>(), stream, s->rb_status.as<unsigned>());
     }
 
     void mark(const char *name)
@@ -374,6 +374,7 @@ struct wm_sim {
         WM_CUDA(cudaMemcpyAsync(status_host, rb_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         WM_CUDA(cudaStreamSynchronize(st));
         const unsigned d = *status_host;
+        if (d & WMDEV_TIMEOUT) return WM_ERR_CUDA;  // a bounded wait inside a kernel ran out
         if (d & WMDEV_OVERFLOW) return WM_ERR_OVERFLOW;
         if (d & (WMDEV_CELL | WMDEV_ROWJUMP)) return WM_ERR_CELL;
         return WM_OK;
