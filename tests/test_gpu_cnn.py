@@ -150,17 +150,20 @@ def test_learned_guess_saves_cg_iterations(gpu, trained, cg_err):
 
 @pytest.mark.parametrize("cin,grouped", [(16, False), (48, True), (48, False)])
 @pytest.mark.parametrize("train", [False, True])
-def test_tensor_core_conv_matches_mma_sync_and_exact_sums(gpu, cin, grouped, train):
+@pytest.mark.parametrize("shape", [(2, 32, 48), (1, 64, 80)])
+def test_tensor_core_conv_matches_mma_sync_and_exact_sums(gpu, cin, grouped, train, shape):
     """The forward convolutions with 48 outputs run on tcgen05 (accumulators in tensor memory).
     Against the warp-level mma.sync kernel on the same BF16 operands, and against exact float64
     sums of those operands: the BF16 outputs agree to 1e-2 normwise (only the FP32 accumulation
-    order differs, which moves a few roundings by one unit), and the kernel reports no timeout."""
+    order differs, which moves a few roundings by one unit), and the kernel reports no timeout.
+    On 32 x 48 every tile's halo wraps around the periodic edges (plain loads); on 64 x 80 the
+    inner tiles' halos come by TMA."""
     import ctypes
 
     from wumingpic2d_gb300._native import check, lib
 
     rng = np.random.default_rng(cin + 7 * grouped + 3 * train)
-    n, H, W = 2, 32, 48
+    n, H, W = shape
     xb = C.bf16(rng.standard_normal((n, H, W, cin)))
     w = C.bf16(0.2 * rng.standard_normal((9, 48, cin)))
     if grouped:

@@ -20,6 +20,8 @@
 #include <algorithm>
 #include <cstdint>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
 #include "wm_launch.cuh"
@@ -28,6 +30,7 @@ namespace {
 
 constexpr int TC_TH = 16, TC_TW = 8;                  // output tile: 16 rows x 8 pixels (M = 128)
 constexpr int TC_HW = TC_TW + 2, TC_HPIX = (TC_TH + 2) * TC_HW;  // halo 18 x 10 pixels
+constexpr int TC_XP = 184;  // pixels per channel-group plane: 180 used, 2944 bytes keeps planes 128-byte aligned for TMA
 constexpr int TC_N = 48;                              // output channels (N)
 constexpr uint32_t TC_TMEM_COLS = 64;                 // FP32 accumulator columns (power of 2 >= N)
 constexpr uint32_t TC_SPIN = 1u << 22;                // mbarrier polls before giving up
@@ -79,18 +82,29 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 
 __device__ __forceinline__ float gelu_tc(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
 
+__device__ __forceinline__ void tma_halo(uint32_t dst, const CUtensorMap *tmap, int c0, int c1, int c2, int c3, uint32_t bar)
+{
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+                 : "memory");
+}
+
 // EPI: 0 = TRAIN (out = GELU(z), zout = z), 1 = INFER (out = GELU(z)); z = conv + bias, BF16.
+// Two halo buffers: while a tile's MMAs and epilogue run, the next tile's halo arrives by TMA
+// (tmap: the input [nimg][H][W][CIN] with boxes of 8 channels x 10 x 18 pixels) when it lies
+// inside the image; tiles whose halo wraps around the periodic edges load it with plain loads.
 template <int CIN, int EPI>
-__global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __nv_bfloat16 *__restrict__ in, const __nv_bfloat16 *__restrict__ wk,
-                                                    const float *__restrict__ bias, int nimg, int H, int W, __nv_bfloat16 *__restrict__ out,
-                                                    __nv_bfloat16 *__restrict__ zout, unsigned *status)
+__global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16 *__restrict__ in,
+                                                       const __nv_bfloat16 *__restrict__ wk, const float *__restrict__ bias, int nimg, int H,
+                                                       int W, __nv_bfloat16 *__restrict__ out, __nv_bfloat16 *__restrict__ zout,
+                                                       unsigned *status)
 {
     constexpr int KG = CIN / 8;  // channel groups of 8 (16 bytes)
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __nv_bfloat16 *w_s = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [9][KG][48][8]
-    __nv_bfloat16 *x_s = w_s + 9 * KG * TC_N * 8;                      // [KG][180][8]
-    uint64_t *bar = reinterpret_cast<uint64_t *>(x_s + KG * TC_HPIX * 8);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar + 1);
+    __nv_bfloat16 *x_s = w_s + 9 * KG * TC_N * 8;                      // [2][KG][TC_XP][8]
+    uint64_t *bars = reinterpret_cast<uint64_t *>(x_s + 2 * KG * TC_XP * 8);  // halo 0, halo 1, MMA
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 3);
     __shared__ int give_up;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -104,51 +118,91 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __nv_bfloat16 *__re
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar)) : "memory");
+        for (int b = 0; b < 3; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bars + b)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         give_up = 0;
     }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the weights, seen by the tensor core
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = *tslot;
-    const uint32_t bar_a = saddr(bar);
-    const uint32_t xs_a = saddr(x_s), ws_a = saddr(w_s);
+    const uint32_t mma_bar = saddr(bars + 2);
+    const uint32_t ws_a = saddr(w_s);
+    auto xs = [&](int buf) { return saddr(x_s + buf * KG * TC_XP * 8); };
 
     const int ntx = W / TC_TW, nty = H / TC_TH;
     const long long ntiles = (long long)nimg * nty * ntx;
-    uint32_t phase = 0;
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int n = (int)(tile / ((long long)nty * ntx));
-        const int rem = (int)(tile % ((long long)nty * ntx));
-        const int y0 = (rem / ntx) * TC_TH, x0 = (rem % ntx) * TC_TW;
-        // the tile's periodic halo in core-matrix rows
-        for (int e = tid; e < TC_HPIX * KG; e += blockDim.x) {
-            const int kg = e % KG, pix = e / KG, hy = pix / TC_HW, hx = pix % TC_HW;
-            int yy = y0 - 1 + hy, xx = x0 - 1 + hx;
-            yy += (yy < 0) ? H : (yy >= H ? -H : 0);
-            xx += (xx < 0) ? W : (xx >= W ? -W : 0);
-            *reinterpret_cast<uint4 *>(x_s + (kg * TC_HPIX + pix) * 8) =
-                *reinterpret_cast<const uint4 *>(in + (((long long)n * H + yy) * W + xx) * CIN + kg * 8);
+    auto coords = [&](long long t, int &n, int &y0, int &x0) {
+        n = (int)(t / ((long long)nty * ntx));
+        const int rem = (int)(t % ((long long)nty * ntx));
+        y0 = (rem / ntx) * TC_TH;
+        x0 = (rem % ntx) * TC_TW;
+    };
+    auto inside = [&](int y0, int x0) { return y0 >= 1 && y0 + TC_TH + 1 <= H && x0 >= 1 && x0 + TC_TW + 1 <= W; };
+    uint32_t pending = 0u, hph = 0u, mph = 0u;  // bit b: a TMA halo copy in flight into buffer b, its barrier's phase
+    auto issue = [&](int buf, int n, int y0, int x0) {  // one thread
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(bars + buf)), "r"((uint32_t)(KG * TC_HPIX * 16))
+                     : "memory");
+#pragma unroll
+        for (int kg = 0; kg < KG; ++kg) tma_halo(xs(buf) + (uint32_t)(kg * TC_XP * 16), &tmap, kg * 8, x0 - 1, y0 - 1, n, saddr(bars + buf));
+    };
+    if ((long long)blockIdx.x < ntiles) {
+        int n, y0, x0;
+        coords(blockIdx.x, n, y0, x0);
+        if (inside(y0, x0)) {
+            if (tid == 0) issue(0, n, y0, x0);
+            pending |= 1u;
         }
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the halo stores, seen by the tensor core
+    }
+    int buf = 0;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+        int n, y0, x0;
+        coords(tile, n, y0, x0);
+        const long long nt = tile + gridDim.x;  // the next tile's halo into the other buffer
+        if (nt < ntiles) {
+            int n1, y1, x1;
+            coords(nt, n1, y1, x1);
+            if (inside(y1, x1)) {
+                if (tid == 0) issue(buf ^ 1, n1, y1, x1);
+                pending |= 1u << (buf ^ 1);
+            }
+        }
+        if (pending & (1u << buf)) {  // this tile's halo came by TMA
+            if (!mbar_wait(saddr(bars + buf), (hph >> buf) & 1u)) give_up = 1;
+            hph ^= 1u << buf;
+            pending &= ~(1u << buf);
+        } else {  // periodic halo across the image edges: plain loads
+            __nv_bfloat16 *xb = x_s + buf * KG * TC_XP * 8;
+            for (int e = tid; e < TC_HPIX * KG; e += blockDim.x) {
+                const int kg = e % KG, pix = e / KG, hy = pix / TC_HW, hx = pix % TC_HW;
+                int yy = y0 - 1 + hy, xx = x0 - 1 + hx;
+                yy += (yy < 0) ? H : (yy >= H ? -H : 0);
+                xx += (xx < 0) ? W : (xx >= W ? -W : 0);
+                *reinterpret_cast<uint4 *>(xb + (kg * TC_XP + pix) * 8) =
+                    *reinterpret_cast<const uint4 *>(in + (((long long)n * H + yy) * W + xx) * CIN + kg * 8);
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the halo stores, seen by the tensor core
+        }
         __syncthreads();
+        if (give_up) break;
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t xa = xs(buf);
 #pragma unroll
             for (int tap = 0; tap < 9; ++tap) {
                 const int dy = tap / 3 - 1, dx = tap % 3 - 1;
 #pragma unroll
                 for (int ks = 0; ks < KG / 2; ++ks) {
-                    const uint64_t ad = smem_desc(xs_a + (uint32_t)((2 * ks * TC_HPIX + (dy + 1) * TC_HW + dx + 1) * 16), TC_HPIX * 16, TC_HW * 16);
+                    const uint64_t ad = smem_desc(xa + (uint32_t)((2 * ks * TC_XP + (dy + 1) * TC_HW + dx + 1) * 16), TC_XP * 16, TC_HW * 16);
                     const uint64_t bd = smem_desc(ws_a + (uint32_t)(((tap * KG + 2 * ks) * TC_N) * 16), TC_N * 16, 8 * 16);
                     mma_f16(tmem, ad, bd, (tap | ks) != 0 ? 1u : 0u);
                 }
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar_a) : "memory");
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mma_bar) : "memory");
         }
-        if (!mbar_wait(bar_a, phase)) give_up = 1;
-        phase ^= 1u;
+        if (!mbar_wait(mma_bar, mph)) give_up = 1;
+        mph ^= 1u;
         __syncthreads();
         if (give_up) break;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -178,14 +232,29 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __nv_bfloat16 *__re
             *reinterpret_cast<uint4 *>(out + p * TC_N + 8 * q) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();  // TMEM read and the halo consumed before the next tile's MMAs and stores
+        __syncthreads();  // TMEM read before the next tile's MMAs
     }
-    if (give_up) {
+    if (give_up) {  // the copies and MMAs still in flight, if any (bounded), before the TMEM goes
         if (tid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
-        mbar_wait(bar_a, phase ^ 1u);  // the MMAs still in flight, if any (bounded)
+        for (int b = 0; b < 2; ++b)
+            if (pending & (1u << b)) mbar_wait(saddr(bars + b), (hph >> b) & 1u);
+        mbar_wait(mma_bar, mph ^ 1u);
     }
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
 }
 
 template <int CIN, int EPI>
@@ -193,14 +262,23 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
               cudaStream_t st)
 {
     constexpr int KG = CIN / 8;
-    const size_t smem = 16 * (size_t)(9 * KG * TC_N + KG * TC_HPIX) + 16;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
+    if (!enc) return WM_ERR_CUDA;
+    CUtensorMap tmap;
+    const cuuint64_t gdim[4] = {(cuuint64_t)CIN, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)nimg};
+    const cuuint64_t gstride[3] = {(cuuint64_t)CIN * 2, (cuuint64_t)W * CIN * 2, (cuuint64_t)H * W * CIN * 2};
+    const cuuint32_t box[4] = {8, TC_HW, TC_TH + 2, 1}, estride[4] = {1, 1, 1, 1};
+    if (enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(in), gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return WM_ERR_BAD_ARG;
+    const size_t smem = 16 * (size_t)(9 * KG * TC_N + 2 * KG * TC_XP) + 32;
     WM_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<CIN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long ntiles = (long long)nimg * (H / TC_TH) * (W / TC_TW);
     // resident CTAs per SM: 3 (registers), 3 x 64 TMEM columns of 512, within the shared memory
     const int per_sm = std::max(1, std::min(3, (int)(200000 / smem)));
     const int grid = (int)std::min<long long>(ntiles, 152LL * per_sm);
-    k_conv3x3_tc<CIN, EPI><<<grid, 128, smem, st>>>(static_cast<const __nv_bfloat16 *>(in), static_cast<const __nv_bfloat16 *>(wk), bias, nimg, H,
-                                                    W, static_cast<__nv_bfloat16 *>(out), static_cast<__nv_bfloat16 *>(zout), status);
+    k_conv3x3_tc<CIN, EPI><<<grid, 128, smem, st>>>(tmap, static_cast<const __nv_bfloat16 *>(in), static_cast<const __nv_bfloat16 *>(wk), bias,
+                                                    nimg, H, W, static_cast<__nv_bfloat16 *>(out), static_cast<__nv_bfloat16 *>(zout), status);
     return wm_check_launch("k_conv3x3_tc");
 }
 
