@@ -198,3 +198,38 @@ def test_tensor_core_conv_matches_mma_sync_and_exact_sums(gpu, cin, grouped, tra
     assert rel_err(a_tc, a_mma) <= 1e-2 and rel_err(a_tc, gx) <= 1e-2
     if train:
         assert rel_err(z_tc, zx) <= 1e-2 and rel_err(z_tc, z_mma) <= 1e-2
+
+
+@pytest.mark.parametrize("shape", [(2, 32, 48), (1, 64, 80)])
+def test_tensor_core_linear_layer_matches_mma_sync(gpu, shape):
+    """The last layer (48 -> 8 channels, FP32 output) on tcgen05 with N padded to 16 zero-weight
+    channels, against the mma.sync kernel (FP32 sums in another order: 1e-5) and exact sums."""
+    import ctypes
+
+    from wumingpic2d_gb300._native import check, lib
+
+    rng = np.random.default_rng(11)
+    n, H, W = shape
+    xb = C.bf16(rng.standard_normal((n, H, W, 48)))
+    w = C.bf16(0.2 * rng.standard_normal((9, 8, 48)))
+    b = (0.1 * rng.standard_normal(8)).astype(np.float32)
+    x_d = torch.tensor(xb, dtype=torch.float32).to("cuda", torch.bfloat16)
+    w_d = torch.tensor(w, dtype=torch.float32).to("cuda", torch.bfloat16)
+    b_d = torch.tensor(b, device="cuda")
+    outs = {}
+    for legacy in (False, True):
+        out = torch.empty((n, H, W, 8), dtype=torch.float32, device="cuda")
+        check(lib().wm_cnn_conv3x3(ctypes.c_void_p(x_d.data_ptr()), ctypes.c_void_p(w_d.data_ptr()), ctypes.c_void_p(b_d.data_ptr()),
+                                   48, 8, cnn.FWD_LINEAR | (32 if legacy else 0), n, H, W, ctypes.c_void_p(out.data_ptr()), None, None,
+                                   None), "wm_cnn_conv3x3")
+        torch.cuda.synchronize()
+        outs[legacy] = out.cpu().numpy()
+    check(lib().wm_cnn_status(1), "wm_cnn_status")
+    zx = np.zeros((n, H, W, 8))
+    for tap in range(9):
+        dy, dx = tap // 3 - 1, tap % 3 - 1
+        zx += np.einsum("nhwc,oc->nhwo", np.roll(xb, (-dy, -dx), axis=(1, 2)).astype(np.float64), w[tap].astype(np.float64))
+    zx += b
+    e_mma, e_exact = rel_err(outs[False], outs[True]), rel_err(outs[False], zx)
+    print(f"\nlinear layer tcgen05 vs mma.sync {e_mma:.2e}, vs exact {e_exact:.2e}")
+    assert e_mma <= 1e-5 and e_exact <= 1e-5

@@ -508,8 +508,9 @@ int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf,
     const void *in = w.x;
     void *bufs[2] = {w.a0, w.a1};
     for (int l = 0; l < WM_CNN_LAYERS - 1; ++l) {
-        if (wm_cnn_cout[l] == 48 && wm_cnn_tc_shape_ok(1, g.ny, g.nx)) {  // tensor cores (tcgen05)
-            WM_TRY(wm_cnn_conv3x3_tc(in, net.wf[l], net.bias[l], wm_cnn_cin[l], false, 1, g.ny, g.nx, bufs[l & 1], nullptr, status, st));
+        if (wm_cnn_tc_shape_ok(1, g.ny, g.nx)) {  // tensor cores (tcgen05)
+            WM_TRY(wm_cnn_conv3x3_tc(in, net.wf[l], net.bias[l], wm_cnn_cin[l], wm_cnn_cout[l], WM_CNN_FWD_INFER, 1, g.ny, g.nx, bufs[l & 1],
+                                     nullptr, status, st));
         } else {
             const int grp = (wm_cnn_cin[l] == 48 && wm_cnn_cout[l] == 48) ? WM_CNN_GROUPED : 0;
             WM_TRY(wm_cnn_conv3x3(in, net.wf[l], net.bias[l], wm_cnn_cin[l], wm_cnn_cout[l], WM_CNN_FWD_INFER | grp | WM_CNN_MMA_SYNC, 1,
@@ -518,8 +519,12 @@ int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf,
         in = bufs[l & 1];
     }
     const int L = WM_CNN_LAYERS - 1;
-    WM_TRY(wm_cnn_conv3x3(in, net.wf[L], net.bias[L], wm_cnn_cin[L], wm_cnn_cout[L], WM_CNN_FWD_LINEAR, 1, g.ny, g.nx, w.pred, nullptr,
-                          nullptr, st));
+    if (wm_cnn_tc_shape_ok(1, g.ny, g.nx))
+        WM_TRY(wm_cnn_conv3x3_tc(in, net.wf[L], net.bias[L], wm_cnn_cin[L], wm_cnn_cout[L], WM_CNN_FWD_LINEAR, 1, g.ny, g.nx, w.pred, nullptr,
+                                 status, st));
+    else
+        WM_TRY(wm_cnn_conv3x3(in, net.wf[L], net.bias[L], wm_cnn_cin[L], wm_cnn_cout[L], WM_CNN_FWD_LINEAR | WM_CNN_MMA_SYNC, 1, g.ny, g.nx,
+                              w.pred, nullptr, nullptr, st));
     k_guess_unpack<<<blocks, 256, 0, st>>>(g, w.pred, w.scale, cand);
     return wm_check_launch("k_guess_unpack");
 }
@@ -533,11 +538,12 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const bool grouped = (mode & WM_CNN_GROUPED) != 0, legacy = (mode & WM_CNN_MMA_SYNC) != 0;
     mode &= ~(WM_CNN_GROUPED | WM_CNN_MMA_SYNC);
-    if (!legacy && cout == 48 && (cin == 16 || cin == 48) && (mode == WM_CNN_FWD_TRAIN || mode == WM_CNN_FWD_INFER) &&
-        wm_cnn_tc_shape_ok(nimg, h, wd)) {
+    const bool tc = (cout == 48 && (cin == 16 || cin == 48) && (mode == WM_CNN_FWD_TRAIN || mode == WM_CNN_FWD_INFER)) ||
+                    (cout == 8 && cin == 48 && mode == WM_CNN_FWD_LINEAR);
+    if (!legacy && tc && wm_cnn_tc_shape_ok(nimg, h, wd)) {
         unsigned *status = cnn_status_word();
         if (!status) return WM_ERR_CUDA;
-        return wm_cnn_conv3x3_tc(in, w, bias, cin, mode == WM_CNN_FWD_TRAIN, nimg, h, wd, out, zout, status, st);
+        return wm_cnn_conv3x3_tc(in, w, bias, cin, cout, mode, nimg, h, wd, out, zout, status, st);
     }
     if (mode != WM_CNN_BWD && !bias) return WM_ERR_BAD_ARG;
     if (mode == WM_CNN_FWD_TRAIN && !zout) return WM_ERR_BAD_ARG;

@@ -31,8 +31,6 @@ namespace {
 constexpr int TC_TH = 16, TC_TW = 8;                  // output tile: 16 rows x 8 pixels (M = 128)
 constexpr int TC_HW = TC_TW + 2, TC_HPIX = (TC_TH + 2) * TC_HW;  // halo 18 x 10 pixels
 constexpr int TC_XP = 184;  // pixels per channel-group plane: 180 used, 2944 bytes keeps planes 128-byte aligned for TMA
-constexpr int TC_N = 48;                              // output channels (N)
-constexpr uint32_t TC_TMEM_COLS = 64;                 // FP32 accumulator columns (power of 2 >= N)
 constexpr uint32_t TC_SPIN = 1u << 22;                // mbarrier polls before giving up
 
 // no-swizzle K-major shared-memory matrix descriptor: start address, leading (K-direction) and
@@ -43,16 +41,16 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
            (1ull << 46);
 }
 
-// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N and M
-constexpr uint32_t TC_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+// kind::f16 instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N and M = 128
+constexpr uint32_t tc_idesc(int n) { return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24); }
 
 __device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t accumulate)
+__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate)
 {
     asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
                  "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
-                 "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate)
+                 "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
                  : "memory");
 }
 
@@ -89,32 +87,35 @@ __device__ __forceinline__ void tma_halo(uint32_t dst, const CUtensorMap *tmap, 
                  : "memory");
 }
 
-// EPI: 0 = TRAIN (out = GELU(z), zout = z), 1 = INFER (out = GELU(z)); z = conv + bias, BF16.
+// EPI: 0 = TRAIN (out = GELU(z), zout = z), 1 = INFER (out = GELU(z)); z = conv + bias, BF16,
+// 48 channels.  2 = LINEAR: out = conv + bias in FP32 [.][COUT] with COUT = 8 real channels, the
+// MMA's N padded to 16 with zero weights.
 // Two halo buffers: while a tile's MMAs and epilogue run, the next tile's halo arrives by TMA
 // (tmap: the input [nimg][H][W][CIN] with boxes of 8 channels x 10 x 18 pixels) when it lies
 // inside the image; tiles whose halo wraps around the periodic edges load it with plain loads.
-template <int CIN, int EPI>
+template <int CIN, int NOUT, int COUT, int EPI>
 __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16 *__restrict__ in,
                                                        const __nv_bfloat16 *__restrict__ wk, const float *__restrict__ bias, int nimg, int H,
-                                                       int W, __nv_bfloat16 *__restrict__ out, __nv_bfloat16 *__restrict__ zout,
-                                                       unsigned *status)
+                                                       int W, void *__restrict__ out, __nv_bfloat16 *__restrict__ zout, unsigned *status)
 {
-    constexpr int KG = CIN / 8;  // channel groups of 8 (16 bytes)
+    constexpr int KG = CIN / 8;                          // channel groups of 8 (16 bytes)
+    constexpr uint32_t TMEM_COLS = NOUT > 32 ? 64 : 32;  // FP32 accumulator columns (power of 2 >= N, >= 32)
+    constexpr uint32_t IDESC = tc_idesc(NOUT);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __nv_bfloat16 *w_s = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [9][KG][48][8]
-    __nv_bfloat16 *x_s = w_s + 9 * KG * TC_N * 8;                      // [2][KG][TC_XP][8]
+    __nv_bfloat16 *x_s = w_s + 9 * KG * NOUT * 8;                      // [2][KG][TC_XP][8]
     uint64_t *bars = reinterpret_cast<uint64_t *>(x_s + 2 * KG * TC_XP * 8);  // halo 0, halo 1, MMA
     uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 3);
     __shared__ int give_up;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    for (int e = tid; e < 9 * TC_N * KG; e += blockDim.x) {
-        const int kg = e % KG, co = (e / KG) % TC_N, tap = e / (KG * TC_N);
-        *reinterpret_cast<uint4 *>(w_s + ((tap * KG + kg) * TC_N + co) * 8) =
-            *reinterpret_cast<const uint4 *>(wk + ((long long)tap * TC_N + co) * CIN + kg * 8);
+    for (int e = tid; e < 9 * NOUT * KG; e += blockDim.x) {  // [9][COUT][CIN] -> core-matrix rows, zero rows past COUT
+        const int kg = e % KG, co = (e / KG) % NOUT, tap = e / (KG * NOUT);
+        *reinterpret_cast<uint4 *>(w_s + ((tap * KG + kg) * NOUT + co) * 8) =
+            co < COUT ? *reinterpret_cast<const uint4 *>(wk + ((long long)tap * COUT + co) * CIN + kg * 8) : make_uint4(0u, 0u, 0u, 0u);
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)), "r"(TC_TMEM_COLS) : "memory");
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)), "r"(TMEM_COLS) : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
@@ -195,8 +196,8 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
 #pragma unroll
                 for (int ks = 0; ks < KG / 2; ++ks) {
                     const uint64_t ad = smem_desc(xa + (uint32_t)((2 * ks * TC_XP + (dy + 1) * TC_HW + dx + 1) * 16), TC_XP * 16, TC_HW * 16);
-                    const uint64_t bd = smem_desc(ws_a + (uint32_t)(((tap * KG + 2 * ks) * TC_N) * 16), TC_N * 16, 8 * 16);
-                    mma_f16(tmem, ad, bd, (tap | ks) != 0 ? 1u : 0u);
+                    const uint64_t bd = smem_desc(ws_a + (uint32_t)(((tap * KG + 2 * ks) * NOUT) * 16), NOUT * 16, 8 * 16);
+                    mma_f16(tmem, ad, bd, IDESC, (tap | ks) != 0 ? 1u : 0u);
                 }
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mma_bar) : "memory");
@@ -208,9 +209,9 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         // epilogue: warp w holds TMEM lanes 32w..32w+31 = MMA rows m = 8 r + c
         const int m = 32 * warp + lane, r = m >> 3, c = m & 7;
-        float v[TC_N];
+        float v[NOUT];
 #pragma unroll
-        for (int q = 0; q < TC_N / 16; ++q) {
+        for (int q = 0; q < NOUT / 16; ++q) {
             float t[16];
             tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * q), t);
 #pragma unroll
@@ -218,8 +219,15 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
         }
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
         const long long p = ((long long)n * H + y0 + r) * W + x0 + c;
+        if constexpr (EPI == 2) {
+            float *o = static_cast<float *>(out) + p * COUT;
 #pragma unroll
-        for (int q = 0; q < TC_N / 8; ++q) {
+            for (int q = 0; q < COUT / 4; ++q)
+                *reinterpret_cast<float4 *>(o + 4 * q) = make_float4(v[4 * q] + bias[4 * q], v[4 * q + 1] + bias[4 * q + 1],
+                                                                     v[4 * q + 2] + bias[4 * q + 2], v[4 * q + 3] + bias[4 * q + 3]);
+        } else {
+#pragma unroll
+        for (int q = 0; q < NOUT / 8; ++q) {
             uint32_t za[4], ga[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
@@ -228,8 +236,9 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
                 za[i] = *reinterpret_cast<const uint32_t *>(&zz);
                 ga[i] = *reinterpret_cast<const uint32_t *>(&gg);
             }
-            if constexpr (EPI == 0) *reinterpret_cast<uint4 *>(zout + p * TC_N + 8 * q) = make_uint4(za[0], za[1], za[2], za[3]);
-            *reinterpret_cast<uint4 *>(out + p * TC_N + 8 * q) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
+            if constexpr (EPI == 0) *reinterpret_cast<uint4 *>(zout + p * NOUT + 8 * q) = make_uint4(za[0], za[1], za[2], za[3]);
+            *reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + p * NOUT + 8 * q) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
+        }
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncthreads();  // TMEM read before the next tile's MMAs
@@ -241,7 +250,7 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
         mbar_wait(mma_bar, mph ^ 1u);
     }
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
@@ -257,7 +266,7 @@ PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
     return fn;
 }
 
-template <int CIN, int EPI>
+template <int CIN, int NOUT, int COUT, int EPI>
 int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H, int W, void *out, void *zout, unsigned *status,
               cudaStream_t st)
 {
@@ -271,14 +280,14 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
     if (enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(in), gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return WM_ERR_BAD_ARG;
-    const size_t smem = 16 * (size_t)(9 * KG * TC_N + 2 * KG * TC_XP) + 32;
-    WM_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<CIN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = 16 * (size_t)(9 * KG * NOUT + 2 * KG * TC_XP) + 32;
+    WM_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<CIN, NOUT, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long ntiles = (long long)nimg * (H / TC_TH) * (W / TC_TW);
     // resident CTAs per SM: 3 (registers), 3 x 64 TMEM columns of 512, within the shared memory
     const int per_sm = std::max(1, std::min(3, (int)(200000 / smem)));
     const int grid = (int)std::min<long long>(ntiles, 152LL * per_sm);
-    k_conv3x3_tc<CIN, EPI><<<grid, 128, smem, st>>>(tmap, static_cast<const __nv_bfloat16 *>(in), static_cast<const __nv_bfloat16 *>(wk), bias,
-                                                    nimg, H, W, static_cast<__nv_bfloat16 *>(out), static_cast<__nv_bfloat16 *>(zout), status);
+    k_conv3x3_tc<CIN, NOUT, COUT, EPI><<<grid, 128, smem, st>>>(tmap, static_cast<const __nv_bfloat16 *>(in), static_cast<const __nv_bfloat16 *>(wk),
+                                                                bias, nimg, H, W, out, static_cast<__nv_bfloat16 *>(zout), status);
     return wm_check_launch("k_conv3x3_tc");
 }
 
@@ -286,13 +295,14 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
 
 bool wm_cnn_tc_shape_ok(int nimg, int H, int W) { return nimg > 0 && H >= TC_TH && W >= TC_TW && H % TC_TH == 0 && W % TC_TW == 0; }
 
-int wm_cnn_conv3x3_tc(const void *in, const void *w, const float *bias, int cin, bool train, int nimg, int h, int wd, void *out, void *zout,
-                      unsigned *status, cudaStream_t st)
+int wm_cnn_conv3x3_tc(const void *in, const void *w, const float *bias, int cin, int cout, int mode, int nimg, int h, int wd, void *out,
+                      void *zout, unsigned *status, cudaStream_t st)
 {
-    if (!wm_cnn_tc_shape_ok(nimg, h, wd) || !status || (train && !zout)) return WM_ERR_BAD_ARG;
-    if (cin == 16) return train ? launch_tc<16, 0>(in, w, bias, nimg, h, wd, out, zout, status, st)
-                                : launch_tc<16, 1>(in, w, bias, nimg, h, wd, out, zout, status, st);
-    if (cin == 48) return train ? launch_tc<48, 0>(in, w, bias, nimg, h, wd, out, zout, status, st)
-                                : launch_tc<48, 1>(in, w, bias, nimg, h, wd, out, zout, status, st);
+    if (!wm_cnn_tc_shape_ok(nimg, h, wd) || !status || (mode == 0 && !zout)) return WM_ERR_BAD_ARG;
+    if (cout == 48 && cin == 16) return mode == 0 ? launch_tc<16, 48, 48, 0>(in, w, bias, nimg, h, wd, out, zout, status, st)
+                                                  : launch_tc<16, 48, 48, 1>(in, w, bias, nimg, h, wd, out, zout, status, st);
+    if (cout == 48 && cin == 48) return mode == 0 ? launch_tc<48, 48, 48, 0>(in, w, bias, nimg, h, wd, out, zout, status, st)
+                                                  : launch_tc<48, 48, 48, 1>(in, w, bias, nimg, h, wd, out, zout, status, st);
+    if (cout == 8 && cin == 48 && mode == 2) return launch_tc<48, 16, 8, 2>(in, w, bias, nimg, h, wd, out, zout, status, st);
     return WM_ERR_BAD_ARG;
 }
