@@ -13,9 +13,12 @@
 // Channel counts are padded to the tensor-core tile: the 9 inputs to 16, the 3 outputs to 8 (16
 // for the output gradient), with zero weights on the padding.
 //
-// Kernels use mma.sync.m16n8k16 BF16 with FP32 accumulation, operands staged in shared memory and
-// read with ldmatrix.  A CTA computes an 8 x 16 pixel tile for all output channels; it keeps the
-// layer's weights resident in shared memory and walks over tiles (persistent grid).
+// The forward convolutions run on the 5th-generation tensor cores (tcgen05.mma, wm_cnn_tc.cu) when
+// the image is a multiple of 16 x 8 pixels.  The kernels here use mma.sync.m16n8k16 BF16 with FP32
+// accumulation, operands staged in shared memory and read with ldmatrix: the input gradient, the
+// weight gradient, other shapes, and the forward layers on request (WM_CNN_MMA_SYNC, the cross-check
+// of the tcgen05 kernels).  A CTA computes an 8 x 16 pixel tile for all output channels; it keeps
+// the layer's weights resident in shared memory and walks over tiles (persistent grid).
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
