@@ -51,7 +51,7 @@ L2_BYTES = 129e6
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--precision", default="both", choices=["both", "fp64", "mixed"],
@@ -122,15 +122,19 @@ class ClockSampler:
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
+    """nvidia-smi samples every 50 ms, started before the warm-up (its start-up takes longer than a
+    short timed region); only the samples taken between mark_start() and mark_stop() count."""
+
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []  # (host time, line)
+        self.t0 = self.t1 = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             threading.Thread(target=self._read, daemon=True).start()
         except OSError:
@@ -138,9 +142,18 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_stop(self):
+        self.t1 = time.perf_counter()
 
     def stop(self):
+        if self.t1 is None:
+            self.mark_stop()
+        time.sleep(0.06)  # the sample that covers the end of the region
         if self.proc:
             self.proc.terminate()
             try:
@@ -149,7 +162,10 @@ class ClockSampler:
                 self.proc.kill()
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        t0 = self.t0 if self.t0 is not None else -1.0
+        for tl, ln in self.lines:
+            if not (t0 <= tl <= self.t1 + 0.06):
+                continue
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -294,13 +310,15 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
     sim.init_weibel(cfg.ppc, cfg.v_drift, cfg.vth_e, cfg.vth_i, cfg.seed)
     t_init = time.perf_counter() - t0
     ntot, dev_bytes = sim.info()
+    clocks = ClockSampler(dist.local)
+    clocks.start()
     sim.step(args.warmup)
     sim.set_timing(True)
 
-    clocks = ClockSampler(dist.local)
     dist.barrier()
-    clocks.start()
+    clocks.mark_start()
     ms = sim.step_timed(args.steps)
+    clocks.mark_stop()
     clk = clocks.stop()
     dist.barrier()
     launches = sim.launches()
