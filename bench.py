@@ -17,10 +17,11 @@ e2e      the same metric through the host-buffer entry point (wm_sim_step_host):
 roofline the dominant particle kernel's algorithmic bytes per launch / its event time.
 cpu_baseline  the CPU restatement of the reference step (oracle/, OpenMP on every host core)
          on a bounded sample of the same workload.
-learned_guess, reconnection_cg, shock
+learned_guess, reconnection_cg, shock, cnn
          the Weibel loop with the learned CG guess; the reconnection workload (Harris sheet
          4096 x 2048, CG to 1e-10) with and without its learned guess; the shock workload
-         (16384 x 1024, 32 ppc, injection every step), all on the mixed path.
+         (16384 x 1024, 32 ppc, injection every step), all on the mixed path; the guess's network
+         alone (inference on a 4096^2 image, training steps on 8 x 512^2).
 --impl reference times that CPU restatement alone (the reference is Fortran + MPI and no
 Fortran compiler exists on this machine).
 Under torchrun (N > 1) each rank runs an independent replica on its own GPU (the path does
@@ -71,6 +72,7 @@ def parse():
     p.add_argument("--shock-steps", type=int, default=5, help="steps of the shock leg (0 skips it)")
     p.add_argument("--rebin", default="permute", choices=["permute", "move"],
                    help="mixed path: the next push reads through the new order (permute) or the particles are moved every step")
+    p.add_argument("--cnn-steps", type=int, default=5, help="repetitions of the network-alone leg (0 skips it)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
@@ -297,6 +299,56 @@ def shock_leg(args):
             "cg_iters_last_step": iters}
 
 
+def cnn_leg(args):
+    """The learned guess's network alone: inference on one 4096 x 4096 image (its forward layers
+    on the tcgen05 tensor cores) and training steps (forward, MSE, input and weight gradients, Adam)
+    on batches of 8 images of 512 x 512, random inputs, the shipped weights."""
+    if args.cnn_steps <= 0 or args.guess == "none" or not os.path.exists(args.guess):
+        return None
+    import torch
+
+    from wumingpic2d_gb300 import cnn
+
+    net = cnn.GuessNet(np.load(args.guess)["params"])
+    g = torch.Generator(device="cuda").manual_seed(args.seed)
+
+    def image(n, h, w):
+        x = torch.zeros((n, h, w, cnn.LAYERS[0][0]), device="cuda")
+        x[..., :11] = torch.randn((n, h, w, 11), device="cuda", generator=g)
+        return x.to(torch.bfloat16)
+
+    def timed(fn, reps):
+        for _ in range(2):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # dense multiply-adds per pixel of the convolutions as computed (the last layer's 8 outputs padded to 16)
+    flop_px = 2 * 9 * (16 * 48 + 4 * 48 * 48 + 48 * 16)
+    x = image(1, 4096, 4096)
+    ms_inf = timed(lambda: net.forward(x, train=False), args.cnn_steps)
+    del x
+    peaks, src = measured_peaks()
+    npx = 4096 * 4096
+    tflops = flop_px * npx / (ms_inf / 1e3) / 1e12
+    xb, yb = image(8, 512, 512), torch.randn((8, 512, 512, 3), device="cuda", generator=g)
+    tr = cnn.Trainer(net)
+    ms_tr = timed(lambda: tr.step(xb, yb), args.cnn_steps)
+    return {"workload": "learned-guess network alone (6 x conv3x3, 48 channels, BF16, FP32 accumulation), random inputs",
+            "inference": {"image": "1 x 4096 x 4096", "ms": round(ms_inf, 3), "pixels_per_s": npx / (ms_inf / 1e3),
+                          "tflops_dense": round(tflops, 1), "frac_of_bf16_peak": round(tflops / peaks["bf16_tflops"], 4),
+                          "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops)", "kernels": "tcgen05 (forward layers)"},
+            "training": {"batch": "8 x 512 x 512", "ms_per_step": round(ms_tr, 3), "pixels_per_s": 8 * 512 * 512 / (ms_tr / 1e3),
+                         "kernels": "forward on tcgen05; input and weight gradients on mma.sync"},
+            "steps": args.cnn_steps}
+
+
 def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
     from wumingpic2d_gb300.sim import Simulation, pinned_zeros, set_device
 
@@ -509,6 +561,9 @@ def main():
         sh = shock_leg(args) if head == "mixed" else None
         if sh is not None:
             line["shock"] = sh
+        cl = cnn_leg(args) if head == "mixed" else None
+        if cl is not None:
+            line["cnn"] = cl
         if other is not None:
             line["fp64_path"] = {"value": other["value"], "unit": UNIT, "ms_per_step": other["ms"] / args.steps,
                                  "speedup_of_mixed": res["value"] / other["value"],
