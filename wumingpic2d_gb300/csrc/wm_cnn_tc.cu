@@ -90,24 +90,29 @@ __device__ __forceinline__ void tma_halo(uint32_t dst, const CUtensorMap *tmap, 
 // EPI: 0 = TRAIN (out = GELU(z), zout = z), 1 = INFER (out = GELU(z)); z = conv + bias, BF16,
 // 48 channels.  2 = LINEAR: out = conv + bias in FP32 [.][COUT] with COUT = 8 real channels, the
 // MMA's N padded to 16 with zero weights.
-// Two halo buffers: while a tile's MMAs and epilogue run, the next tile's halo arrives by TMA
-// (tmap: the input [nimg][H][W][CIN] with boxes of 8 channels x 10 x 18 pixels) when it lies
-// inside the image; tiles whose halo wraps around the periodic edges load it with plain loads.
+// A CTA holds one copy of the layer's weights and runs TC_GROUPS independent groups of four warps,
+// each with its own tiles, two halo buffers, mbarriers, TMEM accumulator and named barrier.  In a
+// group, while a tile's MMAs and epilogue run, the next tile's halo arrives by TMA (tmap: the input
+// [nimg][H][W][CIN] with boxes of 8 channels x 10 x 18 pixels) when it lies inside the image;
+// tiles whose halo wraps around the periodic edges load it with plain loads.
+constexpr int TC_GROUPS = 2;
 template <int CIN, int NOUT, int COUT, int EPI>
-__global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16 *__restrict__ in,
-                                                       const __nv_bfloat16 *__restrict__ wk, const float *__restrict__ bias, int nimg, int H,
-                                                       int W, void *__restrict__ out, __nv_bfloat16 *__restrict__ zout, unsigned *status)
+__global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16 *__restrict__ in,
+                                                                   const __nv_bfloat16 *__restrict__ wk, const float *__restrict__ bias,
+                                                                   int nimg, int H, int W, void *__restrict__ out,
+                                                                   __nv_bfloat16 *__restrict__ zout, unsigned *status)
 {
     constexpr int KG = CIN / 8;                          // channel groups of 8 (16 bytes)
-    constexpr uint32_t TMEM_COLS = NOUT > 32 ? 64 : 32;  // FP32 accumulator columns (power of 2 >= N, >= 32)
+    constexpr uint32_t TMEM_COLS = NOUT > 32 ? 64 : 32;  // FP32 accumulator columns of a group (power of 2 >= N, >= 32)
     constexpr uint32_t IDESC = tc_idesc(NOUT);
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __nv_bfloat16 *w_s = reinterpret_cast<__nv_bfloat16 *>(smem_raw);  // [9][KG][48][8]
-    __nv_bfloat16 *x_s = w_s + 9 * KG * NOUT * 8;                      // [2][KG][TC_XP][8]
-    uint64_t *bars = reinterpret_cast<uint64_t *>(x_s + 2 * KG * TC_XP * 8);  // halo 0, halo 1, MMA
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 3);
-    __shared__ int give_up;
+    __nv_bfloat16 *w_s = reinterpret_cast<__nv_bfloat16 *>(smem_raw);        // [9][KG][NOUT][8]
+    __nv_bfloat16 *x_all = w_s + 9 * KG * NOUT * 8;                           // [group][2][KG][TC_XP][8]
+    uint64_t *bar_all = reinterpret_cast<uint64_t *>(x_all + TC_GROUPS * 2 * KG * TC_XP * 8);  // [group][halo 0, halo 1, MMA]
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar_all + 3 * TC_GROUPS);
+    __shared__ int give_up[TC_GROUPS];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int grp = tid >> 7, gtid = tid & 127, gwarp = warp & 3;  // group, thread and warp in the group
 
     for (int e = tid; e < 9 * NOUT * KG; e += blockDim.x) {  // [9][COUT][CIN] -> core-matrix rows, zero rows past COUT
         const int kg = e % KG, co = (e / KG) % NOUT, tap = e / (KG * NOUT);
@@ -115,25 +120,30 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
             co < COUT ? *reinterpret_cast<const uint4 *>(wk + ((long long)tap * COUT + co) * CIN + kg * 8) : make_uint4(0u, 0u, 0u, 0u);
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)), "r"(TMEM_COLS) : "memory");
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)), "r"(TC_GROUPS * TMEM_COLS)
+                     : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        for (int b = 0; b < 3; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bars + b)) : "memory");
+        for (int b = 0; b < 3 * TC_GROUPS; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar_all + b)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-        give_up = 0;
+        for (int g2 = 0; g2 < TC_GROUPS; ++g2) give_up[g2] = 0;
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the weights, seen by the tensor core
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = *tslot;
+    const uint32_t tmem = *tslot + (uint32_t)(grp * TMEM_COLS);  // this group's accumulator columns
+    uint64_t *bars = bar_all + 3 * grp;
+    __nv_bfloat16 *x_s = x_all + grp * 2 * KG * TC_XP * 8;
     const uint32_t mma_bar = saddr(bars + 2);
     const uint32_t ws_a = saddr(w_s);
     auto xs = [&](int buf) { return saddr(x_s + buf * KG * TC_XP * 8); };
+    auto gsync = [&]() { asm volatile("bar.sync %0, 128;\n" ::"r"(1 + grp) : "memory"); };
 
     const int ntx = W / TC_TW, nty = H / TC_TH;
     const long long ntiles = (long long)nimg * nty * ntx;
+    const long long tstride = (long long)gridDim.x * TC_GROUPS, tfirst = (long long)blockIdx.x * TC_GROUPS + grp;
     auto coords = [&](long long t, int &n, int &y0, int &x0) {
         n = (int)(t / ((long long)nty * ntx));
         const int rem = (int)(t % ((long long)nty * ntx));
@@ -148,34 +158,34 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
 #pragma unroll
         for (int kg = 0; kg < KG; ++kg) tma_halo(xs(buf) + (uint32_t)(kg * TC_XP * 16), &tmap, kg * 8, x0 - 1, y0 - 1, n, saddr(bars + buf));
     };
-    if ((long long)blockIdx.x < ntiles) {
+    if (tfirst < ntiles) {
         int n, y0, x0;
-        coords(blockIdx.x, n, y0, x0);
+        coords(tfirst, n, y0, x0);
         if (inside(y0, x0)) {
-            if (tid == 0) issue(0, n, y0, x0);
+            if (gtid == 0) issue(0, n, y0, x0);
             pending |= 1u;
         }
     }
     int buf = 0;
-    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= 1) {
+    for (long long tile = tfirst; tile < ntiles; tile += tstride, buf ^= 1) {
         int n, y0, x0;
         coords(tile, n, y0, x0);
-        const long long nt = tile + gridDim.x;  // the next tile's halo into the other buffer
+        const long long nt = tile + tstride;  // the next tile's halo into the other buffer
         if (nt < ntiles) {
             int n1, y1, x1;
             coords(nt, n1, y1, x1);
             if (inside(y1, x1)) {
-                if (tid == 0) issue(buf ^ 1, n1, y1, x1);
+                if (gtid == 0) issue(buf ^ 1, n1, y1, x1);
                 pending |= 1u << (buf ^ 1);
             }
         }
         if (pending & (1u << buf)) {  // this tile's halo came by TMA
-            if (!mbar_wait(saddr(bars + buf), (hph >> buf) & 1u)) give_up = 1;
+            if (!mbar_wait(saddr(bars + buf), (hph >> buf) & 1u)) give_up[grp] = 1;
             hph ^= 1u << buf;
             pending &= ~(1u << buf);
         } else {  // periodic halo across the image edges: plain loads
             __nv_bfloat16 *xb = x_s + buf * KG * TC_XP * 8;
-            for (int e = tid; e < TC_HPIX * KG; e += blockDim.x) {
+            for (int e = gtid; e < TC_HPIX * KG; e += 128) {
                 const int kg = e % KG, pix = e / KG, hy = pix / TC_HW, hx = pix % TC_HW;
                 int yy = y0 - 1 + hy, xx = x0 - 1 + hx;
                 yy += (yy < 0) ? H : (yy >= H ? -H : 0);
@@ -185,9 +195,9 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
             }
             asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the halo stores, seen by the tensor core
         }
-        __syncthreads();
-        if (give_up) break;
-        if (tid == 0) {
+        gsync();
+        if (give_up[grp]) break;
+        if (gtid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const uint32_t xa = xs(buf);
 #pragma unroll
@@ -202,55 +212,55 @@ __global__ void __launch_bounds__(128, 3) k_conv3x3_tc(const __grid_constant__ C
             }
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mma_bar) : "memory");
         }
-        if (!mbar_wait(mma_bar, mph)) give_up = 1;
+        if (!mbar_wait(mma_bar, mph)) give_up[grp] = 1;
         mph ^= 1u;
-        __syncthreads();
-        if (give_up) break;
+        gsync();
+        if (give_up[grp]) break;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-        // epilogue: warp w holds TMEM lanes 32w..32w+31 = MMA rows m = 8 r + c
-        const int m = 32 * warp + lane, r = m >> 3, c = m & 7;
-        float v[NOUT];
+        // epilogue, 16 columns at a time: warp w of the group holds TMEM lanes 32w..32w+31 = MMA
+        // rows m = 8 r + c
+        const int m = 32 * gwarp + lane, r = m >> 3, c = m & 7;
+        const long long p = ((long long)n * H + y0 + r) * W + x0 + c;
 #pragma unroll
         for (int q = 0; q < NOUT / 16; ++q) {
-            float t[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * q), t);
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * gwarp) << 16) + (uint32_t)(16 * q), v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            if constexpr (EPI == 2) {
+                float *o = static_cast<float *>(out) + p * COUT;
 #pragma unroll
-            for (int i = 0; i < 16; ++i) v[16 * q + i] = t[i];
-        }
-        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        const long long p = ((long long)n * H + y0 + r) * W + x0 + c;
-        if constexpr (EPI == 2) {
-            float *o = static_cast<float *>(out) + p * COUT;
+                for (int h = 0; h < COUT / 4; ++h)
+                    *reinterpret_cast<float4 *>(o + 4 * h) = make_float4(v[4 * h] + bias[4 * h], v[4 * h + 1] + bias[4 * h + 1],
+                                                                         v[4 * h + 2] + bias[4 * h + 2], v[4 * h + 3] + bias[4 * h + 3]);
+            } else {
 #pragma unroll
-            for (int q = 0; q < COUT / 4; ++q)
-                *reinterpret_cast<float4 *>(o + 4 * q) = make_float4(v[4 * q] + bias[4 * q], v[4 * q + 1] + bias[4 * q + 1],
-                                                                     v[4 * q + 2] + bias[4 * q + 2], v[4 * q + 3] + bias[4 * q + 3]);
-        } else {
+                for (int h = 0; h < 2; ++h) {
+                    const int co = 16 * q + 8 * h;
+                    uint32_t za[4], ga[4];
 #pragma unroll
-        for (int q = 0; q < NOUT / 8; ++q) {
-            uint32_t za[4], ga[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const float z0 = v[8 * q + 2 * i] + bias[8 * q + 2 * i], z1 = v[8 * q + 2 * i + 1] + bias[8 * q + 2 * i + 1];
-                const __nv_bfloat162 zz = __floats2bfloat162_rn(z0, z1), gg = __floats2bfloat162_rn(gelu_tc(z0), gelu_tc(z1));
-                za[i] = *reinterpret_cast<const uint32_t *>(&zz);
-                ga[i] = *reinterpret_cast<const uint32_t *>(&gg);
+                    for (int i = 0; i < 4; ++i) {
+                        const float z0 = v[8 * h + 2 * i] + bias[co + 2 * i], z1 = v[8 * h + 2 * i + 1] + bias[co + 2 * i + 1];
+                        const __nv_bfloat162 zz = __floats2bfloat162_rn(z0, z1), gg = __floats2bfloat162_rn(gelu_tc(z0), gelu_tc(z1));
+                        za[i] = *reinterpret_cast<const uint32_t *>(&zz);
+                        ga[i] = *reinterpret_cast<const uint32_t *>(&gg);
+                    }
+                    if constexpr (EPI == 0) *reinterpret_cast<uint4 *>(zout + p * NOUT + co) = make_uint4(za[0], za[1], za[2], za[3]);
+                    *reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + p * NOUT + co) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
+                }
             }
-            if constexpr (EPI == 0) *reinterpret_cast<uint4 *>(zout + p * NOUT + 8 * q) = make_uint4(za[0], za[1], za[2], za[3]);
-            *reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + p * NOUT + 8 * q) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
-        }
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        __syncthreads();  // TMEM read before the next tile's MMAs
+        gsync();  // TMEM read before the group's next MMAs
     }
-    if (give_up) {  // the copies and MMAs still in flight, if any (bounded), before the TMEM goes
-        if (tid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
+    if (give_up[grp]) {  // the copies and MMAs still in flight, if any (bounded), before the TMEM goes
+        if (gtid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
         for (int b = 0; b < 2; ++b)
             if (pending & (1u << b)) mbar_wait(saddr(bars + b), (hph >> b) & 1u);
         mbar_wait(mma_bar, mph ^ 1u);
     }
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(*tslot), "r"(TC_GROUPS * TMEM_COLS) : "memory");
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
@@ -280,14 +290,15 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
     if (enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(in), gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return WM_ERR_BAD_ARG;
-    const size_t smem = 16 * (size_t)(9 * KG * NOUT + 2 * KG * TC_XP) + 32;
+    const size_t smem = 16 * (size_t)(9 * KG * NOUT + TC_GROUPS * 2 * KG * TC_XP) + 8 * 3 * TC_GROUPS + 16;
     WM_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<CIN, NOUT, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long ntiles = (long long)nimg * (H / TC_TH) * (W / TC_TW);
-    // resident CTAs per SM: 3 (registers), 3 x 64 TMEM columns of 512, within the shared memory
-    const int per_sm = std::max(1, std::min(3, (int)(200000 / smem)));
-    const int grid = (int)std::min<long long>(ntiles, 152LL * per_sm);
-    k_conv3x3_tc<CIN, NOUT, COUT, EPI><<<grid, 128, smem, st>>>(tmap, static_cast<const __nv_bfloat16 *>(in), static_cast<const __nv_bfloat16 *>(wk),
-                                                                bias, nimg, H, W, out, static_cast<__nv_bfloat16 *>(zout), status);
+    // resident CTAs per SM: at most 2 (registers; 2 x 2 x 64 TMEM columns of 512), within the shared memory
+    const int per_sm = std::max(1, std::min(2, (int)(233472 / (smem + 2048))));  // 228 KB per SM, 2 KB per CTA for the static part and the system
+    const int grid = (int)std::min<long long>((ntiles + TC_GROUPS - 1) / TC_GROUPS, 152LL * per_sm);
+    k_conv3x3_tc<CIN, NOUT, COUT, EPI><<<grid, 128 * TC_GROUPS, smem, st>>>(tmap, static_cast<const __nv_bfloat16 *>(in),
+                                                                            static_cast<const __nv_bfloat16 *>(wk), bias, nimg, H, W, out,
+                                                                            static_cast<__nv_bfloat16 *>(zout), status);
     return wm_check_launch("k_conv3x3_tc");
 }
 
