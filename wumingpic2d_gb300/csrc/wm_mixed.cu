@@ -630,45 +630,67 @@ __device__ __forceinline__ double f2d_exact(float f)
 
 // uj(k, ix, iy) over the ghosted grid = sum of the tile currents that cover the node, in the
 // order (species, cell row, tile), accumulated in FP64.  A node is covered by the tiles of at most
-// 5 cell rows (iy-4 .. iy) and 2 tiles (ix/64 - 1 and ix/64); all of a species' loads are issued
-// before the sums (predicated off where the row or tile does not exist).
-__global__ void k_mixed_jfold(WmGeom g, int ntiles, const float *__restrict__ jtile, FView<3, false> uj)
+// 5 cell rows (iy-4 .. iy) and, in the first 4 columns of every tile but the first, by 2 tiles
+// (ix/32 - 1 and ix/32).  The threads take those two-tile columns first and the one-tile columns
+// after, so a warp's lanes agree on the number of tiles and the FP64 pipe issues no adds that are
+// switched off; all of a node's loads are issued before its sums.
+template <bool PAIR>
+__device__ __forceinline__ void jfold_node(const WmGeom &g, int ntiles, const float *__restrict__ jtile, FView<3, false> &uj, int ix, int iy)
 {
-    const long long n = (long long)g.nxw * g.nyw;
     const long long tstride = 3LL * 5 * MX_JW;  // floats per tile
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
-        const int ix = (int)(e % g.nxw), iy = (int)(e / g.nxw);
-        const int th = min(ntiles - 1, ix / MX_TW);
-        const int lx1 = ix - th * MX_TW, lx0 = lx1 + MX_TW;  // column in tile th and in tile th-1
-        const bool t0ok = th >= 1 && lx0 < MX_JW, t1ok = lx1 < MX_JW;
-        double s[3] = {0.0, 0.0, 0.0};
-        for (int isp = 0; isp < g.nsp; ++isp) {
-            float v[5][2][3];
+    const int th = min(ntiles - 1, ix / MX_TW);
+    const int lx1 = ix - th * MX_TW, lx0 = lx1 + MX_TW;  // column in tile th and (PAIR) in tile th-1
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int isp = 0; isp < g.nsp; ++isp) {
+        float v[5][2][3];
 #pragma unroll
-            for (int r = 0; r < 5; ++r) {
-                const int cj = iy - 4 + r, ly = 4 - r;
-                const bool rok = cj >= 0 && cj < g.ny;
-                const float *row = jtile + (((long long)isp * g.ny + (rok ? cj : 0)) * ntiles + th) * tstride + ly * MX_JW;
+        for (int r = 0; r < 5; ++r) {
+            const int cj = iy - 4 + r, ly = 4 - r;
+            const bool rok = cj >= 0 && cj < g.ny;
+            const float *row = jtile + (((long long)isp * g.ny + (rok ? cj : 0)) * ntiles + th) * tstride + ly * MX_JW;
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    v[r][0][k] = (rok && t0ok) ? __ldg(row - tstride + k * 5 * MX_JW + lx0) : 0.f;
-                    v[r][1][k] = (rok && t1ok) ? __ldg(row + k * 5 * MX_JW + lx1) : 0.f;
-                }
-            }
-#pragma unroll
-            for (int r = 0; r < 5; ++r) {
-                const int cj = iy - 4 + r;
-                const bool rok = cj >= 0 && cj < g.ny;
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    if (rok && t0ok) s[k] += f2d_exact(v[r][0][k]);
-                    if (rok && t1ok) s[k] += f2d_exact(v[r][1][k]);
-                }
+            for (int k = 0; k < 3; ++k) {
+                if constexpr (PAIR) v[r][0][k] = rok ? __ldg(row - tstride + k * 5 * MX_JW + lx0) : 0.f;
+                v[r][1][k] = rok ? __ldg(row + k * 5 * MX_JW + lx1) : 0.f;
             }
         }
-        uj(0, ix, iy) = s[0];
-        uj(1, ix, iy) = s[1];
-        uj(2, ix, iy) = s[2];
+#pragma unroll
+        for (int r = 0; r < 5; ++r) {
+            const int cj = iy - 4 + r;
+            if (cj < 0 || cj >= g.ny) continue;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                if constexpr (PAIR) s[k] += f2d_exact(v[r][0][k]);
+                s[k] += f2d_exact(v[r][1][k]);
+            }
+        }
+    }
+    uj(0, ix, iy) = s[0];
+    uj(1, ix, iy) = s[1];
+    uj(2, ix, iy) = s[2];
+}
+
+__global__ void k_mixed_jfold(WmGeom g, int ntiles, const float *__restrict__ jtile, FView<3, false> uj)
+{
+    const int npc = 4 * max(0, min(ntiles - 1, (g.nxw - MX_TW) / MX_TW + 1));  // two-tile columns 32t .. 32t+3, t = 1 .. ntiles-1
+    const int nsc = g.nxw - npc;                                                // the other columns
+    const long long npair = (long long)npc * g.nyw, n = (long long)g.nxw * g.nyw;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        if (e < npair) {
+            const int iy = (int)(e / npc), j = (int)(e % npc);
+            jfold_node<true>(g, ntiles, jtile, uj, MX_TW * (1 + j / 4) + j % 4, iy);
+        } else {
+            const long long m = e - npair;
+            const int iy = (int)(m / nsc), j = (int)(m % nsc);
+            int ix;
+            if (j < MX_TW) {
+                ix = j;  // tile 0
+            } else {
+                const int j2 = j - MX_TW, blk = j2 / (MX_TW - 4);
+                ix = blk < ntiles - 1 ? MX_TW * (1 + blk) + 4 + j2 % (MX_TW - 4) : MX_TW * ntiles + (j2 - (MX_TW - 4) * (ntiles - 1));
+            }
+            jfold_node<false>(g, ntiles, jtile, uj, ix, iy);
+        }
     }
 }
 
