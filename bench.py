@@ -345,7 +345,7 @@ def cnn_leg(args):
                           "tflops_dense": round(tflops, 1), "frac_of_bf16_peak": round(tflops / peaks["bf16_tflops"], 4),
                           "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops)", "kernels": "tcgen05 (forward layers)"},
             "training": {"batch": "8 x 512 x 512", "ms_per_step": round(ms_tr, 3), "pixels_per_s": 8 * 512 * 512 / (ms_tr / 1e3),
-                         "kernels": "forward on tcgen05; input and weight gradients on mma.sync"},
+                         "kernels": "forward and input gradient on tcgen05; weight gradient on mma.sync"},
             "steps": args.cnn_steps}
 
 

@@ -348,10 +348,10 @@ enum { WM_CNN_FWD_TRAIN = 0, WM_CNN_FWD_INFER = 1, WM_CNN_FWD_LINEAR = 2, WM_CNN
  * over three groups of 16 channels, as in the learned guess, and only the diagonal blocks are
  * computed (the other weights must be zero; their gradient is returned as zero). */
 enum { WM_CNN_GROUPED = 16 };
-/* The forward modes (FWD_TRAIN, FWD_INFER, FWD_LINEAR) run on the 5th-generation tensor cores
- * (tcgen05.mma, accumulators in tensor memory) when h is a multiple of 16 and w of 8; OR-ing
- * WM_CNN_MMA_SYNC into the mode selects the warp-level mma.sync kernel instead (the one the
- * backward mode and other shapes use). */
+/* The convolutions (all four modes) run on the 5th-generation tensor cores (tcgen05.mma,
+ * accumulators in tensor memory) when h is a multiple of 16 and w of 8; OR-ing WM_CNN_MMA_SYNC
+ * into the mode selects the warp-level mma.sync kernel instead (the one other shapes and the
+ * weight gradient use). */
 enum { WM_CNN_MMA_SYNC = 32 };
 
 /* One 3x3 convolution, (cin, cout) in {(16, 48), (48, 48), (48, 8)}.  Modes:

@@ -233,3 +233,42 @@ def test_tensor_core_linear_layer_matches_mma_sync(gpu, shape):
     e_mma, e_exact = rel_err(outs[False], outs[True]), rel_err(outs[False], zx)
     print(f"\nlinear layer tcgen05 vs mma.sync {e_mma:.2e}, vs exact {e_exact:.2e}")
     assert e_mma <= 1e-5 and e_exact <= 1e-5
+
+
+@pytest.mark.parametrize("cin", [16, 48])
+@pytest.mark.parametrize("shape", [(2, 32, 48), (1, 64, 80)])
+def test_tensor_core_input_gradient_matches_mma_sync(gpu, cin, shape):
+    """The input-gradient convolution of training (out = conv * GELU'(zprev), no bias) on tcgen05
+    against the mma.sync kernel and against exact sums of the same BF16 operands."""
+    import ctypes
+    import math
+
+    from wumingpic2d_gb300._native import check, lib
+
+    rng = np.random.default_rng(cin + 1)
+    n, H, W = shape
+    xb = C.bf16(rng.standard_normal((n, H, W, cin)))
+    w = C.bf16(0.2 * rng.standard_normal((9, 48, cin)))
+    zp = C.bf16(rng.standard_normal((n, H, W, 48)))
+    x_d = torch.tensor(xb, dtype=torch.float32).to("cuda", torch.bfloat16)
+    w_d = torch.tensor(w, dtype=torch.float32).to("cuda", torch.bfloat16)
+    z_d = torch.tensor(zp, dtype=torch.float32).to("cuda", torch.bfloat16)
+    outs = {}
+    for legacy in (False, True):
+        out = torch.empty((n, H, W, 48), dtype=torch.bfloat16, device="cuda")
+        check(lib().wm_cnn_conv3x3(ctypes.c_void_p(x_d.data_ptr()), ctypes.c_void_p(w_d.data_ptr()), None, cin, 48,
+                                   cnn.BWD | (32 if legacy else 0), n, H, W, ctypes.c_void_p(out.data_ptr()), None,
+                                   ctypes.c_void_p(z_d.data_ptr()), None), "wm_cnn_conv3x3")
+        torch.cuda.synchronize()
+        outs[legacy] = out.float().cpu().numpy()
+    check(lib().wm_cnn_status(1), "wm_cnn_status")
+    acc = np.zeros((n, H, W, 48))
+    for tap in range(9):
+        dy, dx = tap // 3 - 1, tap % 3 - 1
+        acc += np.einsum("nhwc,oc->nhwo", np.roll(xb, (-dy, -dx), axis=(1, 2)).astype(np.float64), w[tap].astype(np.float64))
+    erf = np.vectorize(math.erf)
+    gp = 0.5 * (1 + erf(zp / np.sqrt(2))) + zp * np.exp(-0.5 * zp**2) / np.sqrt(2 * np.pi)
+    ref = acc * gp
+    e_mma, e_exact = rel_err(outs[False], outs[True]), rel_err(outs[False], ref)
+    print(f"\ninput gradient tcgen05 vs mma.sync {e_mma:.2e}, vs exact {e_exact:.2e}")
+    assert e_mma <= 1e-2 and e_exact <= 1e-2

@@ -13,11 +13,11 @@
 // Channel counts are padded to the tensor-core tile: the 9 inputs to 16, the 3 outputs to 8 (16
 // for the output gradient), with zero weights on the padding.
 //
-// The forward convolutions run on the 5th-generation tensor cores (tcgen05.mma, wm_cnn_tc.cu) when
-// the image is a multiple of 16 x 8 pixels.  The kernels here use mma.sync.m16n8k16 BF16 with FP32
-// accumulation, operands staged in shared memory and read with ldmatrix: the input gradient, the
-// weight gradient, other shapes, and the forward layers on request (WM_CNN_MMA_SYNC, the cross-check
-// of the tcgen05 kernels).  A CTA computes an 8 x 16 pixel tile for all output channels; it keeps
+// The convolutions (forward and input gradient) run on the 5th-generation tensor cores (tcgen05.mma,
+// wm_cnn_tc.cu) when the image is a multiple of 16 x 8 pixels.  The kernels here use
+// mma.sync.m16n8k16 BF16 with FP32 accumulation, operands staged in shared memory and read with
+// ldmatrix: the weight gradient, other shapes, and the convolutions on request (WM_CNN_MMA_SYNC, the
+// cross-check of the tcgen05 kernels).  A CTA computes an 8 x 16 pixel tile for all output channels; it keeps
 // the layer's weights resident in shared memory and walks over tiles (persistent grid).
 #include <algorithm>
 #include <cmath>
@@ -513,7 +513,7 @@ int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf,
     for (int l = 0; l < WM_CNN_LAYERS - 1; ++l) {
         if (wm_cnn_tc_shape_ok(1, g.ny, g.nx)) {  // tensor cores (tcgen05)
             WM_TRY(wm_cnn_conv3x3_tc(in, net.wf[l], net.bias[l], wm_cnn_cin[l], wm_cnn_cout[l], WM_CNN_FWD_INFER, 1, g.ny, g.nx, bufs[l & 1],
-                                     nullptr, status, st));
+                                     nullptr, nullptr, status, st));
         } else {
             const int grp = (wm_cnn_cin[l] == 48 && wm_cnn_cout[l] == 48) ? WM_CNN_GROUPED : 0;
             WM_TRY(wm_cnn_conv3x3(in, net.wf[l], net.bias[l], wm_cnn_cin[l], wm_cnn_cout[l], WM_CNN_FWD_INFER | grp | WM_CNN_MMA_SYNC, 1,
@@ -524,7 +524,7 @@ int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf,
     const int L = WM_CNN_LAYERS - 1;
     if (wm_cnn_tc_shape_ok(1, g.ny, g.nx))
         WM_TRY(wm_cnn_conv3x3_tc(in, net.wf[L], net.bias[L], wm_cnn_cin[L], wm_cnn_cout[L], WM_CNN_FWD_LINEAR, 1, g.ny, g.nx, w.pred, nullptr,
-                                 status, st));
+                                 nullptr, status, st));
     else
         WM_TRY(wm_cnn_conv3x3(in, net.wf[L], net.bias[L], wm_cnn_cin[L], wm_cnn_cout[L], WM_CNN_FWD_LINEAR | WM_CNN_MMA_SYNC, 1, g.ny, g.nx,
                               w.pred, nullptr, nullptr, st));
@@ -541,12 +541,12 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const bool grouped = (mode & WM_CNN_GROUPED) != 0, legacy = (mode & WM_CNN_MMA_SYNC) != 0;
     mode &= ~(WM_CNN_GROUPED | WM_CNN_MMA_SYNC);
-    const bool tc = (cout == 48 && (cin == 16 || cin == 48) && (mode == WM_CNN_FWD_TRAIN || mode == WM_CNN_FWD_INFER)) ||
+    const bool tc = (cout == 48 && (cin == 16 || cin == 48) && (mode == WM_CNN_FWD_TRAIN || mode == WM_CNN_FWD_INFER || mode == WM_CNN_BWD)) ||
                     (cout == 8 && cin == 48 && mode == WM_CNN_FWD_LINEAR);
     if (!legacy && tc && wm_cnn_tc_shape_ok(nimg, h, wd)) {
         unsigned *status = cnn_status_word();
         if (!status) return WM_ERR_CUDA;
-        return wm_cnn_conv3x3_tc(in, w, bias, cin, cout, mode, nimg, h, wd, out, zout, status, st);
+        return wm_cnn_conv3x3_tc(in, w, bias, cin, cout, mode, nimg, h, wd, out, zout, zprev, status, st);
     }
     if (mode != WM_CNN_BWD && !bias) return WM_ERR_BAD_ARG;
     if (mode == WM_CNN_FWD_TRAIN && !zout) return WM_ERR_BAD_ARG;

@@ -1,6 +1,7 @@
 // wm_cnn_tc.cu -- the forward 3x3 convolutions of the learned CG guess (cout = 48) on the
 // 5th-generation tensor cores: tcgen05.mma with both operands in shared memory and the FP32
-// accumulator in tensor memory (TMEM), read back with tcgen05.ld for the bias + GELU epilogue.
+// accumulator in tensor memory (TMEM), read back with tcgen05.ld for the epilogue (bias + GELU, or
+// GELU' for the input gradient of training).
 //
 // Implicit GEMM per CTA tile of 16 rows x 8 pixels: M = 128 pixels, N = 48 output channels,
 // K = 9 taps x cin, one tcgen05.mma (M128 N48 K16) per tap and 16 input channels.  The tile's
@@ -79,6 +80,11 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
 }
 
 __device__ __forceinline__ float gelu_tc(float z) { return 0.5f * z * (1.f + erff(z * 0.70710678118654752f)); }
+// d GELU / dz = Phi(z) + z phi(z)
+__device__ __forceinline__ float gelu_grad_tc(float z)
+{
+    return 0.5f * (1.f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+}
 
 __device__ __forceinline__ void tma_halo(uint32_t dst, const CUtensorMap *tmap, int c0, int c1, int c2, int c3, uint32_t bar)
 {
@@ -89,7 +95,8 @@ __device__ __forceinline__ void tma_halo(uint32_t dst, const CUtensorMap *tmap, 
 
 // EPI: 0 = TRAIN (out = GELU(z), zout = z), 1 = INFER (out = GELU(z)); z = conv + bias, BF16,
 // 48 channels.  2 = LINEAR: out = conv + bias in FP32 [.][COUT] with COUT = 8 real channels, the
-// MMA's N padded to 16 with zero weights.
+// MMA's N padded to 16 with zero weights.  3 = BWD (the input gradient of training): out = conv *
+// GELU'(zprev) in BF16, no bias.
 // A CTA holds one copy of the layer's weights and runs TC_GROUPS independent groups of four warps,
 // each with its own tiles, two halo buffers, mbarriers, TMEM accumulator and named barrier.  In a
 // group, while a tile's MMAs and epilogue run, the next tile's halo arrives by TMA (tmap: the input
@@ -100,7 +107,8 @@ template <int CIN, int NOUT, int COUT, int EPI>
 __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_constant__ CUtensorMap tmap, const __nv_bfloat16 *__restrict__ in,
                                                                    const __nv_bfloat16 *__restrict__ wk, const float *__restrict__ bias,
                                                                    int nimg, int H, int W, void *__restrict__ out,
-                                                                   __nv_bfloat16 *__restrict__ zout, unsigned *status)
+                                                                   __nv_bfloat16 *__restrict__ zout, const __nv_bfloat16 *__restrict__ zprev,
+                                                                   unsigned *status)
 {
     constexpr int KG = CIN / 8;                          // channel groups of 8 (16 bytes)
     constexpr uint32_t TMEM_COLS = NOUT > 32 ? 64 : 32;  // FP32 accumulator columns of a group (power of 2 >= N, >= 32)
@@ -226,7 +234,23 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
             float v[16];
             tmem_ld16(tmem + ((uint32_t)(32 * gwarp) << 16) + (uint32_t)(16 * q), v);
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-            if constexpr (EPI == 2) {
+            if constexpr (EPI == 3) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int co = 16 * q + 8 * h;
+                    const uint4 zz = *reinterpret_cast<const uint4 *>(zprev + p * NOUT + co);
+                    const uint32_t zw[4] = {zz.x, zz.y, zz.z, zz.w};
+                    uint32_t ga[4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        const __nv_bfloat162 zp = *reinterpret_cast<const __nv_bfloat162 *>(&zw[i]);
+                        const __nv_bfloat162 gg = __floats2bfloat162_rn(v[8 * h + 2 * i] * gelu_grad_tc(__bfloat162float(zp.x)),
+                                                                        v[8 * h + 2 * i + 1] * gelu_grad_tc(__bfloat162float(zp.y)));
+                        ga[i] = *reinterpret_cast<const uint32_t *>(&gg);
+                    }
+                    *reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + p * NOUT + co) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
+                }
+            } else if constexpr (EPI == 2) {
                 float *o = static_cast<float *>(out) + p * COUT;
 #pragma unroll
                 for (int h = 0; h < COUT / 4; ++h)
@@ -277,8 +301,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
 }
 
 template <int CIN, int NOUT, int COUT, int EPI>
-int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H, int W, void *out, void *zout, unsigned *status,
-              cudaStream_t st)
+int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H, int W, void *out, void *zout, const void *zprev,
+              unsigned *status, cudaStream_t st)
 {
     constexpr int KG = CIN / 8;
     PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
@@ -298,7 +322,8 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
     const int grid = (int)std::min<long long>((ntiles + TC_GROUPS - 1) / TC_GROUPS, 152LL * per_sm);
     k_conv3x3_tc<CIN, NOUT, COUT, EPI><<<grid, 128 * TC_GROUPS, smem, st>>>(tmap, static_cast<const __nv_bfloat16 *>(in),
                                                                             static_cast<const __nv_bfloat16 *>(wk), bias, nimg, H, W, out,
-                                                                            static_cast<__nv_bfloat16 *>(zout), status);
+                                                                            static_cast<__nv_bfloat16 *>(zout),
+                                                                            static_cast<const __nv_bfloat16 *>(zprev), status);
     return wm_check_launch("k_conv3x3_tc");
 }
 
@@ -307,13 +332,18 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
 bool wm_cnn_tc_shape_ok(int nimg, int H, int W) { return nimg > 0 && H >= TC_TH && W >= TC_TW && H % TC_TH == 0 && W % TC_TW == 0; }
 
 int wm_cnn_conv3x3_tc(const void *in, const void *w, const float *bias, int cin, int cout, int mode, int nimg, int h, int wd, void *out,
-                      void *zout, unsigned *status, cudaStream_t st)
+                      void *zout, const void *zprev, unsigned *status, cudaStream_t st)
 {
-    if (!wm_cnn_tc_shape_ok(nimg, h, wd) || !status || (mode == 0 && !zout)) return WM_ERR_BAD_ARG;
-    if (cout == 48 && cin == 16) return mode == 0 ? launch_tc<16, 48, 48, 0>(in, w, bias, nimg, h, wd, out, zout, status, st)
-                                                  : launch_tc<16, 48, 48, 1>(in, w, bias, nimg, h, wd, out, zout, status, st);
-    if (cout == 48 && cin == 48) return mode == 0 ? launch_tc<48, 48, 48, 0>(in, w, bias, nimg, h, wd, out, zout, status, st)
-                                                  : launch_tc<48, 48, 48, 1>(in, w, bias, nimg, h, wd, out, zout, status, st);
-    if (cout == 8 && cin == 48 && mode == 2) return launch_tc<48, 16, 8, 2>(in, w, bias, nimg, h, wd, out, zout, status, st);
+    if (!wm_cnn_tc_shape_ok(nimg, h, wd) || !status || (mode == 0 && !zout) || (mode == 3 && !zprev) || (mode != 3 && !bias))
+        return WM_ERR_BAD_ARG;
+    if (cout == 48 && (cin == 16 || cin == 48)) {
+        if (mode == 0) return cin == 16 ? launch_tc<16, 48, 48, 0>(in, w, bias, nimg, h, wd, out, zout, zprev, status, st)
+                                        : launch_tc<48, 48, 48, 0>(in, w, bias, nimg, h, wd, out, zout, zprev, status, st);
+        if (mode == 1) return cin == 16 ? launch_tc<16, 48, 48, 1>(in, w, bias, nimg, h, wd, out, zout, zprev, status, st)
+                                        : launch_tc<48, 48, 48, 1>(in, w, bias, nimg, h, wd, out, zout, zprev, status, st);
+        if (mode == 3) return cin == 16 ? launch_tc<16, 48, 48, 3>(in, w, bias, nimg, h, wd, out, zout, zprev, status, st)
+                                        : launch_tc<48, 48, 48, 3>(in, w, bias, nimg, h, wd, out, zout, zprev, status, st);
+    }
+    if (cout == 8 && cin == 48 && mode == 2) return launch_tc<48, 16, 8, 2>(in, w, bias, nimg, h, wd, out, zout, zprev, status, st);
     return WM_ERR_BAD_ARG;
 }

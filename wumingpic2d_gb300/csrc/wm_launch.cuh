@@ -135,12 +135,12 @@ int wm_cnn_net_prepare(WmCnnNet &net, cudaStream_t st);
 int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf, FView<3, false> uj, const WmCnnWork &w, double *cand,
                        cudaStream_t st,
                        unsigned *status);
-// wm_cnn_tc.cu: the forward convolutions on tcgen05 (h a multiple of 16, w of 8): (cin, cout) =
-// (16, 48) or (48, 48) with mode WM_CNN_FWD_TRAIN / _INFER, (48, 8) with WM_CNN_FWD_LINEAR; a
+// wm_cnn_tc.cu: the convolutions on tcgen05 (h a multiple of 16, w of 8): (cin, cout) = (16, 48) or
+// (48, 48) with mode WM_CNN_FWD_TRAIN / _INFER / _BWD (zprev), (48, 8) with WM_CNN_FWD_LINEAR; a
 // timed-out wait sets WMDEV_TIMEOUT in *status
 bool wm_cnn_tc_shape_ok(int nimg, int H, int W);
 int wm_cnn_conv3x3_tc(const void *in, const void *w, const float *bias, int cin, int cout, int mode, int nimg, int h, int wd, void *out,
-                      void *zout, unsigned *status, cudaStream_t st);
+                      void *zout, const void *zprev, unsigned *status, cudaStream_t st);
 
 // wm_paraio.cu: the resident state in the order of the paraio files
 int wm_launch_mom_file(const WmGeom &g, const double *mom, FView<6, false> uf, double *out, cudaStream_t st);
