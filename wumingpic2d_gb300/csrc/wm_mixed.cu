@@ -393,15 +393,21 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
             cx[m] = cx[m - 1] + dsx[m];
             cy[m] = cy[m - 1] + dsy[m];
         }
+        // the species factor folded into the cumulative weights, qg/2 and qg/3 formed once
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            cx[m] *= mq;
+            cy[m] *= mq;
+        }
+        const float qh = 0.5f * qg, q3 = (1.f / 3.f) * qg;
 #pragma unroll
         for (int jp = 0; jp < 5; ++jp) {
             const bool inner = jp >= 1 && jp <= 3;
             const float wy = inner ? s0y[jp] + 0.5f * dsy[jp] : 0.5f * dsy[jp];
-            const float fy = mq * wy;
 #pragma unroll
-            for (int m = 0; m < 4; ++m) ax[jp][m] = fmaf(fy, cx[m], ax[jp][m]);
+            for (int m = 0; m < 4; ++m) ax[jp][m] = fmaf(wy, cx[m], ax[jp][m]);
             const float z1 = qg * wy;
-            const float z2 = qg * (inner ? 0.5f * s0y[jp] + (1.f / 3.f) * dsy[jp] : (1.f / 3.f) * dsy[jp]);
+            const float z2 = inner ? fmaf(qh, s0y[jp], q3 * dsy[jp]) : q3 * dsy[jp];
 #pragma unroll
             for (int ip = 0; ip < 5; ++ip) {
                 az[jp][ip] = fmaf(dsx[ip], z2, az[jp][ip]);
@@ -410,7 +416,7 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
         }
 #pragma unroll
         for (int ip = 0; ip < 5; ++ip) {
-            const float fx = mq * ((ip >= 1 && ip <= 3) ? s0x[ip] + 0.5f * dsx[ip] : 0.5f * dsx[ip]);
+            const float fx = (ip >= 1 && ip <= 3) ? s0x[ip] + 0.5f * dsx[ip] : 0.5f * dsx[ip];
 #pragma unroll
             for (int m = 0; m < 4; ++m) ay[m][ip] = fmaf(fx, cy[m], ay[m][ip]);
         }
