@@ -3,18 +3,21 @@
 // Particles carry their position as (cell, FP32 offset in [0,1)) -- the cell is implicit in the
 // cell-sorted rows -- and FP32 momenta.  k_mixed_fields turns the FP64 Yee fields into the
 // cell-centred fields of particle.f90:68-81 once per step, as FP32.  k_mixed_push_deposit then
-// does, for one (species, row, 64-cell tile): the Buneman-Boris push of particle.f90:96-161 in
+// does, for one (species, row, 32-cell tile): the Buneman-Boris push of particle.f90:96-161 in
 // FP32, the Esirkepov deposit of field.f90:224-298 in FP32, the periodic wrap of
 // boundary_periodic.f90:61-96 and :143-165 as integer cell arithmetic, and the destination cell key
-// and row direction the rebin needs.  Four lanes share a cell; each lane's next particle is copied
-// into shared memory (cp.async) while the current one is pushed.  The TSC-weighted 3x3 gather of
+// and row direction the rebin needs.  Four lanes share a cell; each lane's next two particles are
+// copied into shared memory (cp.async) while the current one is pushed.  The TSC-weighted 3x3 gather of
 // each field is a biquadratic in the particle's offsets, so the kernel stages its nine
 // coefficients per cell and field and evaluates it by Horner's rule, two fields per packed
 // fma.rn.f32x2.  Each lane keeps the cell's 5x5x3 partial currents in registers (the cell's
 // particles all deposit on the same 5x5 nodes); the four lanes add theirs with shuffles, and the
 // tile's node currents are summed from the per-cell partials in a fixed order.  Tile currents go
 // to a per-tile buffer; k_mixed_jfold adds them into the FP64 global J node by node in a fixed
-// order, so the result is deterministic and no atomics touch the currents.
+// order, so the result is deterministic and no atomics touch the currents.  The rebin either
+// records the new cell order as a slot permutation that the next push reads through
+// (k_mixed_perm; the push then writes its particles out in cell order) or moves the particles into
+// it (k_mixed_move); both give the same state.
 #include <algorithm>
 
 #include "wm_launch.cuh"

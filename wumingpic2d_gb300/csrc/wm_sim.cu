@@ -10,6 +10,10 @@
 //   push A->B, deposit(A,B)->uj, field solve, then particle_x + particle_y + sort__bucket fused:
 //   classify B (wrap, direction, destination cell), particle_y slots, cell counts -> cumcnt,
 //   and one gather B->A into the new cell-sorted order.
+// Mixed path: FP32 particles (cell implicit, FP32 offsets and momenta); push + deposit fused,
+// FP64 fold, field solve; the new cell order is kept as a slot permutation that the next push
+// reads through (or, with WM_REBIN_MOVE, the particles are moved into it), materialize() writes
+// the cell-sorted state out for the calls that need it.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
