@@ -287,33 +287,16 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(*tslot), "r"(TC_GROUPS * TMEM_COLS) : "memory");
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder()
-{
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
-}
-
 template <int CIN, int NOUT, int COUT, int EPI>
 int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H, int W, void *out, void *zout, const void *zprev,
               unsigned *status, cudaStream_t st)
 {
     constexpr int KG = CIN / 8;
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tmap_encoder();
-    if (!enc) return WM_ERR_CUDA;
     CUtensorMap tmap;
-    const cuuint64_t gdim[4] = {(cuuint64_t)CIN, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)nimg};
-    const cuuint64_t gstride[3] = {(cuuint64_t)CIN * 2, (cuuint64_t)W * CIN * 2, (cuuint64_t)H * W * CIN * 2};
-    const cuuint32_t box[4] = {8, TC_HW, TC_TH + 2, 1}, estride[4] = {1, 1, 1, 1};
-    if (enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(in), gdim, gstride, box, estride, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-        return WM_ERR_BAD_ARG;
+    const unsigned long long gdim[4] = {(unsigned long long)CIN, (unsigned long long)W, (unsigned long long)H, (unsigned long long)nimg};
+    const unsigned long long gstride[3] = {(unsigned long long)CIN * 2, (unsigned long long)W * CIN * 2, (unsigned long long)H * W * CIN * 2};
+    const unsigned box[4] = {8, TC_HW, TC_TH + 2, 1};
+    WM_TRY(wm_tensor_map(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, in, gdim, gstride, box));
     const size_t smem = 16 * (size_t)(9 * KG * NOUT + TC_GROUPS * 2 * KG * TC_XP) + 8 * 3 * TC_GROUPS + 16;
     WM_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<CIN, NOUT, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long ntiles = (long long)nimg * (H / TC_TH) * (W / TC_TW);
@@ -328,6 +311,32 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
 }
 
 }  // namespace
+
+int wm_tensor_map(CUtensorMap *map, CUtensorMapDataType type, int rank, const void *base, const unsigned long long *dims,
+                  const unsigned long long *strides, const unsigned *box)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+    if (!enc) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            return WM_ERR_CUDA;
+        enc = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    cuuint64_t d[5], st[4];
+    cuuint32_t b[5], es[5];
+    for (int i = 0; i < rank; ++i) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        es[i] = 1;
+        if (i + 1 < rank) st[i] = strides[i];
+    }
+    return enc(map, type, (cuuint32_t)rank, const_cast<void *>(base), d, st, b, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+               ? WM_OK
+               : WM_ERR_BAD_ARG;
+}
 
 bool wm_cnn_tc_shape_ok(int nimg, int H, int W) { return nimg > 0 && H >= TC_TH && W >= TC_TW && H % TC_TH == 0 && W % TC_TW == 0; }
 

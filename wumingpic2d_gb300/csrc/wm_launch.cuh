@@ -1,5 +1,7 @@
 // wm_launch.cuh -- host launchers exported by the kernel translation units.
 #pragma once
+#include <cuda.h>  // CUtensorMap (TMA descriptors)
+
 #include "wm_internal.cuh"
 
 // wm_particles.cu
@@ -135,6 +137,10 @@ int wm_cnn_net_prepare(WmCnnNet &net, cudaStream_t st);
 int wm_cnn_infer_guess(const WmGeom &g, const WmCnnNet &net, FView<6, false> uf, FView<3, false> uj, const WmCnnWork &w, double *cand,
                        cudaStream_t st,
                        unsigned *status);
+// A tiled TMA descriptor (no interleave, no swizzle, zero fill out of bounds): dims and box
+// innermost first, strides in bytes of dims 1 .. rank-1.
+int wm_tensor_map(CUtensorMap *map, CUtensorMapDataType type, int rank, const void *base, const unsigned long long *dims,
+                  const unsigned long long *strides, const unsigned *box);
 // wm_cnn_tc.cu: the convolutions on tcgen05 (h a multiple of 16, w of 8): (cin, cout) = (16, 48) or
 // (48, 48) with mode WM_CNN_FWD_TRAIN / _INFER / _BWD (zprev), (48, 8) with WM_CNN_FWD_LINEAR; a
 // timed-out wait sets WMDEV_TIMEOUT in *status

@@ -6,8 +6,9 @@
 // does, for one (species, row, 32-cell tile): the Buneman-Boris push of particle.f90:96-161 in
 // FP32, the Esirkepov deposit of field.f90:224-298 in FP32, the periodic wrap of
 // boundary_periodic.f90:61-96 and :143-165 as integer cell arithmetic, and the destination cell key
-// and row direction the rebin needs.  Four lanes share a cell; each lane's next two particles are
-// copied into shared memory (cp.async) while the current one is pushed.  The TSC-weighted 3x3 gather of
+// and row direction the rebin needs.  The tile's cell-centred fields arrive as one TMA box; four
+// lanes share a cell; each lane's next two particles are copied into shared memory (cp.async)
+// while the current one is pushed.  The TSC-weighted 3x3 gather of
 // each field is a biquadratic in the particle's offsets, so the kernel stages its nine
 // coefficients per cell and field and evaluates it by Horner's rule, two fields per packed
 // fma.rn.f32x2.  Each lane keeps the cell's 5x5x3 partial currents in registers (the cell's
@@ -33,6 +34,7 @@ constexpr int MX_TW = MX_THREADS / MX_LPC;  // cells per tile (one row, one spec
 constexpr int MX_JW = MX_TW + 4;            // node columns a tile deposits on
 constexpr int MX_FS = 60;                   // floats per cell of staged stencil: 9 x 6 used; 60 keeps 128-bit reads conflict-free
 constexpr int MX_PW = MX_TW + 8;            // per-cell partial rows: 4 zero cells on each side
+constexpr int MX_FTW = MX_TW + 4;           // columns of the staged field tile: the 34 a tile uses, rounded to 16 bytes
 constexpr int MX_CB = 6;                    // bits of the tile cell in a move code: rank << 10 | cell << 4 | direction
 static_assert(MX_TW <= (1 << MX_CB), "a tile's cells fit the move code");
 constexpr unsigned FULL = 0xffffffffu;
@@ -122,20 +124,36 @@ __device__ __forceinline__ void store_particle(const MixedView &b, long long p, 
 }
 
 // Cell-centred fields (i+1/2, j+1/2) of particle.f90:68-81 for cells -1..nx and rows -1..ny,
-// averaged in FP64 and rounded once to FP32: fcc[m][(jy+1)*(nx+2) + ix+1].
-__global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__ fcc)
+// averaged in FP64 and rounded once to FP32: fcc[m][(jy+1)*pitch + ix+1], the row pitch a
+// multiple of 4 floats (16 bytes, for the push's TMA loads); the pad columns are never read.
+__global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__ fcc, int pitch)
 {
     const int W = g.nx + 2;
-    const long long n = (long long)W * (g.ny + 2);
+    const long long n = (long long)W * (g.ny + 2), plane = (long long)pitch * (g.ny + 2);
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
         const int ix = (int)(e % W) + 1, iy = (int)(e / W) + 1;  // ghosted index of cell ix-2, row iy-2
-        fcc[e] = (float)(0.5 * (uf(0, ix, iy) + uf(0, ix, iy + 1)));
-        fcc[n + e] = (float)(0.5 * (uf(1, ix, iy) + uf(1, ix + 1, iy)));
-        fcc[2 * n + e] = (float)(0.25 * (uf(2, ix, iy) + uf(2, ix + 1, iy) + uf(2, ix, iy + 1) + uf(2, ix + 1, iy + 1)));
-        fcc[3 * n + e] = (float)(0.5 * (uf(3, ix, iy) + uf(3, ix + 1, iy)));
-        fcc[4 * n + e] = (float)(0.5 * (uf(4, ix, iy) + uf(4, ix, iy + 1)));
-        fcc[5 * n + e] = (float)uf(5, ix, iy);
+        const long long o = (long long)(iy - 1) * pitch + ix - 1;
+        fcc[o] = (float)(0.5 * (uf(0, ix, iy) + uf(0, ix, iy + 1)));
+        fcc[plane + o] = (float)(0.5 * (uf(1, ix, iy) + uf(1, ix + 1, iy)));
+        fcc[2 * plane + o] = (float)(0.25 * (uf(2, ix, iy) + uf(2, ix + 1, iy) + uf(2, ix, iy + 1) + uf(2, ix + 1, iy + 1)));
+        fcc[3 * plane + o] = (float)(0.5 * (uf(3, ix, iy) + uf(3, ix + 1, iy)));
+        fcc[4 * plane + o] = (float)(0.5 * (uf(4, ix, iy) + uf(4, ix, iy + 1)));
+        fcc[5 * plane + o] = (float)uf(5, ix, iy);
     }
+}
+
+// bounded mbarrier wait (parity), as the TMA load of the push's field tile needs
+__device__ __forceinline__ bool mx_bar_wait(uint32_t bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < (1u << 22); ++i) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+                     : "=r"(done)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
 }
 
 // One CTA per (tile of 64 cells, row, species); 4 lanes per cell.  The loop body has no branches:
@@ -147,11 +165,12 @@ __global__ void k_mixed_fields(WmGeom g, FView<6, false> uf, float *__restrict__
 #endif
 // GATHER: the particle of cell-sorted slot p is at slot perm[p] of set a (the previous step's push
 // output, see k_mixed_perm); otherwise it is at slot p.  The push does not touch the ids.
+// fmap: TMA descriptor of the cell-centred fields (columns, rows, planes), boxes of MX_FTW x 3 x 6.
 template <int BC, bool GATHER>  // BC = WM_BC_*: the walls' code is compiled only where it runs
 __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
-    k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const unsigned *__restrict__ perm, const float *__restrict__ fcc,
-                         const int *__restrict__ cumcnt, unsigned *__restrict__ code, int *__restrict__ cnt9, float *__restrict__ jtile,
-                         unsigned *status)
+    k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const unsigned *__restrict__ perm,
+                         const __grid_constant__ CUtensorMap fmap, const int *__restrict__ cumcnt, unsigned *__restrict__ code,
+                         int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status)
 {
     __shared__ int dcnt[MX_TW][9];  // per cell: particles so far that move in direction d
     __shared__ __align__(16) float fcell[MX_TW][MX_FS];  // [cell][(b*3 + a)*6 + m]
@@ -160,22 +179,25 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     __shared__ float spc[5];
     __shared__ float pbuf[MX_NBUF][5][MX_THREADS];  // each lane's next particles, MX_PFD ahead
     __shared__ unsigned permring[GATHER ? MX_PR : 1][MX_THREADS];
-    float(*tmp)[3][MX_TW + 2] = reinterpret_cast<float(*)[3][MX_TW + 2]>(&cellpj[0][0]);
-    static_assert(6 * 3 * (MX_TW + 2) <= 65 * MX_PW, "node rows fit in the partials buffer");
+    __shared__ __align__(128) float tmp[6][3][MX_FTW];  // the tile's cell-centred fields (one TMA box)
+    __shared__ __align__(8) uint64_t fbar;
     const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
     const int row = isp * g.ny + jr;
     const int c0 = tile * MX_TW;
     const int ncell = min(MX_TW, g.nx - c0);
     const int tid = threadIdx.x;
 
-    // cell-centred fields of cells c0-1 .. c0+ncell, rows jr-1 .. jr+1
-    {
-        const int W = g.nx + 2, tw = ncell + 2;
-        const long long n = (long long)W * (g.ny + 2);
-        for (int e = tid; e < 18 * tw; e += MX_THREADS) {
-            const int aa = e % tw, mb = e / tw, bb = mb % 3, m = mb / 3;
-            tmp[m][bb][aa] = fcc[m * n + (long long)(jr + bb) * W + c0 + aa];
-        }
+    // cell-centred fields of cells c0-1 .. c0+MX_FTW-2, rows jr-1 .. jr+1: one TMA box (columns past
+    // the grid read as zero), completing on an mbarrier that every thread waits on below
+    const uint32_t fbar_a = (uint32_t)__cvta_generic_to_shared(&fbar);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(fbar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fbar_a), "r"((uint32_t)sizeof(tmp)) : "memory");
+        asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+                         (uint32_t)__cvta_generic_to_shared(&tmp[0][0][0])),
+                     "l"(reinterpret_cast<uint64_t>(&fmap)), "r"(c0), "r"(jr), "r"(0), "r"(fbar_a)
+                     : "memory");
     }
     const int *ccrow = cumcnt + (long long)(g.nx + 1) * row;
     for (int e = tid; e <= ncell; e += MX_THREADS) cc[e] = ccrow[c0 + e];
@@ -191,6 +213,7 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
             }
     }
     __syncthreads();
+    if (!mx_bar_wait(fbar_a, 0)) atomicOr(status, (unsigned)WMDEV_TIMEOUT);  // (the step then fails)
     // Each cell's six fields as biquadratics in the centred offsets hx, hy of particle.f90:96-129:
     // sum_ab T(a,b) sx_a(hx) sy_b(hy) = sum_pq C(q,p) hx^p hy^q, with the TSC weights
     // sx = (1/8 - hx/2 + hx^2/2, 3/4 - hx^2, 1/8 + hx/2 + hx^2/2).  Stored [(q*3 + p)*6 + m].
@@ -799,13 +822,14 @@ __global__ void __launch_bounds__(PACK_THREADS) k_mixed_pack(WmGeom g, MixedView
 
 int wm_mixed_ntiles(const WmGeom &g) { return (g.nx + MX_TW - 1) / MX_TW; }
 size_t wm_mixed_jtile_floats(const WmGeom &g) { return (size_t)g.nsp * g.ny * wm_mixed_ntiles(g) * 3 * 5 * MX_JW; }
-size_t wm_mixed_fcc_floats(const WmGeom &g) { return (size_t)6 * (g.nx + 2) * (g.ny + 2); }
+static int fcc_pitch(const WmGeom &g) { return (g.nx + 2 + 3) & ~3; }
+size_t wm_mixed_fcc_floats(const WmGeom &g) { return (size_t)6 * fcc_pitch(g) * (g.ny + 2); }
 
 int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cudaStream_t st)
 {
     const long long n = (long long)(g.nx + 2) * (g.ny + 2);
     const unsigned blocks = (unsigned)std::min<long long>((n + 255) / 256, 152LL * 16);
-    k_mixed_fields<<<blocks, 256, 0, st>>>(g, uf, fcc);
+    k_mixed_fields<<<blocks, 256, 0, st>>>(g, uf, fcc, fcc_pitch(g));
     return wm_check_launch("k_mixed_fields");
 }
 
@@ -834,7 +858,15 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
     }
     dim3 grid(wm_mixed_ntiles(g), g.ny, g.nsp);
     unsigned *code = reinterpret_cast<unsigned *>(sc.key);
-#define WM_MX_PUSH(BCV, GV) k_mixed_push_deposit<BCV, GV><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, perm, fcc, cumcnt, code, cnt9, jtile, sc.status)
+    CUtensorMap fmap;
+    {
+        const unsigned long long p = (unsigned long long)fcc_pitch(g);
+        const unsigned long long dims[3] = {(unsigned long long)g.nx + 2, (unsigned long long)g.ny + 2, 6};
+        const unsigned long long strides[2] = {4 * p, 4 * p * (g.ny + 2)};
+        const unsigned box[3] = {MX_FTW, 3, 6};
+        WM_TRY(wm_tensor_map(&fmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, fcc, dims, strides, box));
+    }
+#define WM_MX_PUSH(BCV, GV) k_mixed_push_deposit<BCV, GV><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, perm, fmap, cumcnt, code, cnt9, jtile, sc.status)
     if (g.bc == WM_BC_RECONNECTION) {
         if (perm) WM_MX_PUSH(WM_BC_RECONNECTION, true);
         else WM_MX_PUSH(WM_BC_RECONNECTION, false);
