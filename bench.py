@@ -477,6 +477,8 @@ def all_rooflines(res, args):
             gbs = b * res["ntot"] / (t / args.steps / 1e3) / 1e9
             out[name] = {"achieved": round(gbs, 1), "frac": round(gbs / peaks["hbm_gbs"], 4), "bytes_per_particle": b,
                          "ms_per_launch": round(t / args.steps, 3)}
+            if name == "sort_perm":  # on a low-priority stream beside the field solve: its event time includes the time it yields
+                out[name]["beside_field_solve"] = True
     return out
 
 

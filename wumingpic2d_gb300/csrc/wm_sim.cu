@@ -147,7 +147,11 @@ struct wm_sim {
     cudaEvent_t xev[XFER_CHUNKS + 1] = {};
     int xfer_setup()
     {
-        if (!st2) WM_CUDA(cudaStreamCreateWithFlags(&st2, cudaStreamNonBlocking));
+        if (!st2) {
+            int least = 0, greatest = 0;
+            WM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+            WM_CUDA(cudaStreamCreateWithPriority(&st2, cudaStreamNonBlocking, least));
+        }
         for (cudaEvent_t &e : xev)
             if (!e) WM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         return WM_OK;
@@ -170,6 +174,11 @@ struct wm_sim {
     bool timing = false;
     std::vector<Mark> marks;
     size_t nmarks = 0;
+    // the mixed step's rebin runs on a second stream beside the field solve: its events, and the
+    // timing marks recorded on that stream
+    cudaEvent_t rb_push_done = nullptr, rb_done = nullptr;
+    std::vector<Mark> smarks;
+    size_t nsmarks = 0;
     std::vector<const char *> t_names;
     std::vector<double> t_ms;
     long long launches = 0;
@@ -256,6 +265,18 @@ struct wm_sim {
         ++nmarks;
     }
     static void mark_cb(void *self, const char *name) { static_cast<wm_sim *>(self)->mark(name); }
+    void smark(const char *name)  // a timing mark on the rebin's stream
+    {
+        if (!timing) return;
+        if (nsmarks == smarks.size()) {
+            Mark m{name, nullptr};
+            cudaEventCreate(&m.ev);
+            smarks.push_back(m);
+        }
+        smarks[nsmarks].name = name;
+        cudaEventRecord(smarks[nsmarks].ev, st2);
+        ++nsmarks;
+    }
     // phase events of the host-buffer path (load and store), recorded only with timing on
     std::vector<Mark> phases;
     size_t nphases = 0;
@@ -354,6 +375,13 @@ struct wm_sim {
         guess_on = false;
         for (Mark &m : marks) cudaEventDestroy(m.ev);
         marks.clear();
+        for (Mark &m : smarks) cudaEventDestroy(m.ev);
+        smarks.clear();
+        for (cudaEvent_t *e : {&rb_push_done, &rb_done})
+            if (*e) {
+                cudaEventDestroy(*e);
+                *e = nullptr;
+            }
         for (Mark &m : phases) cudaEventDestroy(m.ev);
         phases.clear();
         if (scal_host) cudaFreeHost(scal_host);
@@ -470,15 +498,16 @@ struct wm_sim {
     // kernel; FP64 current fold, field solve and the same particle_y / sort permutation.
     // Injection, first half (after the new row counts exist): this step's counts per row and the
     // new row bases with room behind each row for them.  Without injection: the plain row bases.
-    int rowbases(WmRebinScratch &sc)
+    int rowbases(WmRebinScratch &sc) { return rowbases(sc, st); }
+    int rowbases(WmRebinScratch &sc, cudaStream_t s)
     {
-        if (!inject_on) return wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, st);
+        if (!inject_on) return wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, s);
         inj.it = (int)it;
         inj.cap = cap;
         WM_TRY(wm_launch_inject_counts(g, inj, sc.np2_new, inj_rows.as<int>(), inj_ninc.as<long long>(), inj_nptot.as<long long>(),
-                                       sc.status, st));
-        WM_TRY(wm_launch_inject_reserve(g, sc.np2_new, inj_rows.as<int>(), inj_tmp.as<int>(), st));
-        return wm_launch_rowbase(g.nrows, inj_tmp.as<int>(), sc.rowbase_new, st);
+                                       sc.status, s));
+        WM_TRY(wm_launch_inject_reserve(g, sc.np2_new, inj_rows.as<int>(), inj_tmp.as<int>(), s));
+        return wm_launch_rowbase(g.nrows, inj_tmp.as<int>(), sc.rowbase_new, s);
     }
     // second half (after the move): the new particles behind the sorted ones, np2 and cumcnt
     // advanced (proj/shock/app.f90:829-848), and the upstream field at the boundary columns
@@ -574,30 +603,43 @@ struct wm_sim {
                                             mx_cnt9.as<int>(), jtile.as<float>(), st));
         ++nl;
         mark("push_deposit");
+        // The rebin needs the push's counts and codes only: destination counts, scan, row bases and
+        // the permutations run on the second stream while this one folds the current and solves
+        // the fields (FP64-bound work beside memory-bound work); the next push waits for both.
+        WM_TRY(xfer_setup());
+        if (!rb_push_done) WM_CUDA(cudaEventCreateWithFlags(&rb_push_done, cudaEventDisableTiming));
+        if (!rb_done) WM_CUDA(cudaEventCreateWithFlags(&rb_done, cudaEventDisableTiming));
+        WM_CUDA(cudaEventRecord(rb_push_done, st));
+        WM_CUDA(cudaStreamWaitEvent(st2, rb_push_done, 0));
+        smark("start");
+        int rs = wm_launch_mixed_incoming(g, mx_cnt9.as<int>(), mx_off9.as<int>(), sc, st2);
+        if (rs == WM_OK) rs = wm_launch_scan_cells(g, sc, cumcnt_alt.as<int>(), sc.np2_new, st2);
+        if (rs == WM_OK) rs = rowbases(sc, st2);
+        smark("scan");
+        if (rs == WM_OK)
+            rs = wm_launch_mixed_perm(g, rowbase[cur].as<long long>(), sc.rowbase_new, cumcnt.as<int>(), cumcnt_alt.as<int>(), mx_off9.as<int>(),
+                                      sc, mx_perm.as<unsigned>(), gather ? mx_idperm[idp].as<unsigned>() : nullptr,
+                                      mx_idperm[1 - idp].as<unsigned>(), st2);
+        smark("sort_perm");
+        if (rs == WM_OK && inject_on)  // the new particles past the push output (positions in B, ids in A[5]), their slots in the permutations
+            rs = wm_launch_inject_particles(g, inj, mview(B, 1 - cur, 0), sc.np2_new, cumcnt_alt.as<int>(), inj_rows.as<int>(),
+                                            inj_ninc.as<long long>(), inj_nptot.as<long long>(), st2, mx_perm.as<unsigned>(),
+                                            mx_idperm[1 - idp].as<unsigned>(), rowbase[cur].as<long long>() + g.nrows);
+        WM_CUDA(cudaEventRecord(rb_done, st2));
+        nl += (inject_on ? 7 : 4);
         WM_TRY(wm_launch_mixed_jfold(g, jtile.as<float>(), uj(), st));
         ++nl;
         mark("deposit");
         WmFieldWork w = work();
         const int s = wm_field_solve(g, k, uf(), uj(), df(), w, iters, 4, st, timing ? &wm_sim::mark_cb : nullptr, this, &nl, guess());
+        WM_CUDA(cudaStreamWaitEvent(st, rb_done, 0));  // (also when the solve failed: no work of this step left in flight)
         if (s != WM_OK) return s;
-        WM_TRY(wm_launch_mixed_incoming(g, mx_cnt9.as<int>(), mx_off9.as<int>(), sc, st));
-        WM_TRY(wm_launch_scan_cells(g, sc, cumcnt_alt.as<int>(), sc.np2_new, st));
-        WM_TRY(rowbases(sc));
-        nl += inject_on ? 5 : 3;
-        mark("scan");
-        WM_TRY(wm_launch_mixed_perm(g, rowbase[cur].as<long long>(), sc.rowbase_new, cumcnt.as<int>(), cumcnt_alt.as<int>(), mx_off9.as<int>(),
-                                    sc, mx_perm.as<unsigned>(), gather ? mx_idperm[idp].as<unsigned>() : nullptr,
-                                    mx_idperm[1 - idp].as<unsigned>(), st));
-        ++nl;
-        mark("sort_perm");
-        if (inject_on) {  // the new particles past the push output (positions in B, ids in A[5]), their slots in the permutations
-            WM_TRY(wm_launch_inject_particles(g, inj, mview(B, 1 - cur, 0), sc.np2_new, cumcnt_alt.as<int>(), inj_rows.as<int>(),
-                                              inj_ninc.as<long long>(), inj_nptot.as<long long>(), st, mx_perm.as<unsigned>(),
-                                              mx_idperm[1 - idp].as<unsigned>(), rowbase[cur].as<long long>() + g.nrows));
+        WM_TRY(rs);
+        if (inject_on) {  // the upstream field at the boundary columns, after the solve's field update
             WM_TRY(wm_launch_inject_fields(g, inj, uf(), st));
-            nl += 3;
-            mark("inject");
+            ++nl;
         }
+        mark("rebin_wait");
         // set B now holds the pushed particles in the old cell order: it becomes set A (the ids
         // stay in A[5], reached through the new idperm)
         for (int c = 0; c < 5; ++c) std::swap(A[c], B[c]);
@@ -699,7 +741,11 @@ int wm_sim_create(const wm_sim_config *cfg, wm_sim **out)
     k.cg_itemax = cfg->cg_itemax;
     s->precision = cfg->precision;
     s->cap_req = cfg->capacity;
-    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess ||
+    // the main stream at the highest priority: the mixed step's rebin runs beside the field solve on
+    // a second stream of the lowest, so the solve's blocks are scheduled first
+    int prio_least = 0, prio_greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+    if (cudaStreamCreateWithPriority(&s->st, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
         cudaMallocHost((void **)&s->scal_host, wm_field_scal_bytes()) != cudaSuccess ||
         cudaMallocHost((void **)&s->status_host, sizeof(unsigned)) != cudaSuccess) {
         s->release();
@@ -980,10 +1026,26 @@ int wm_sim_step(wm_sim *s, int nsteps)
 {
     if (!s || !s->loaded) return WM_ERR_NOT_INIT;
     s->nmarks = 0;
+    s->nsmarks = 0;
     s->launches = 0;
     s->t_names.clear();
     s->t_ms.clear();
     for (int i = 0; i < nsteps; ++i) WM_TRY(s->step_once());
+    if (s->timing && s->nsmarks > 1) {  // the rebin's kernels on the second stream (beside the field solve)
+        WM_CUDA(cudaStreamSynchronize(s->st));
+        for (size_t m = 1; m < s->nsmarks; ++m) {
+            if (std::strcmp(s->smarks[m].name, "start") == 0) continue;
+            float ms = 0.f;
+            WM_CUDA(cudaEventElapsedTime(&ms, s->smarks[m - 1].ev, s->smarks[m].ev));
+            size_t idx = 0;
+            while (idx < s->t_names.size() && std::strcmp(s->t_names[idx], s->smarks[m].name) != 0) ++idx;
+            if (idx == s->t_names.size()) {
+                s->t_names.push_back(s->smarks[m].name);
+                s->t_ms.push_back(0.0);
+            }
+            s->t_ms[idx] += ms;
+        }
+    }
     if (s->timing && s->nmarks > 1) {
         WM_CUDA(cudaStreamSynchronize(s->st));
         for (size_t m = 1; m < s->nmarks; ++m) {
