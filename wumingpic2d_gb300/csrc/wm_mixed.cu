@@ -426,25 +426,47 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
             cy[m] *= mq;
         }
         const float qh = 0.5f * qg, q3 = (1.f / 3.f) * qg;
+        float wy[5], z1[5], z2[5];
 #pragma unroll
         for (int jp = 0; jp < 5; ++jp) {
             const bool inner = jp >= 1 && jp <= 3;
-            const float wy = inner ? s0y[jp] + 0.5f * dsy[jp] : 0.5f * dsy[jp];
+            wy[jp] = inner ? s0y[jp] + 0.5f * dsy[jp] : 0.5f * dsy[jp];
+            z1[jp] = qg * wy[jp];
+            z2[jp] = inner ? fmaf(qh, s0y[jp], q3 * dsy[jp]) : q3 * dsy[jp];
+        }
+        // the accumulators in pairs, one packed FMA per pair (each element's FMAs in the same order)
+        auto acc2 = [](float &lo, float &hi, unsigned long long m1, unsigned long long m2) {
+            unpack2(fma2(m1, m2, pack2(lo, hi)), lo, hi);
+        };
+        const unsigned long long cx01 = pack2(cx[0], cx[1]), cx23 = pack2(cx[2], cx[3]);
+        const unsigned long long cy01 = pack2(cy[0], cy[1]), cy23 = pack2(cy[2], cy[3]);
 #pragma unroll
-            for (int m = 0; m < 4; ++m) ax[jp][m] = fmaf(wy, cx[m], ax[jp][m]);
-            const float z1 = qg * wy;
-            const float z2 = inner ? fmaf(qh, s0y[jp], q3 * dsy[jp]) : q3 * dsy[jp];
-#pragma unroll
-            for (int ip = 0; ip < 5; ++ip) {
-                az[jp][ip] = fmaf(dsx[ip], z2, az[jp][ip]);
-                if (ip >= 1 && ip <= 3) az[jp][ip] = fmaf(s0x[ip], z1, az[jp][ip]);
-            }
+        for (int jp = 0; jp < 5; ++jp) {
+            const unsigned long long w2 = pack2(wy[jp], wy[jp]);
+            acc2(ax[jp][0], ax[jp][1], w2, cx01);
+            acc2(ax[jp][2], ax[jp][3], w2, cx23);
         }
 #pragma unroll
         for (int ip = 0; ip < 5; ++ip) {
             const float fx = (ip >= 1 && ip <= 3) ? s0x[ip] + 0.5f * dsx[ip] : 0.5f * dsx[ip];
+            const unsigned long long f2 = pack2(fx, fx);
+            acc2(ay[0][ip], ay[1][ip], f2, cy01);
+            acc2(ay[2][ip], ay[3][ip], f2, cy23);
+        }
+        const unsigned long long z2a = pack2(z2[0], z2[1]), z2b = pack2(z2[2], z2[3]);
+        const unsigned long long z1a = pack2(z1[0], z1[1]), z1b = pack2(z1[2], z1[3]);
 #pragma unroll
-            for (int m = 0; m < 4; ++m) ay[m][ip] = fmaf(fx, cy[m], ay[m][ip]);
+        for (int ip = 0; ip < 5; ++ip) {
+            const unsigned long long d2 = pack2(dsx[ip], dsx[ip]);
+            acc2(az[0][ip], az[1][ip], d2, z2a);
+            acc2(az[2][ip], az[3][ip], d2, z2b);
+            az[4][ip] = fmaf(dsx[ip], z2[4], az[4][ip]);
+            if (ip >= 1 && ip <= 3) {
+                const unsigned long long s2 = pack2(s0x[ip], s0x[ip]);
+                acc2(az[0][ip], az[1][ip], s2, z1a);
+                acc2(az[2][ip], az[3][ip], s2, z1b);
+                az[4][ip] = fmaf(s0x[ip], z1[4], az[4][ip]);
+            }
         }
         if constexpr (BC == WM_BC_RECONNECTION) {  // particle_x after the field solve (boundary_reconnection.f90:80-91)
             int cn = cg + incx;
