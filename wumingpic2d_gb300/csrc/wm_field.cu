@@ -23,6 +23,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int CG_THREADS = 256;
+constexpr int CG_BLOCKS = 152 * 4;  // one wave: 4 CTAs of 256 threads on each of the 152 SMs
 
 // ------------------------------------------------------------ ghost patterns
 template <class FV>
@@ -408,52 +409,28 @@ __global__ void k_guess_pick(WmGeom g, FV6 df, const double *__restrict__ cand, 
     }
 }
 
-// ap = A p and p.ap (:395-415).
-__global__ void __launch_bounds__(CG_THREADS) k_cg_ap(WmGeom g, FieldK fk, const double *__restrict__ p, double *__restrict__ ap,
-                                                      double *partial, unsigned *ticket, CgScal *scal)
-{
-    const long long ncell = (long long)g.nx * g.ny;
-    const bool act[3] = {scal[0].active != 0, scal[1].active != 0, scal[2].active != 0};
-    if (!act[0] && !act[1] && !act[2]) return;  // uniform across the grid: no CTA takes a ticket
-    double acc[3] = {0.0, 0.0, 0.0};
-    for (GridCell q(g.nx); q.e < ncell; q.next()) {
-        const long long e = q.e;
-        const int ci = q.c, cj = q.r;
-        const long long row = (long long)cj * g.nx;
-        const long long es = (long long)wrapm(cj - 1, g.ny) * g.nx + ci, en = (long long)wrapm(cj + 1, g.ny) * g.nx + ci;
-#pragma unroll
-        for (int l = 0; l < 3; ++l) {
-            if (!act[l]) continue;
-            const double *pl = p + l * ncell;
-            const double pc = pl[e];
-            double xl, xr;
-            x_neighbours(g, l, ci, [&](int c) { return pl[row + c]; }, xl, xr);
-            const double a = -pl[es] - xl + fk.f4 * pc - xr - pl[en];
-            ap[l * ncell + e] = a;
-            acc[l] += pc * a;
-        }
-    }
-    double tot[3];
-    if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot)) {
-        for (int l = 0; l < 3; ++l)
-            if (act[l]) {
-                scal[l].sum2 = tot[l];
-                scal[l].av = scal[l].sumr / tot[l];
-                scal[l].ite += 1;
-            }
-    }
-}
-
-// phi += av p, r -= av ap, ||r||^2; then the lagged stop test and beta (:417-443).
+// One launch of the CG iterations (field.f90:395-450), the three components staggered: component
+// l runs phase (t - l) mod 3 of its iteration at launch t (it starts at launch l), so that each
+// launch mixes one component's FP64-bound stencil with the other two's HBM-bound updates.
+//   phase 0 (:395-415): ap = A p and p.ap, then av = sumr / p.ap;
+//   phase 1 (:417-443): phi += av p, r -= av ap, ||r||^2, the lagged stop test and bv;
+//   phase 2 (:444-450): p = r + bv p.
+// A component that stopped in phase 1 skips the rest.  Per component the arithmetic, its order
+// and the reduction tree (fixed grid, fixed per-thread cells) do not depend on the staggering.
 template <class FV6>
-__global__ void __launch_bounds__(CG_THREADS) k_cg_update(WmGeom g, FieldK fk, FV6 df, const double *__restrict__ p,
-                                                          double *__restrict__ r, const double *__restrict__ ap, double *partial,
-                                                          unsigned *ticket, CgScal *scal)
+__global__ void __launch_bounds__(CG_THREADS, CG_BLOCKS / 152) k_cg_phase(WmGeom g, FieldK fk, FV6 df, double *__restrict__ p, double *__restrict__ r,
+                                                         double *__restrict__ ap, double *partial, unsigned *ticket, CgScal *scal, int t)
 {
     const long long ncell = (long long)g.nx * g.ny;
-    const bool act[3] = {scal[0].active != 0, scal[1].active != 0, scal[2].active != 0};
-    if (!act[0] && !act[1] && !act[2]) return;
-    const double av[3] = {scal[0].av, scal[1].av, scal[2].av};
+    int ph[3];
+    bool act[3];
+#pragma unroll
+    for (int l = 0; l < 3; ++l) {
+        ph[l] = t >= l ? (t - l) % 3 : -1;
+        act[l] = ph[l] >= 0 && scal[l].active != 0;
+    }
+    if (!act[0] && !act[1] && !act[2]) return;  // uniform across the grid: no CTA takes a ticket
+    const double av[3] = {scal[0].av, scal[1].av, scal[2].av}, bv[3] = {scal[0].bv, scal[1].bv, scal[2].bv};
     double acc[3] = {0.0, 0.0, 0.0};
     for (GridCell q(g.nx); q.e < ncell; q.next()) {
         const long long e = q.e;
@@ -461,43 +438,51 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_update(WmGeom g, FieldK fk, F
 #pragma unroll
         for (int l = 0; l < 3; ++l) {
             if (!act[l]) continue;
-            df(l, ci + 2, cj + 2) = df(l, ci + 2, cj + 2) + av[l] * p[l * ncell + e];
-            const double rv = r[l * ncell + e] - av[l] * ap[l * ncell + e];
-            r[l * ncell + e] = rv;
-            acc[l] += rv * rv;
+            const long long o = l * ncell + e;
+            if (ph[l] == 0) {
+                const double *pl = p + l * ncell;
+                const long long row = (long long)cj * g.nx;
+                const long long es = (long long)wrapm(cj - 1, g.ny) * g.nx + ci, en = (long long)wrapm(cj + 1, g.ny) * g.nx + ci;
+                const double pc = pl[e];
+                double xl, xr;
+                x_neighbours(g, l, ci, [&](int c) { return pl[row + c]; }, xl, xr);
+                const double a = -pl[es] - xl + fk.f4 * pc - xr - pl[en];
+                ap[o] = a;
+                acc[l] += pc * a;
+            } else if (ph[l] == 1) {
+                df(l, ci + 2, cj + 2) = df(l, ci + 2, cj + 2) + av[l] * p[o];
+                const double rv = r[o] - av[l] * ap[o];
+                r[o] = rv;
+                acc[l] += rv * rv;
+            } else {
+                p[o] = r[o] + bv[l] * p[o];
+            }
         }
     }
-    double tot[3];
-    if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot)) {
-        for (int l = 0; l < 3; ++l)
-            if (act[l]) {
+    if ((act[0] && ph[0] < 2) || (act[1] && ph[1] < 2) || (act[2] && ph[2] < 2)) {
+        double tot[3];
+        if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot)) {
+            for (int l = 0; l < 3; ++l) {
+                if (!act[l]) continue;
                 CgScal &s = scal[l];
-                s.sum1 = tot[l];
-                s.sum_g = sqrt(s.sumr);
-                if (s.ite >= fk.itemax) {
-                    s.status = WM_ERR_CG_MAXITER;
-                    s.active = 0;
-                } else {
-                    s.bv = tot[l] / s.sumr;
-                    s.sumr = tot[l];
-                    s.active = (s.sum_g > s.eps);
+                if (ph[l] == 0) {
+                    s.sum2 = tot[l];
+                    s.av = s.sumr / tot[l];
+                    s.ite += 1;
+                } else if (ph[l] == 1) {
+                    s.sum1 = tot[l];
+                    s.sum_g = sqrt(s.sumr);
+                    if (s.ite >= fk.itemax) {
+                        s.status = WM_ERR_CG_MAXITER;
+                        s.active = 0;
+                    } else {
+                        s.bv = tot[l] / s.sumr;
+                        s.sumr = tot[l];
+                        s.active = (s.sum_g > s.eps);
+                    }
                 }
             }
-    }
-}
-
-// p = r + bv p (:444-450) for components that keep iterating.
-__global__ void __launch_bounds__(CG_THREADS) k_cg_pupdate(WmGeom g, const double *__restrict__ r, double *__restrict__ p,
-                                                           const CgScal *scal)
-{
-    const long long ncell = (long long)g.nx * g.ny;
-    const bool act[3] = {scal[0].active != 0, scal[1].active != 0, scal[2].active != 0};
-    if (!act[0] && !act[1] && !act[2]) return;
-    const double bv[3] = {scal[0].bv, scal[1].bv, scal[2].bv};
-    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ncell; e += (long long)gridDim.x * blockDim.x) {
-#pragma unroll
-        for (int l = 0; l < 3; ++l)
-            if (act[l]) p[l * ncell + e] = r[l * ncell + e] + bv[l] * p[l * ncell + e];
+        }
     }
 }
 
@@ -613,7 +598,6 @@ int wm_launch_soa_to_aos(int nc, long long npts, const double *s, double *a, cud
 }
 
 // --------------------------------------------------------------- field solve
-constexpr int CG_BLOCKS = 152 * 4;
 int wm_field_cg_blocks() { return CG_BLOCKS; }
 size_t wm_field_scal_bytes() { return sizeof(CgScal) * 3; }
 
@@ -666,20 +650,19 @@ int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<
     WM_TRY(wm_check_launch("k_cg_resid"));
     nl += 2;
     M("cg_setup");
-    int done_iters = 0;
-    for (;;) {
+    // cg_batch iterations (3 launches each) between host checks of the "still iterating" flags;
+    // launch t runs phase (t - l) mod 3 of component l
+    const int t_max = 3 * (fk.itemax + 1) + 2;
+    for (int t = 0;;) {
         WM_CUDA(cudaMemcpyAsync(w.scal_host, w.scal, sizeof(CgScal) * 3, cudaMemcpyDeviceToHost, st));
         WM_CUDA(cudaStreamSynchronize(st));
         const bool any = w.scal_host[0].active || w.scal_host[1].active || w.scal_host[2].active;
-        if (!any || done_iters >= fk.itemax + 1) break;
-        for (int b = 0; b < cg_batch; ++b) {
-            k_cg_ap<<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, w.p, w.ap, w.partial, w.ticket, w.scal);
-            k_cg_update<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.p, w.r, w.ap, w.partial, w.ticket, w.scal);
-            k_cg_pupdate<<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, w.r, w.p, w.scal);
-            nl += 3;
+        if (!any || t >= t_max) break;
+        for (int b = 0; b < 3 * cg_batch; ++b, ++t) {
+            k_cg_phase<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.p, w.r, w.ap, w.partial, w.ticket, w.scal, t);
+            ++nl;
         }
         WM_TRY(wm_check_launch("cg iteration"));
-        done_iters += cg_batch;
     }
     M("cg_iterate");
     int status = WM_OK;
