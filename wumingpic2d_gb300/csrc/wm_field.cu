@@ -417,8 +417,10 @@ __global__ void k_guess_pick(WmGeom g, FV6 df, const double *__restrict__ cand, 
 //   phase 2 (:444-450): p = r + bv p.
 // A component that stopped in phase 1 skips the rest.  Per component the arithmetic, its order
 // and the reduction tree (fixed grid, fixed per-thread cells) do not depend on the staggering.
+// Registers are bounded for one CTA per SM more than the grid places, so that the mixed step's
+// rebin kernels, which run on a second stream beside the field solve, find room on every SM.
 template <class FV6>
-__global__ void __launch_bounds__(CG_THREADS, CG_BLOCKS / 152) k_cg_phase(WmGeom g, FieldK fk, FV6 df, double *__restrict__ p, double *__restrict__ r,
+__global__ void __launch_bounds__(CG_THREADS, CG_BLOCKS / 152 + 1) k_cg_phase(WmGeom g, FieldK fk, FV6 df, double *__restrict__ p, double *__restrict__ r,
                                                          double *__restrict__ ap, double *partial, unsigned *ticket, CgScal *scal, int t)
 {
     const long long ncell = (long long)g.nx * g.ny;
