@@ -201,6 +201,23 @@ def ncu_traffic():
 
 
 # ------------------------------------------------------------------ CPU baseline
+def cpu_cores():
+    """Host cores this process may run on (its affinity mask, which the container sets) and the
+    cores the host has online."""
+    try:
+        allowed = len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        allowed = os.cpu_count() or 1
+    online = None
+    try:
+        with open("/sys/devices/system/cpu/online") as f:
+            online = sum(int(b) - int(a) + 1 for a, _, b in (r.partition("-") if "-" in r else (r, "-", r)
+                                                             for r in f.read().strip().split(",")))
+    except (OSError, ValueError):
+        pass
+    return {"allowed": allowed, "host_online": online}
+
+
 def cpu_sample(args, steps: int):
     """The CPU restatement (OpenMP, every host core) on a strip of the workload."""
     from oracle import init as I
@@ -209,7 +226,7 @@ def cpu_sample(args, steps: int):
 
     cfg = WeibelConfig(nx=args.nx, ny=args.cpu_rows, ppc=args.ppc, seed=args.seed + 7, slack=1.2)
     d = cfg.dims()
-    threads = os.cpu_count() or 1
+    threads = cpu_cores()["allowed"]
     O.set_threads(threads)
     par = O.make_par(d, cfg.delt, cfg.charge, cfg.mass)
     up0, _, np2 = I.weibel(d, cfg.ppc, cfg.v_drift, cfg.vth_e, cfg.vth_i, cfg.seed)  # the GPU generator's state
@@ -442,25 +459,47 @@ def run_gpu(args, dist: Dist, precision: str, state, do_e2e: bool):
 # components and the i64 id (60 B).
 # FP64 operations per particle of the FP64 path's compute-bound kernels, counted from the
 # reference's code (particle.f90:96-161: ~215 plus 2 square roots and 3 divisions; field.f90:224-298:
-# ~570 plus a square root and a division); GB300's FP64 rate is 1.25 TFLOP/s nominal.
+# ~570 plus a square root and a division).  The denominator is GB300's FP64 rate as measured by
+# wm_fp64_fma_rate (independent FP64 FMA chains on whole waves of the SMs, CUDA events); the
+# nominal 1.25 TFLOP/s only where that measurement is unavailable.
 FP64_FLOP = {"push": 215, "deposit": 570}
-FP64_PEAK_TFLOPS = 1.25
+FP64_NOMINAL_TFLOPS = 1.25
 
 
-def fp64_rooflines(res, args):
+def fp64_peak():
+    import ctypes
+
+    from wumingpic2d_gb300._native import check, lib
+
+    tf, ms = ctypes.c_double(), ctypes.c_double()
+    try:
+        check(lib().wm_fp64_fma_rate(ctypes.byref(tf), ctypes.byref(ms)), "wm_fp64_fma_rate")
+    except Exception as exc:  # noqa: BLE001 -- reported, the nominal rate is used instead
+        return FP64_NOMINAL_TFLOPS, f"nominal (measurement failed: {exc})"
+    return tf.value, f"measured: k_fp64_fma (independent FP64 FMA chains, whole SM waves), {ms.value:.1f} ms, CUDA events"
+
+
+def fp64_rooflines(res, args, peak):
+    tflops, src = peak
     out = {}
     for name, f in FP64_FLOP.items():
         t = res["ktimes"].get(name)
         if t:
             tf = f * res["ntot"] / (t / args.steps / 1e3) / 1e12
-            out[name] = {"flop_per_particle": f, "achieved_tflops": round(tf, 3), "frac": round(tf / FP64_PEAK_TFLOPS, 3)}
-    out["peak"] = {"tflops": FP64_PEAK_TFLOPS, "source": "nominal FP64 rate (MEASURED_PEAKS.json has no FP64 figure)"}
+            out[name] = {"flop_per_particle": f, "achieved_tflops": round(tf, 3), "frac": round(tf / tflops, 3)}
+    out["peak"] = {"tflops": round(tflops, 4), "source": src, "nominal_tflops": FP64_NOMINAL_TFLOPS}
     return out
 
 
 ALGO_BYTES = {"fp64": {"push": 80, "deposit": 56, "sort_move": 96},
               "mixed": {"push_deposit": 48, "sort_perm": 16},
               "mixed_move": {"push_deposit": 44, "sort_move": 60}}
+# The path's own algorithmic bytes per particle, independent of this design: the push reads and
+# writes x, y, u (FP64 80 B; mixed: two FP32 offsets and three FP32 momenta, 40 B), the deposit
+# reads old x, y and new x, y, u (56 B; mixed 28 B, which the fused kernel takes from registers).
+# ALGO_BYTES above adds what this design moves on top (the permutation entry, the move code).
+PATH_BYTES = {"fp64": {"push": 80, "deposit": 56, "sort_move": 96},
+              "mixed": {"push_deposit": 40}, "mixed_move": {"push_deposit": 40}}
 
 
 def prec_key(res, args):
@@ -493,11 +532,15 @@ def roofline(res, args, name=None):
         return None
     name = name or max(cand, key=cand.get)
     t = cand[name] / steps / 1e3
-    achieved = algo[name] * ntot / t / 1e9
+    path_b = PATH_BYTES[prec_key(res, args)].get(name, algo[name])
+    achieved = path_b * ntot / t / 1e9
+    design = algo[name] * ntot / t / 1e9
     tr = ncu_traffic().get(f"{prec_key(res, args)}:{name}")
     return {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
             "frac": round(achieved / peaks["hbm_gbs"], 4), "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": (tr * ntot if tr else None), "bytes_per_particle_algorithmic": algo[name],
+            "traffic": (tr * ntot if tr else None), "bytes_per_particle_algorithmic": path_b,
+            "bytes_per_particle_design": algo[name], "achieved_at_design_bytes": round(design, 1),
+            "frac_at_design_bytes": round(design / peaks["hbm_gbs"], 4),
             "ms_per_launch": round(t * 1e3, 3)}
 
 
@@ -516,6 +559,7 @@ def main():
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
                 "config": {"workload": workload, "nx": args.nx, "ny": args.ny, "ppc": args.ppc},
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+                                 "host_online": cpu_cores()["host_online"],
                                  "note": "C restatement of the reference step (no Fortran compiler on this machine)"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
@@ -531,7 +575,9 @@ def main():
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
         v, cores, sample = cpu_sample(args, args.cpu_steps)
-        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+               "core_note": "cores = OpenMP threads = the cores in this process's affinity mask (host_online: all the host has)",
+               "host_online": cpu_cores()["host_online"]}
     if dist.rank == 0:
         d = res["d"]
         kt = res["ktimes"]
@@ -571,7 +617,7 @@ def main():
                                  "speedup_of_mixed": res["value"] / other["value"],
                                  "cg_iters_last_step": other["iters"],
                                  "kernel_ms_per_step": {k: round(v / args.steps, 3) for k, v in other["ktimes"].items()},
-                                 "roofline": roofline(other, args), "roofline_fp64": fp64_rooflines(other, args),
+                                 "roofline": roofline(other, args), "roofline_fp64": fp64_rooflines(other, args, fp64_peak()),
                                  "gpu_launches": other["launches"],
                                  "clocks": other["clocks"]}
         print(json.dumps(line), flush=True)

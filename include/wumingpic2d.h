@@ -298,12 +298,20 @@ int wm_sim_set_work(wm_sim *s, const double *df);
  * fixed static device array inside this library, so it allocates nothing: at most 65536 interior
  * cells (nx*ny; more returns WM_ERR_BAD_ARG), 39.3 MB of device memory held by every GPU that
  * loads the library until exit.  All calls share that scratch, so calls that overlap on the GPU
- * race; the first call on a device looks the scratch up (cudaGetSymbolAddress) and should come
- * before any stream capture.  stream: a cudaStream_t, or NULL for the default stream; the call
- * returns after the work on it has finished. */
+ * race.  The first call on a device looks the scratch up (cudaGetSymbolAddress); under CUDA's
+ * default lazy module loading that first call is also when the array is placed in device memory,
+ * which is an allocation: make it at start-up, before any stream capture begins, so that the
+ * memory is committed then and later calls allocate nothing.  stream: a cudaStream_t, or NULL for
+ * the default stream.  The call is synchronous: it reads a status word back and waits for the
+ * stream, then returns WM_OK, or WM_ERR_CELL if a particle moved more than one cell. */
 int wm_deposit_current_noalloc(const double *up, const double *gp, const int *cumcnt, double *uj, int ndim, int np, int nsp,
                                int nxgs, int nxge, int nygs, int nyge, double delx, double delt, double c, const double *q,
                                void *stream);
+
+/* No counterpart in the reference: the measured FP64 rate of this GPU (TFLOP/s), from CUDA events
+ * around a kernel of independent FP64 fused multiply-add chains on whole waves of the SMs; the
+ * denominator of the FP64 path's roofline.  ms (may be NULL) receives the kernel's time. */
+int wm_fp64_fma_rate(double *tflops, double *ms);
 
 /* Page-lock (pin) a host buffer so that copies from and to it run at full link speed. */
 int wm_host_register(void *ptr, size_t bytes);

@@ -21,7 +21,9 @@ HERE = Path(__file__).resolve().parent
 REF_DIR = HERE / "_ref"
 GEN_C = REF_DIR / "wuming_ref.c"
 LIB = REF_DIR / "libref.so"
-DEFAULT_SOURCE = Path(os.environ.get("WM_REFERENCE_COMMON", "/root/reference/common"))
+# The reference checkout's common/ directory: $WM_REFERENCE_COMMON, else a checkout named
+# "reference" beside this repository.
+DEFAULT_SOURCE = Path(os.environ.get("WM_REFERENCE_COMMON", str(HERE.parent.parent / "reference" / "common")))
 
 
 def generate(source: Path = DEFAULT_SOURCE) -> bool:

@@ -2,8 +2,9 @@
 
 The reference's common/ modules are translated to C (oracle/f90c.py), compiled with the
 single-rank glue and run on a small seeded Weibel state; inputs and outputs are saved to
-golden_weibel_16x12.npz.  Needs the reference source tree (WM_REFERENCE_COMMON, default
-/root/reference/common); the committed .npz is what the tests read.
+golden_weibel_16x12.npz.  Needs the reference source tree (WM_REFERENCE_COMMON, default: the
+common/ directory of a checkout named "reference" beside this repository); the committed .npz is
+what the tests read.
 
     python tests/golden/make_golden.py
 """

@@ -2,9 +2,11 @@
 CPU network (oracle/cnn_ref.py, which emulates the same BF16 roundings), training on pairs the
 FP64 solver produced, and the iteration count it saves inside the resident step.
 
-Stated bounds (normwise relative): forward output 2e-2, stored activations 2e-2, parameter
-gradients 5e-2 per layer.  The differences come from FP32 accumulation order against exact sums,
-which moves a few BF16 roundings by one unit.
+Stated bounds (normwise relative): forward output, stored activations and pre-activations 5e-3,
+parameter gradients 3e-3 per layer, loss 1e-3; tcgen05 against mma.sync and exact sums 5e-3.  The
+differences come from FP32 accumulation order against exact sums, which moves a few BF16 roundings
+by one unit (2^-8 = 3.9e-3 of an element at most); a wrong descriptor, tap or epilogue gives errors
+of order one.
 """
 import numpy as np
 import pytest
@@ -51,7 +53,7 @@ def test_forward_matches_oracle(gpu, grouped):
     e_act = max(rel_err(a.float().cpu().numpy(), r) for a, r in zip(acts[1:], racts[1:]))
     e_z = max(rel_err(z.float().cpu().numpy(), r) for z, r in zip(zs, rzs))
     print(f"\nforward vs oracle: infer {e_inf:.2e} train {e_tr:.2e} activations {e_act:.2e} pre-activations {e_z:.2e}")
-    assert e_inf <= 2e-2 and e_tr <= 2e-2 and e_act <= 2e-2 and e_z <= 2e-2
+    assert e_inf <= 5e-3 and e_tr <= 5e-3 and e_act <= 5e-3 and e_z <= 5e-3
     assert np.array_equal(pred_i.cpu().numpy(), pred_t.cpu().numpy())  # same arithmetic in both modes
     assert not pred_i.cpu().numpy()[..., 3:].any()  # padded outputs stay zero
 
@@ -77,9 +79,9 @@ def test_gradients_match_oracle(gpu, grouped):
         errs.append((rel_err(dw, rdw), rel_err(db[:rdb.size], rdb)))
     print("\ngradients vs oracle (dW, db) per layer: " + ", ".join(f"({a:.1e}, {b:.1e})" for a, b in errs)
           + f"; loss {float(loss.item()):.6e} vs {rloss:.6e}")
-    assert abs(float(loss.item()) - rloss) <= 1e-2 * rloss
+    assert abs(float(loss.item()) - rloss) <= 1e-3 * rloss
     for a, b in errs:
-        assert a <= 5e-2 and b <= 5e-2
+        assert a <= 3e-3 and b <= 3e-3
 
 
 def _weibel_sim(seed, nx=128, ny=128, ppc=16, cg_err=1e-6):
@@ -154,7 +156,7 @@ def test_learned_guess_saves_cg_iterations(gpu, trained, cg_err):
 def test_tensor_core_conv_matches_mma_sync_and_exact_sums(gpu, cin, grouped, train, shape):
     """The forward convolutions with 48 outputs run on tcgen05 (accumulators in tensor memory).
     Against the warp-level mma.sync kernel on the same BF16 operands, and against exact float64
-    sums of those operands: the BF16 outputs agree to 1e-2 normwise (only the FP32 accumulation
+    sums of those operands: the BF16 outputs agree to 5e-3 normwise (only the FP32 accumulation
     order differs, which moves a few roundings by one unit), and the kernel reports no timeout.
     On 32 x 48 every tile's halo wraps around the periodic edges (plain loads); on 64 x 80 the
     inner tiles' halos come by TMA."""
@@ -195,9 +197,9 @@ def test_tensor_core_conv_matches_mma_sync_and_exact_sums(gpu, cin, grouped, tra
     gx = 0.5 * zx * (1 + np.vectorize(__import__("math").erf)(zx / np.sqrt(2)))
     (a_tc, z_tc), (a_mma, z_mma) = outs[False], outs[True]
     print(f"\ntcgen05 vs mma.sync {rel_err(a_tc, a_mma):.2e}, vs exact {rel_err(a_tc, gx):.2e} (mma.sync vs exact {rel_err(a_mma, gx):.2e})")
-    assert rel_err(a_tc, a_mma) <= 1e-2 and rel_err(a_tc, gx) <= 1e-2
+    assert rel_err(a_tc, a_mma) <= 5e-3 and rel_err(a_tc, gx) <= 5e-3
     if train:
-        assert rel_err(z_tc, zx) <= 1e-2 and rel_err(z_tc, z_mma) <= 1e-2
+        assert rel_err(z_tc, zx) <= 5e-3 and rel_err(z_tc, z_mma) <= 5e-3
 
 
 @pytest.mark.parametrize("shape", [(2, 32, 48), (1, 64, 80)])
@@ -271,4 +273,4 @@ def test_tensor_core_input_gradient_matches_mma_sync(gpu, cin, shape):
     ref = acc * gp
     e_mma, e_exact = rel_err(outs[False], outs[True]), rel_err(outs[False], ref)
     print(f"\ninput gradient tcgen05 vs mma.sync {e_mma:.2e}, vs exact {e_exact:.2e}")
-    assert e_mma <= 1e-2 and e_exact <= 1e-2
+    assert e_mma <= 5e-3 and e_exact <= 5e-3

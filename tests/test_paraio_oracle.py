@@ -11,7 +11,8 @@ import pytest
 
 from oracle import paraio as PIO
 
-EXPECTED = Path(os.environ.get("WM_REFERENCE_ROOT", "/root/reference")) / "utils/iocore/jsonio_expected.json"
+# the reference checkout: $WM_REFERENCE_ROOT, else a checkout named "reference" beside this repository
+EXPECTED = Path(os.environ.get("WM_REFERENCE_ROOT", str(Path(__file__).resolve().parents[2] / "reference"))) / "utils/iocore/jsonio_expected.json"
 
 
 def test_fortran_real_format():

@@ -7,7 +7,11 @@ comes from a fixed static array inside the library.  This test acts as such a ca
 device buffers itself through the CUDA runtime, calls the entry point several times in a row on
 different states (the calls share the library's scratch), and compares each current with the one
 field__fdtd_i deposits on the allocating path, to the 1e-12 normwise tolerance of the other GPU
-tests.  It also checks that a grid over the size limit is refused.  This file is collected last.
+tests.  It also checks that the device's free memory does not change on the calls after the first
+(the first may place the static array in device memory under lazy module loading), that a particle
+moving more than one cell is reported as WM_ERR_CELL and the next valid call returns WM_OK (the
+shared status word is cleared on every call), and that a grid over the size limit is refused.
+This file is collected last.
 """
 import ctypes
 import ctypes.util
@@ -23,6 +27,7 @@ from wumingpic2d_gb300._native import lib
 pytestmark = pytest.mark.gpu
 TOL = 1e-12
 WM_ERR_BAD_ARG = 3
+WM_ERR_CELL = 4
 
 
 class CallerBuffers:
@@ -43,6 +48,7 @@ class CallerBuffers:
         rt.cudaMalloc.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]
         rt.cudaMemcpy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
         rt.cudaFree.argtypes = [ctypes.c_void_p]
+        rt.cudaMemGetInfo.argtypes = [ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
         self.rt = rt
         self.ptrs = []
 
@@ -59,6 +65,11 @@ class CallerBuffers:
 
     def get(self, p, out):
         assert self.rt.cudaMemcpy(out.ctypes.data, p, out.nbytes, self.D2H) == 0
+
+    def free_bytes(self):
+        free, total = ctypes.c_size_t(), ctypes.c_size_t()
+        assert self.rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+        return free.value
 
     def free(self):
         for p in self.ptrs:
@@ -78,16 +89,27 @@ def allocating_path(st):
     return gp, uj
 
 
-def noalloc_path(bufs, st, gp):
+def noalloc_call(bufs, st, gp):
+    """One call on caller-owned copies of (up, gp, cumcnt); returns (status, uj, the device's free
+    bytes just before and just after the call)."""
     d = st.d
     dup, dgp, dcc = bufs.put(st.up), bufs.put(gp), bufs.put(st.cumcnt)
     uj = d.alloc_uj()
     duj = bufs.alloc(uj.nbytes)
     q = np.ascontiguousarray(st.cfg.charge, dtype=np.float64)
+    before = bufs.free_bytes()
     status = lib().wm_deposit_current_noalloc(dup, dgp, dcc, duj, d.ndim, d.np, d.nsp, d.nxgs, d.nxge, d.nygs, d.nyge, 1.0,
                                               st.cfg.delt, 1.0, q.ctypes.data, None)
-    assert status == 0, status
+    after = bufs.free_bytes()
     bufs.get(duj, uj)
+    return status, uj, (before, after)
+
+
+def noalloc_path(bufs, st, gp, check_free=False):
+    status, uj, (before, after) = noalloc_call(bufs, st, gp)
+    assert status == 0, status
+    if check_free:  # not the first call on this device: the entry point allocates nothing
+        assert before - after < 2 << 20, (before, after)  # an allocation takes at least one 2 MiB page
     return uj
 
 
@@ -97,8 +119,8 @@ def test_noalloc_deposit_matches_allocating_path_on_consecutive_calls(gpu):
     expected = [allocating_path(st) for st in states]
     bufs = CallerBuffers()
     try:
-        for st, (gp, uj_ref) in [(states[0], expected[0]), (states[1], expected[1]), (states[0], expected[0])]:
-            uj = noalloc_path(bufs, st, gp)
+        for n, (st, (gp, uj_ref)) in enumerate([(states[0], expected[0]), (states[1], expected[1]), (states[0], expected[0])]):
+            uj = noalloc_path(bufs, st, gp, check_free=n > 0)
             for k in range(3):
                 assert rel_err(uj[k], uj_ref[k]) <= TOL, k
     finally:
@@ -112,5 +134,23 @@ def test_noalloc_refuses_grids_over_the_limit(gpu):
         q = np.array([1.0, -1.0])
         status = lib().wm_deposit_current_noalloc(p, p, p, p, 6, 16, 2, 2, 513, 2, 257, 1.0, 0.5, 1.0, q.ctypes.data, None)
         assert status == WM_ERR_BAD_ARG
+    finally:
+        bufs.free()
+
+
+def test_noalloc_reports_a_particle_moving_more_than_one_cell(gpu):
+    st = State(nx=40, ny=32, ppc=8, seed=23, field_amp=0.05)
+    gp, uj_ref = allocating_path(st)
+    bad = gp.copy(order="F")
+    x = bad[0, 0, 5, 1]  # one electron of row 5 lands three cells away, still inside the grid
+    bad[0, 0, 5, 1] = x - 3.0 if x >= st.d.nxgs + 4 else x + 3.0
+    assert st.d.nxgs <= bad[0, 0, 5, 1] < st.d.nxge + 1
+    bufs = CallerBuffers()
+    try:
+        status, _, _ = noalloc_call(bufs, st, bad)
+        assert status == WM_ERR_CELL
+        uj = noalloc_path(bufs, st, gp)  # the status word starts from zero again
+        for k in range(3):
+            assert rel_err(uj[k], uj_ref[k]) <= TOL, k
     finally:
         bufs.free()

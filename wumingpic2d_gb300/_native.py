@@ -97,6 +97,7 @@ SIGNATURES = {
     "wm_sim_guess_stats": [_P, _P],
     "wm_set_device": [_I],
     "wm_deposit_current_noalloc": [_P, _P, _P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _P, _P],
+    "wm_fp64_fma_rate": [ctypes.POINTER(_D), ctypes.POINTER(_D)],
     "wm_host_register": [_P, ctypes.c_size_t],
     "wm_host_unregister": [_P],
     "wm_host_alloc": [_P, ctypes.c_size_t],

@@ -213,7 +213,17 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
             }
     }
     __syncthreads();
-    if (!mx_bar_wait(fbar_a, 0)) atomicOr(status, (unsigned)WMDEV_TIMEOUT);  // (the step then fails)
+    // Every thread waits (bounded) for the field tile.  If any gave up, the CTA records the timeout
+    // (the step then fails), waits once more (bounded) so that the copy is not left writing into
+    // this CTA's shared memory after it exits, and pushes with zero fields rather than from a
+    // partly written tile: the move codes, counts and tile currents stay well formed, so the
+    // kernels after it stay in bounds.
+    if (__syncthreads_or(!mx_bar_wait(fbar_a, 0))) {
+        if (tid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
+        mx_bar_wait(fbar_a, 0);
+        for (int e = tid; e < 6 * 3 * MX_FTW; e += MX_THREADS) (&tmp[0][0][0])[e] = 0.f;
+        __syncthreads();
+    }
     // Each cell's six fields as biquadratics in the centred offsets hx, hy of particle.f90:96-129:
     // sum_ab T(a,b) sx_a(hx) sy_b(hy) = sum_pq C(q,p) hx^p hy^q, with the TSC weights
     // sx = (1/8 - hx/2 + hx^2/2, 3/4 - hx^2, 1/8 + hx/2 + hx^2/2).  Stored [(q*3 + p)*6 + m].

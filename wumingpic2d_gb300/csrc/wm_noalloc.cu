@@ -15,8 +15,10 @@
 //   * every call uses the same scratch: calls that overlap on the GPU (different streams, or
 //     different host threads on one device) race and give wrong currents; serialise them;
 //   * the first call on each device looks up the scratch's device address with
-//     cudaGetSymbolAddress (once per device, with that device current); make that first call
-//     before any stream capture.
+//     cudaGetSymbolAddress (once per device, with that device current); under CUDA's default
+//     lazy module loading that first call is also when the array is placed in device memory, so
+//     make it at start-up, before any stream capture begins, and later calls allocate nothing;
+//   * every call is synchronous: it reads the status word back and waits for the stream.
 // The kernels are the ones of the allocating path (k_deposit_cells, k_deposit_fold and the
 // current fold of boundary_periodic__curre); only the source of their scratch differs.
 #include <mutex>
