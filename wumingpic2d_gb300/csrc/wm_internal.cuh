@@ -63,16 +63,20 @@ struct AoSView {
 
 // Mixed-precision particles: FP32 offsets (dx, dy) in [0, 1) inside the particle's cell, FP32
 // momenta, i64 pid.  The cell itself is not stored: rows are cell-sorted and cumcnt gives it.
+// (dx, dy, ux, uy) share one 16-byte record, so a particle moves with one vector access and one
+// 4-byte access to the uz plane; the ids are a separate plane.
 struct MixedView {
-    float *x, *y, *ux, *uy, *uz;  // x, y hold the in-cell offsets
+    float4 *xyuv;  // (dx, dy, ux, uy) per slot
+    float *uz;
     long long *pid;
     const long long *rowbase;
     __device__ __forceinline__ long long idx(int row, int s0) const { return rowbase[row] + s0; }
-    __device__ __forceinline__ float &X(long long p) const { return x[p]; }
-    __device__ __forceinline__ float &Y(long long p) const { return y[p]; }
-    __device__ __forceinline__ float &UX(long long p) const { return ux[p]; }
-    __device__ __forceinline__ float &UY(long long p) const { return uy[p]; }
+    __device__ __forceinline__ float &X(long long p) const { return xyuv[p].x; }
+    __device__ __forceinline__ float &Y(long long p) const { return xyuv[p].y; }
+    __device__ __forceinline__ float &UX(long long p) const { return xyuv[p].z; }
+    __device__ __forceinline__ float &UY(long long p) const { return xyuv[p].w; }
     __device__ __forceinline__ float &UZ(long long p) const { return uz[p]; }
+    __device__ __forceinline__ float4 &XYUV(long long p) const { return xyuv[p]; }
     __device__ __forceinline__ long long getpid(long long p) const { return pid[p]; }
     __device__ __forceinline__ void setpid(long long p, long long v) const { pid[p] = v; }
 };
@@ -84,6 +88,12 @@ __device__ __forceinline__ void copy_particle(const V &dst, long long pd, const 
     dst.Y(pd) = src.Y(ps);
     dst.UX(pd) = src.UX(ps);
     dst.UY(pd) = src.UY(ps);
+    dst.UZ(pd) = src.UZ(ps);
+    dst.setpid(pd, src.getpid(ps));
+}
+__device__ __forceinline__ void copy_particle(const MixedView &dst, long long pd, const MixedView &src, long long ps)
+{
+    dst.XYUV(pd) = src.XYUV(ps);
     dst.UZ(pd) = src.UZ(ps);
     dst.setpid(pd, src.getpid(ps));
 }

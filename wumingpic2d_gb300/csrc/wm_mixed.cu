@@ -7,12 +7,13 @@
 // FP32, the Esirkepov deposit of field.f90:224-298 in FP32, the periodic wrap of
 // boundary_periodic.f90:61-96 and :143-165 as integer cell arithmetic, and the destination cell key
 // and row direction the rebin needs.  The tile's cell-centred fields arrive as one TMA box; four
-// lanes share a cell; each lane's next two particles are copied into shared memory (cp.async)
-// while the current one is pushed.  The TSC-weighted 3x3 gather of
+// lanes share a cell, so the cell's (dx, dy, ux, uy) records move as two full 32-byte sectors per
+// step of the loop; each lane's next two particles (the 16-byte record and uz) are copied into
+// shared memory (cp.async) while the current one is pushed.  The TSC-weighted 3x3 gather of
 // each field is a biquadratic in the particle's offsets, so the kernel stages its nine
 // coefficients per cell and field and evaluates it by Horner's rule, two fields per packed
 // fma.rn.f32x2.  Each lane keeps the cell's 5x5x3 partial currents in registers (the cell's
-// particles all deposit on the same 5x5 nodes); the four lanes add theirs with shuffles, and the
+// particles all deposit on the same 5x5 nodes); the cell's lanes add theirs with shuffles, and the
 // tile's node currents are summed from the per-cell partials in a fixed order.  Tile currents go
 // to a per-tile buffer; k_mixed_jfold adds them into the FP64 global J node by node in a fixed
 // order, so the result is deterministic and no atomics touch the currents.  The rebin either
@@ -29,7 +30,10 @@ namespace {
 #define WM_MX_THREADS 128  // threads per push CTA (a build-time choice, 128 or 256; 128 measured 2.6 % faster)
 #endif
 constexpr int MX_THREADS = WM_MX_THREADS;
-constexpr int MX_LPC = 4;                   // lanes per cell
+#ifndef WM_MX_LPC
+#define WM_MX_LPC 4  // lanes per cell (4: the cell's four 16-byte records fill two sectors per step; 8 measured 14 % slower)
+#endif
+constexpr int MX_LPC = WM_MX_LPC;           // lanes per cell
 constexpr int MX_TW = MX_THREADS / MX_LPC;  // cells per tile (one row, one species)
 constexpr int MX_JW = MX_TW + 4;            // node columns a tile deposits on
 constexpr int MX_FS = 60;                   // floats per cell of staged stencil: 9 x 6 used; 60 keeps 128-bit reads conflict-free
@@ -106,20 +110,24 @@ __device__ __forceinline__ void cp_async4(float *dst, const float *src, unsigned
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src), "r"(nbytes)
                  : "memory");
 }
+// The same for one 16-byte record (both addresses 16-byte aligned; nbytes 0 or 16).
+__device__ __forceinline__ void cp_async16(float4 *dst, const float4 *src, unsigned nbytes)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"((unsigned)__cvta_generic_to_shared(dst)), "l"(src), "r"(nbytes)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// The pushed particle's five components and its move code, stored only by lanes that hold a
-// particle (one predicate for the six stores: the loop body has no branches).
+// The pushed particle (one 16-byte record, uz) and its move code, stored only by lanes that
+// hold a particle (one predicate for the three stores: the loop body has no branches).
 __device__ __forceinline__ void store_particle(const MixedView &b, long long p, float x, float y, float ux, float uy, float uz,
                                                unsigned *code, unsigned cv, bool pred)
 {
     asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %0, 0;\n\t"
-                 "@q st.global.f32 [%1], %2;\n\t@q st.global.f32 [%3], %4;\n\t@q st.global.f32 [%5], %6;\n\t"
-                 "@q st.global.f32 [%7], %8;\n\t@q st.global.f32 [%9], %10;\n\t@q st.global.u32 [%11], %12;\n\t}"
-                 ::"r"((unsigned)pred), "l"(b.x + p), "f"(x), "l"(b.y + p), "f"(y), "l"(b.ux + p), "f"(ux), "l"(b.uy + p), "f"(uy),
-                 "l"(b.uz + p), "f"(uz), "l"(code + p), "r"(cv)
+                 "@q st.global.v4.f32 [%1], {%2, %3, %4, %5};\n\t@q st.global.f32 [%6], %7;\n\t@q st.global.u32 [%8], %9;\n\t}"
+                 ::"r"((unsigned)pred), "l"(b.xyuv + p), "f"(x), "f"(y), "f"(ux), "f"(uy), "l"(b.uz + p), "f"(uz), "l"(code + p), "r"(cv)
                  : "memory");
 }
 
@@ -156,7 +164,7 @@ __device__ __forceinline__ bool mx_bar_wait(uint32_t bar, uint32_t parity)
     return false;
 }
 
-// One CTA per (tile of 64 cells, row, species); 4 lanes per cell.  The loop body has no branches:
+// One CTA per (tile of MX_TW cells, row, species); MX_LPC lanes per cell.  The loop body has no branches:
 // a lane past the end of its cell runs on a zero particle with zero deposit weights and its stores
 // switched off.  Each lane's next particle is copied into shared memory (cp.async) while the
 // current one is pushed.
@@ -177,7 +185,8 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     __shared__ float cellpj[65][MX_PW];                   // per-cell partials; first holds the node rows
     __shared__ int cc[MX_TW + 1];
     __shared__ float spc[5];
-    __shared__ float pbuf[MX_NBUF][5][MX_THREADS];  // each lane's next particles, MX_PFD ahead
+    __shared__ float4 pbuf4[MX_NBUF][MX_THREADS];   // each lane's next particles, MX_PFD ahead: (dx, dy, ux, uy)
+    __shared__ float pbufz[MX_NBUF][MX_THREADS];    // and uz
     __shared__ unsigned permring[GATHER ? MX_PR : 1][MX_THREADS];
     __shared__ __align__(128) float tmp[6][3][MX_FTW];  // the tile's cell-centred fields (one TMA box)
     __shared__ __align__(8) uint64_t fbar;
@@ -282,13 +291,8 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     auto canon = [&](int it) { return rbase + s_beg + sub + (long long)it * MX_LPC; };
     auto prefetch = [&](int it, int slot, long long q, int jperm) {
         const bool v = it < nmine;
-        const unsigned nb = v ? 4u : 0u;
-        float(*dst)[MX_THREADS] = pbuf[slot];
-        cp_async4(&dst[0][tid], a.x + q, nb);
-        cp_async4(&dst[1][tid], a.y + q, nb);
-        cp_async4(&dst[2][tid], a.ux + q, nb);
-        cp_async4(&dst[3][tid], a.uy + q, nb);
-        cp_async4(&dst[4][tid], a.uz + q, nb);
+        cp_async16(&pbuf4[slot][tid], a.xyuv + q, v ? 16u : 0u);
+        cp_async4(&pbufz[slot][tid], a.uz + q, v ? 4u : 0u);
         if (GATHER && jperm >= 0) {  // (the first MX_PFD groups carry no perm entry)
             const bool vp = jperm < nmine;
             cp_async4(reinterpret_cast<float *>(&permring[jperm % MX_PR][tid]), reinterpret_cast<const float *>(perm + (vp ? canon(jperm) : 0)),
@@ -323,11 +327,12 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
         if (it + MX_PFD < nwarp) prefetch(it + MX_PFD, wslot, source(it + MX_PFD), it + 2 * MX_PFD + 1);
         else cp_async_commit();
         cp_async_wait<MX_PFD>();
-        const float(*src)[MX_THREADS] = pbuf[rslot];
+        const float4 pin = pbuf4[rslot][tid];
+        float u3 = pbufz[rslot][tid];
         rslot = rslot + 1 == MX_NBUF ? 0 : rslot + 1;
         wslot = wslot + 1 == MX_NBUF ? 0 : wslot + 1;
-        const float dx = src[0][tid], dy = src[1][tid];
-        float u1 = src[2][tid], u2 = src[3][tid], u3 = src[4][tid];
+        const float dx = pin.x, dy = pin.y;
+        float u1 = pin.z, u2 = pin.w;
         float sx0, sx1, sx2, sy0, sy1, sy2;
         shape3(dx - 0.5f, sx0, sx1, sx2);
         shape3(dy - 0.5f, sy0, sy1, sy2);
@@ -507,7 +512,7 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     if (has_cell)
         for (int dd = sub; dd < 9; dd += MX_LPC) cnt9[((long long)row * g.nx + cg) * 9 + dd] = dcnt[c][dd];
 
-    // the 4 lanes of a cell add their partial currents; lane 0 of the cell keeps the sum
+    // the MX_LPC lanes of a cell add their partial currents; lane 0 of the cell keeps the sum
 #pragma unroll
     for (int jp = 0; jp < 5; ++jp)
 #pragma unroll
@@ -669,10 +674,7 @@ __global__ void k_mixed_gather(WmGeom g, MixedView src, MixedView dst, const uns
     const long long rb = dst.rowbase[row];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
         const long long p = rb + s, q = perm[p];
-        dst.X(p) = src.X(q);
-        dst.Y(p) = src.Y(q);
-        dst.UX(p) = src.UX(q);
-        dst.UY(p) = src.UY(q);
+        dst.XYUV(p) = src.XYUV(q);
         dst.UZ(p) = src.UZ(q);
         dst.setpid(p, src.getpid((long long)idperm[p]));
     }
@@ -780,10 +782,7 @@ __global__ void k_mixed_unpack(WmGeom g, const double *__restrict__ stage, int p
             key[p] = 0;
             continue;
         }
-        dst.X(p) = ox;
-        dst.Y(p) = oy;
-        dst.UX(p) = (float)a[2];
-        dst.UY(p) = (float)a[3];
+        dst.XYUV(p) = make_float4(ox, oy, (float)a[2], (float)a[3]);
         dst.UZ(p) = (float)a[4];
         dst.setpid(p, __double_as_longlong(a[5]));
         const int k = row * g.nx + ci;
@@ -834,10 +833,11 @@ __global__ void __launch_bounds__(PACK_THREADS) k_mixed_pack(WmGeom g, MixedView
             }
             const long long p = rb + s;
             double *a = buf + 6 * threadIdx.x;
-            a[0] = (double)(g.nxgs + c0 + lo) + (double)src.X(p);
-            a[1] = (double)(g.nys + jr) + (double)src.Y(p);
-            a[2] = src.UX(p);
-            a[3] = src.UY(p);
+            const float4 r = src.XYUV(p);
+            a[0] = (double)(g.nxgs + c0 + lo) + (double)r.x;
+            a[1] = (double)(g.nys + jr) + (double)r.y;
+            a[2] = r.z;
+            a[3] = r.w;
             a[4] = src.UZ(p);
             a[5] = __longlong_as_double(src.getpid(p));
         }

@@ -202,10 +202,7 @@ struct wm_sim {
     MixedView mview(DevBuf *S, int rb, int pidw = -1) const
     {
         MixedView v;
-        v.x = S[0].as<float>();
-        v.y = S[1].as<float>();
-        v.ux = S[2].as<float>();
-        v.uy = S[3].as<float>();
+        v.xyuv = S[0].as<float4>();
         v.uz = S[4].as<float>();
         v.pid = (pidw < 0 ? S[5] : (pidw == 0 ? A[5] : B[5])).as<long long>();
         v.rowbase = rowbase[rb].as<long long>();
@@ -297,8 +294,9 @@ struct wm_sim {
     {
         const size_t nf = (size_t)g.nxw * g.nyw, nc = (size_t)g.nx * g.ny;
         cap = capacity;
-        for (int c = 0; c < 6; ++c) {  // mixed: five FP32 components and the i64 pid
-            const size_t esz = (mixed() && c < 5) ? 4 : 8;
+        for (int c = 0; c < 6; ++c) {  // mixed: the (dx, dy, ux, uy) records in [0], the uz plane in [4], the i64 pid
+            const size_t esz = !mixed() ? 8 : c == 0 ? 16 : c == 4 ? 4 : c == 5 ? 8 : 0;
+            if (esz == 0) continue;
             WM_TRY(A[c].ensure(esz * (size_t)cap));
             WM_TRY(B[c].ensure(esz * (size_t)cap));
         }
