@@ -224,3 +224,48 @@ def test_mixed_rebin_permutation_equals_move_with_injection(gpu):
     for x, y in zip(a, b):
         assert np.array_equal(x.view(np.uint64) if x.dtype == np.float64 else x, y.view(np.uint64) if y.dtype == np.float64 else y)
     assert np.array_equal(ea4, eb4) and np.array_equal(ea, eb)
+
+
+def test_mixed_one_step_with_many_cell_changes(gpu):
+    """A hot plasma (electrons at 0.5c thermal speed, 96 per cell) in which more than 16 particles
+    of a cell change cell in one step.  The push keeps up to 16 such particles per cell in a queue
+    that its cell's lanes deposit after the loop; a tile whose queue overflows is recomputed with
+    every particle deposited in the loop.  The step must meet the bounds of the one-step test above
+    against the FP64 oracle, and two runs of three steps agree bit for bit."""
+    st = State(nx=64, ny=32, ppc=96, seed=49, field_amp=0.05, df_amp=1e-3, slack=2.0)
+    st.up[2:5, :, :, 1] *= 10.0  # (118 of the 2048 cells see more than 16 electrons leave; the ion tiles none)
+    st.gp = st.up.copy(order="F")
+    ref = st.copy()
+    S = ref.oracle_state()
+    assert O.step(ref.par, ref.d, ref.up, ref.gp, ref.uf, ref.cumcnt, ref.np2, S)[0] == 0
+    # the electrons of the busiest cell that changed cell in the step: more than the queue holds
+    d = st.d
+    (pid0, c0), (pid1, c1) = by_pid(d, st.up, st.np2)[1], by_pid(d, ref.up, ref.np2)[1]
+    assert np.array_equal(pid0, pid1)
+    cell0 = (np.floor(c0[1]) * d.nx + np.floor(c0[0])).astype(int)
+    moved = (np.floor(c0[0]) != np.floor(c1[0])) | (np.floor(c0[1]) != np.floor(c1[1]))
+    assert np.bincount(cell0[moved]).max() > 16
+    with _sim(st) as sim:
+        sim.load(st.up, st.uf, st.np2)
+        sim.set_work(st.df)
+        sim.step(1)
+        up, uf, np2, cc = sim.store()
+        df, uj = sim.get_work()
+    a, b = by_pid(d, up, np2), by_pid(d, ref.up, ref.np2)
+    for isp in range(2):
+        assert np.array_equal(a[isp][0], b[isp][0])
+        assert np.max(np.abs(periodic_diff(a[isp][1][0], b[isp][1][0], d.nx))) <= 2e-6
+        assert np.max(np.abs(periodic_diff(a[isp][1][1], b[isp][1][1], d.ny))) <= 2e-6
+        assert rel_err(np.stack(a[isp][1][2:5]), np.stack(b[isp][1][2:5])) <= 2e-6
+    for k in range(3):
+        assert rel_err(uj[k], S.uj[k]) <= 1e-5, k
+    for k in range(6):
+        assert rel_err(uf[k], ref.uf[k]) <= 1e-5, k
+    outs = []
+    for _ in range(2):
+        with _sim(st) as sim:
+            sim.load(st.up, st.uf, st.np2)
+            sim.step(3)
+            outs.append(sim.store())
+    for x, y in zip(*outs):
+        assert np.array_equal(x.view(np.uint64) if x.dtype == np.float64 else x, y.view(np.uint64) if y.dtype == np.float64 else y)

@@ -96,8 +96,11 @@ int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cuda
 // k_mixed_perm records it as a slot permutation that the next push reads through (perm != null:
 // the particle of slot p is at slot perm[p] of a; the push leaves the ids alone, and k_mixed_perm
 // composes the permutation of the id array, idperm, instead).
+// ovf: 1 + (tiles of the grid) u32 of scratch for the list of tiles whose queue of cell-changing
+// particles overflowed (wm_mixed_ovf_words); those tiles are recomputed by a second launch.
 int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const unsigned *perm, const float *fcc,
-                                 const int *cumcnt, const WmRebinScratch &sc, int *cnt9, float *jtile, cudaStream_t st);
+                                 const int *cumcnt, const WmRebinScratch &sc, int *cnt9, float *jtile, unsigned *ovf, cudaStream_t st);
+size_t wm_mixed_ovf_words(const WmGeom &g);
 int wm_launch_mixed_incoming(const WmGeom &g, const int *cnt9, int *off9, const WmRebinScratch &sc, cudaStream_t st);
 int wm_launch_mixed_move(const WmGeom &g, MixedView src, MixedView dst, const int *cumcnt_old, const int *cumcnt_new, const int *off9,
                          const WmRebinScratch &sc, cudaStream_t st);

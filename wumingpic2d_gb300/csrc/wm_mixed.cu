@@ -48,6 +48,10 @@ constexpr unsigned FULL = 0xffffffffu;
 constexpr int MX_PFD = WM_MX_PFD;
 constexpr int MX_NBUF = MX_PFD + 1;
 constexpr int MX_PR = MX_PFD + 2;  // perm entries each lane holds (GATHER): iterations it+MX_PFD .. it+2 MX_PFD+1
+#ifndef WM_MX_XQ
+#define WM_MX_XQ 16
+#endif
+constexpr int MX_XQ = WM_MX_XQ;  // per-cell queue of particles that changed cell, deposited after the loop
 
 struct MxConst {
     float fac1[WM_MAX_SP], txxx[WM_MAX_SP], fac2[WM_MAX_SP], mqdd[WM_MAX_SP], q[WM_MAX_SP];
@@ -174,15 +178,26 @@ __device__ __forceinline__ bool mx_bar_wait(uint32_t bar, uint32_t parity)
 // GATHER: the particle of cell-sorted slot p is at slot perm[p] of set a (the previous step's push
 // output, see k_mixed_perm); otherwise it is at slot p.  The push does not touch the ids.
 // fmap: TMA descriptor of the cell-centred fields (columns, rows, planes), boxes of MX_FTW x 3 x 6.
-template <int BC, bool GATHER>  // BC = WM_BC_*: the walls' code is compiled only where it runs
-__global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
-    k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const unsigned *__restrict__ perm,
-                         const __grid_constant__ CUtensorMap fmap, const int *__restrict__ cumcnt, unsigned *__restrict__ code,
-                         int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status)
+// SPLIT: particles that change cell go through the per-cell queue (a tile whose queue overflows is
+// appended to ovf = {count, tiles...} and recomputed by k_mixed_push_redo); otherwise (the redo)
+// every particle is deposited in the loop with the full form.  parity: the phase of the CTA's
+// field-tile mbarrier for this tile (the CTA's tiles alternate it).
+constexpr int MX_PJ_BYTES = 65 * MX_PW * 4;
+constexpr int MX_XQ_BYTES = MX_TW * MX_XQ * 24;
+template <int BC, bool GATHER, bool SPLIT>
+__device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc, const MixedView &a, const MixedView &b,
+                                             const unsigned *__restrict__ perm, const CUtensorMap &fmap, const int *__restrict__ cumcnt,
+                                             unsigned *__restrict__ code, int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status,
+                                             unsigned *ovf, int tile, int jr, int isp, uint32_t parity)
 {
     __shared__ int dcnt[MX_TW][9];  // per cell: particles so far that move in direction d
     __shared__ __align__(16) float fcell[MX_TW][MX_FS];  // [cell][(b*3 + a)*6 + m]
-    __shared__ float cellpj[65][MX_PW];                   // per-cell partials; first holds the node rows
+    // per-cell partials after the loop (the first rows hold the node sums); during the loop (SPLIT)
+    // the same bytes hold the per-cell queue of particles that changed cell
+    __shared__ __align__(16) unsigned char qpj[SPLIT && MX_XQ_BYTES > MX_PJ_BYTES ? MX_XQ_BYTES : MX_PJ_BYTES];
+    float(*cellpj)[MX_PW] = reinterpret_cast<float(*)[MX_PW]>(qpj);
+    float4(*xq4)[MX_XQ] = reinterpret_cast<float4(*)[MX_XQ]>(qpj);                           // old dx, dy; new dx, dy
+    float2(*xq2)[MX_XQ] = reinterpret_cast<float2(*)[MX_XQ]>(qpj + MX_TW * MX_XQ * 16);      // q vz; increments + 1 (2-bit fields)
     __shared__ int cc[MX_TW + 1];
     __shared__ float spc[5];
     __shared__ float4 pbuf4[MX_NBUF][MX_THREADS];   // each lane's next particles, MX_PFD ahead: (dx, dy, ux, uy)
@@ -190,7 +205,6 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     __shared__ unsigned permring[GATHER ? MX_PR : 1][MX_THREADS];
     __shared__ __align__(128) float tmp[6][3][MX_FTW];  // the tile's cell-centred fields (one TMA box)
     __shared__ __align__(8) uint64_t fbar;
-    const int tile = blockIdx.x, jr = blockIdx.y, isp = blockIdx.z;
     const int row = isp * g.ny + jr;
     const int c0 = tile * MX_TW;
     const int ncell = min(MX_TW, g.nx - c0);
@@ -200,8 +214,10 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     // the grid read as zero), completing on an mbarrier that every thread waits on below
     const uint32_t fbar_a = (uint32_t)__cvta_generic_to_shared(&fbar);
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(fbar_a) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        if (parity == 0) {  // the CTA's first tile
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(fbar_a) : "memory");
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        }
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fbar_a), "r"((uint32_t)sizeof(tmp)) : "memory");
         asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
                          (uint32_t)__cvta_generic_to_shared(&tmp[0][0][0])),
@@ -227,9 +243,9 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     // this CTA's shared memory after it exits, and pushes with zero fields rather than from a
     // partly written tile: the move codes, counts and tile currents stay well formed, so the
     // kernels after it stay in bounds.
-    if (__syncthreads_or(!mx_bar_wait(fbar_a, 0))) {
+    if (__syncthreads_or(!mx_bar_wait(fbar_a, parity))) {
         if (tid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
-        mx_bar_wait(fbar_a, 0);
+        mx_bar_wait(fbar_a, parity);
         for (int e = tid; e < 6 * 3 * MX_FTW; e += MX_THREADS) (&tmp[0][0][0])[e] = 0.f;
         __syncthreads();
     }
@@ -253,12 +269,6 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
             fcell[c][(1 * 3 + p) * 6 + m] = 0.5f * (P[2][p] - P[0][p]);
             fcell[c][(2 * 3 + p) * 6 + m] = 0.5f * P[0][p] - P[1][p] + 0.5f * P[2][p];
         }
-    }
-    __syncthreads();
-    // the node rows are consumed: zero the pad columns of the partials buffer
-    for (int e = tid; e < 65 * 8; e += MX_THREADS) {
-        const int r = e >> 3, q = e & 7;
-        cellpj[r][q < 4 ? q : MX_TW + q] = 0.f;
     }
     for (int e = tid; e < MX_TW * 9; e += MX_THREADS) (&dcnt[0][0])[e] = 0;
     __syncthreads();
@@ -284,6 +294,93 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
             if (jp < 4) ay[jp][ip] = 0.f;
             az[jp][ip] = 0.f;
         }
+    // Esirkepov's full 5x5 form (field.f90:224-298) for one particle: old offsets (dxo, dyo) in its
+    // cell, new offsets (nxn, nyn) in the cell inc = (ix, iy) away, weights mq = -q dx/dt and
+    // qg = q vz (zero for no deposit), added to this lane's accumulators.
+    auto deposit_full = [&](float dxo, float dyo, float nxn, float nyn, int ix, int iy, float mq, float qg) {
+        float sx0, sx1, sx2, sy0, sy1, sy2;
+        shape3(dxo - 0.5f, sx0, sx1, sx2);
+        shape3(dyo - 0.5f, sy0, sy1, sy2);
+        // old shape on nodes 1..3 about the old cell, new shape on 1+inc..3+inc
+        float dsx[5], dsy[5];
+        {
+            float b0, b1, b2;
+            shape3(nxn - 0.5f, b0, b1, b2);
+            const bool lo = ix < 0, mid = ix == 0, hi = ix > 0;
+            dsx[0] = lo ? b0 : 0.f;
+            dsx[1] = (lo ? b1 : mid ? b0 : 0.f) - sx0;
+            dsx[2] = (lo ? b2 : mid ? b1 : b0) - sx1;
+            dsx[3] = (hi ? b1 : mid ? b2 : 0.f) - sx2;
+            dsx[4] = hi ? b2 : 0.f;
+            shape3(nyn - 0.5f, b0, b1, b2);
+            const bool ylo = iy < 0, ymid = iy == 0, yhi = iy > 0;
+            dsy[0] = ylo ? b0 : 0.f;
+            dsy[1] = (ylo ? b1 : ymid ? b0 : 0.f) - sy0;
+            dsy[2] = (ylo ? b2 : ymid ? b1 : b0) - sy1;
+            dsy[3] = (yhi ? b1 : ymid ? b2 : 0.f) - sy2;
+            dsy[4] = yhi ? b2 : 0.f;
+        }
+        const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f}, s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
+        float cx[4], cy[4];
+        cx[0] = dsx[0];
+        cy[0] = dsy[0];
+    #pragma unroll
+        for (int m = 1; m < 4; ++m) {
+            cx[m] = cx[m - 1] + dsx[m];
+            cy[m] = cy[m - 1] + dsy[m];
+        }
+        // the species factor folded into the cumulative weights, qg/2 and qg/3 formed once
+    #pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            cx[m] *= mq;
+            cy[m] *= mq;
+        }
+        const float qh = 0.5f * qg, q3 = (1.f / 3.f) * qg;
+        float wy[5], z1[5], z2[5];
+    #pragma unroll
+        for (int jp = 0; jp < 5; ++jp) {
+            const bool inner = jp >= 1 && jp <= 3;
+            wy[jp] = inner ? s0y[jp] + 0.5f * dsy[jp] : 0.5f * dsy[jp];
+            z1[jp] = qg * wy[jp];
+            z2[jp] = inner ? fmaf(qh, s0y[jp], q3 * dsy[jp]) : q3 * dsy[jp];
+        }
+        // the accumulators in pairs, one packed FMA per pair (each element's FMAs in the same order)
+        auto acc2 = [](float &lo, float &hi, unsigned long long m1, unsigned long long m2) {
+            unpack2(fma2(m1, m2, pack2(lo, hi)), lo, hi);
+            };
+            const unsigned long long cx01 = pack2(cx[0], cx[1]), cx23 = pack2(cx[2], cx[3]);
+            const unsigned long long cy01 = pack2(cy[0], cy[1]), cy23 = pack2(cy[2], cy[3]);
+    #pragma unroll
+            for (int jp = 0; jp < 5; ++jp) {
+                const unsigned long long w2 = pack2(wy[jp], wy[jp]);
+                acc2(ax[jp][0], ax[jp][1], w2, cx01);
+                acc2(ax[jp][2], ax[jp][3], w2, cx23);
+            }
+    #pragma unroll
+            for (int ip = 0; ip < 5; ++ip) {
+                const float fx = (ip >= 1 && ip <= 3) ? s0x[ip] + 0.5f * dsx[ip] : 0.5f * dsx[ip];
+                const unsigned long long f2 = pack2(fx, fx);
+                acc2(ay[0][ip], ay[1][ip], f2, cy01);
+                acc2(ay[2][ip], ay[3][ip], f2, cy23);
+            }
+            const unsigned long long z2a = pack2(z2[0], z2[1]), z2b = pack2(z2[2], z2[3]);
+            const unsigned long long z1a = pack2(z1[0], z1[1]), z1b = pack2(z1[2], z1[3]);
+    #pragma unroll
+            for (int ip = 0; ip < 5; ++ip) {
+                const unsigned long long d2 = pack2(dsx[ip], dsx[ip]);
+                acc2(az[0][ip], az[1][ip], d2, z2a);
+                acc2(az[2][ip], az[3][ip], d2, z2b);
+                az[4][ip] = fmaf(dsx[ip], z2[4], az[4][ip]);
+                if (ip >= 1 && ip <= 3) {
+                    const unsigned long long s2 = pack2(s0x[ip], s0x[ip]);
+                    acc2(az[0][ip], az[1][ip], s2, z1a);
+                    acc2(az[2][ip], az[3][ip], s2, z1b);
+                    az[4][ip] = fmaf(s0x[ip], z1[4], az[4][ip]);
+                }
+            }
+    };
+    const unsigned cellmask = ((1u << MX_LPC) - 1u) << (lane & ~(MX_LPC - 1));  // this cell's lanes in the warp
+    int xn = 0;  // particles of this cell that changed cell so far (the same in all its lanes)
     unsigned bad = 0;
     // lane's particle of iteration it (at slot q of set a) -> pbuf[slot]; a lane past its cell copies zeros.
     // GATHER: the perm entry of iteration j travels in the copy group of iteration j - MX_PFD - 1
@@ -404,83 +501,52 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
             incx = cn - cg;
             bad |= valid & (incx < -1 || incx > 1);
         }
-        // Esirkepov: old shape on nodes 1..3 about the old cell, new shape on 1+inc..3+inc
-        float dsx[5], dsy[5];
-        {
-            float b0, b1, b2;
-            shape3(nx1 - 0.5f, b0, b1, b2);
-            const bool lo = incx < 0, mid = incx == 0, hi = incx > 0;
-            dsx[0] = lo ? b0 : 0.f;
-            dsx[1] = (lo ? b1 : mid ? b0 : 0.f) - sx0;
-            dsx[2] = (lo ? b2 : mid ? b1 : b0) - sx1;
-            dsx[3] = (hi ? b1 : mid ? b2 : 0.f) - sx2;
-            dsx[4] = hi ? b2 : 0.f;
-            shape3(ny1 - 0.5f, b0, b1, b2);
-            const bool ylo = incy < 0, ymid = incy == 0, yhi = incy > 0;
-            dsy[0] = ylo ? b0 : 0.f;
-            dsy[1] = (ylo ? b1 : ymid ? b0 : 0.f) - sy0;
-            dsy[2] = (ylo ? b2 : ymid ? b1 : b0) - sy1;
-            dsy[3] = (yhi ? b1 : ymid ? b2 : 0.f) - sy2;
-            dsy[4] = yhi ? b2 : 0.f;
-        }
-        const float s0x[5] = {0.f, sx0, sx1, sx2, 0.f}, s0y[5] = {0.f, sy0, sy1, sy2, 0.f};
-        const float mq = valid ? mqdd : 0.f;           // zero weights for a lane past its cell
+        // Esirkepov (field.f90:224-298).  A particle that stays in its cell (inc = 0 in x and y: most
+        // of them) has its old and new shapes on the 3x3 nodes about the cell, so it adds only Jx on
+        // columns 1-2, Jy on rows 1-2 and Jz on the 3x3 block: the terms the full form gives there,
+        // each node's FMAs in the same order.  (The full form's other terms are zero for it, but for
+        // the rounding residue of the cumulative sums cx(3) and cy(3), which the continuity equation
+        // sets to zero and which are dropped.)  A particle that changes cell is queued in shared
+        // memory and deposited with the full form by its cell's lanes after the loop; if the cell's
+        // queue is full, the warp deposits it at once.
+        const float mq = valid ? mqdd : 0.f;  // zero weights for a lane past its cell
         const float qg = valid ? qs * u3 * ig_dep : 0.f;
-        float cx[4], cy[4];
-        cx[0] = dsx[0];
-        cy[0] = dsy[0];
-#pragma unroll
-        for (int m = 1; m < 4; ++m) {
-            cx[m] = cx[m - 1] + dsx[m];
-            cy[m] = cy[m - 1] + dsy[m];
+        const bool stay = !SPLIT || (incx == 0 && incy == 0);
+        const bool cross = SPLIT && valid && !stay;
+        const unsigned xm = __ballot_sync(FULL, cross) & cellmask;
+        const int xslot = xn + __popc(xm & lanemask_lt());
+        xn += __popc(xm);
+        if (cross && xslot < MX_XQ) {
+            xq4[c][xslot] = make_float4(dx, dy, nx1, ny1);
+            xq2[c][xslot] = make_float2(qg, __int_as_float(((incx > 0) - (incx < 0) + 1) | (((incy > 0) - (incy < 0) + 1) << 2)));
         }
-        // the species factor folded into the cumulative weights, qg/2 and qg/3 formed once
+        if constexpr (!SPLIT) {
+            deposit_full(dx, dy, nx1, ny1, incx, incy, mq, qg);
+        } else {
+            float b0, b1, b2, c0, c1, c2;
+            shape3(nx1 - 0.5f, b0, b1, b2);
+            shape3(ny1 - 0.5f, c0, c1, c2);
+            const float ms = stay ? mq : 0.f, qz = stay ? qg : 0.f;
+            const float ex[3] = {b0 - sx0, b1 - sx1, b2 - sx2}, ey[3] = {c0 - sy0, c1 - sy1, c2 - sy2};  // dsx, dsy on nodes 1..3
+            const float sxa[3] = {sx0, sx1, sx2}, sya[3] = {sy0, sy1, sy2};
+            const float cx1 = ex[0] * ms, cx2 = (ex[0] + ex[1]) * ms;
+            const float cy1 = ey[0] * ms, cy2 = (ey[0] + ey[1]) * ms;
+            const float qh = 0.5f * qz, q3 = (1.f / 3.f) * qz;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-            cx[m] *= mq;
-            cy[m] *= mq;
-        }
-        const float qh = 0.5f * qg, q3 = (1.f / 3.f) * qg;
-        float wy[5], z1[5], z2[5];
+            for (int j = 0; j < 3; ++j) {
+                const float wy = sya[j] + 0.5f * ey[j];
+                ax[j + 1][1] = fmaf(wy, cx1, ax[j + 1][1]);
+                ax[j + 1][2] = fmaf(wy, cx2, ax[j + 1][2]);
+                const float fx = sxa[j] + 0.5f * ex[j];
+                ay[1][j + 1] = fmaf(fx, cy1, ay[1][j + 1]);
+                ay[2][j + 1] = fmaf(fx, cy2, ay[2][j + 1]);
+            }
 #pragma unroll
-        for (int jp = 0; jp < 5; ++jp) {
-            const bool inner = jp >= 1 && jp <= 3;
-            wy[jp] = inner ? s0y[jp] + 0.5f * dsy[jp] : 0.5f * dsy[jp];
-            z1[jp] = qg * wy[jp];
-            z2[jp] = inner ? fmaf(qh, s0y[jp], q3 * dsy[jp]) : q3 * dsy[jp];
-        }
-        // the accumulators in pairs, one packed FMA per pair (each element's FMAs in the same order)
-        auto acc2 = [](float &lo, float &hi, unsigned long long m1, unsigned long long m2) {
-            unpack2(fma2(m1, m2, pack2(lo, hi)), lo, hi);
-        };
-        const unsigned long long cx01 = pack2(cx[0], cx[1]), cx23 = pack2(cx[2], cx[3]);
-        const unsigned long long cy01 = pack2(cy[0], cy[1]), cy23 = pack2(cy[2], cy[3]);
+            for (int j = 0; j < 3; ++j) {
+                const float wy = sya[j] + 0.5f * ey[j];
+                const float z1 = qz * wy, z2 = fmaf(qh, sya[j], q3 * ey[j]);
 #pragma unroll
-        for (int jp = 0; jp < 5; ++jp) {
-            const unsigned long long w2 = pack2(wy[jp], wy[jp]);
-            acc2(ax[jp][0], ax[jp][1], w2, cx01);
-            acc2(ax[jp][2], ax[jp][3], w2, cx23);
-        }
-#pragma unroll
-        for (int ip = 0; ip < 5; ++ip) {
-            const float fx = (ip >= 1 && ip <= 3) ? s0x[ip] + 0.5f * dsx[ip] : 0.5f * dsx[ip];
-            const unsigned long long f2 = pack2(fx, fx);
-            acc2(ay[0][ip], ay[1][ip], f2, cy01);
-            acc2(ay[2][ip], ay[3][ip], f2, cy23);
-        }
-        const unsigned long long z2a = pack2(z2[0], z2[1]), z2b = pack2(z2[2], z2[3]);
-        const unsigned long long z1a = pack2(z1[0], z1[1]), z1b = pack2(z1[2], z1[3]);
-#pragma unroll
-        for (int ip = 0; ip < 5; ++ip) {
-            const unsigned long long d2 = pack2(dsx[ip], dsx[ip]);
-            acc2(az[0][ip], az[1][ip], d2, z2a);
-            acc2(az[2][ip], az[3][ip], d2, z2b);
-            az[4][ip] = fmaf(dsx[ip], z2[4], az[4][ip]);
-            if (ip >= 1 && ip <= 3) {
-                const unsigned long long s2 = pack2(s0x[ip], s0x[ip]);
-                acc2(az[0][ip], az[1][ip], s2, z1a);
-                acc2(az[2][ip], az[3][ip], s2, z1b);
-                az[4][ip] = fmaf(s0x[ip], z1[4], az[4][ip]);
+                for (int i = 0; i < 3; ++i) az[j + 1][i + 1] = fmaf(sxa[i], z1, fmaf(ex[i], z2, az[j + 1][i + 1]));
             }
         }
         if constexpr (BC == WM_BC_RECONNECTION) {  // particle_x after the field solve (boundary_reconnection.f90:80-91)
@@ -507,7 +573,29 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
         bad |= valid & (rank >= (1 << (28 - MX_CB)));
         store_particle(b, p, nx1, ny1, u1, u2, u3, code, ((unsigned)rank << (4 + MX_CB)) | ((unsigned)c << 4) | (unsigned)d, valid);
     }
+    // the queued particles of each cell that changed cell, deposited by the cell's lanes with the full form
+    if constexpr (SPLIT) {
+        const int nq = min(xn, MX_XQ);
+        int nit = nq > sub ? (nq - sub + MX_LPC - 1) / MX_LPC : 0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nit = max(nit, __shfl_xor_sync(FULL, nit, o));
+        __syncwarp();
+        for (int j = 0; j < nit; ++j) {
+            const int k = sub + j * MX_LPC;
+            const bool v = k < nq;
+            const float4 r = v ? xq4[c][k] : make_float4(0.5f, 0.5f, 0.5f, 0.5f);
+            const float2 r2 = v ? xq2[c][k] : make_float2(0.f, __int_as_float(5));
+            const int ic = __float_as_int(r2.y);
+            deposit_full(r.x, r.y, r.z, r.w, (ic & 3) - 1, (ic >> 2) - 1, v ? mqdd : 0.f, v ? r2.x : 0.f);
+        }
+    }
     if (bad) atomicOr(status, (unsigned)WMDEV_CELL);
+    if constexpr (SPLIT) {  // a queue that overflowed: the whole tile is recomputed by k_mixed_push_redo
+        if (__syncthreads_or(xn > MX_XQ) && tid == 0) {
+            const unsigned k = atomicAdd(ovf, 1u);
+            ovf[1 + k] = (unsigned)(((isp * g.ny + jr) * ((g.nx + MX_TW - 1) / MX_TW)) + tile);
+        }
+    }
     // this tile's per-cell direction counts (the cells of a warp are its own)
     if (has_cell)
         for (int dd = sub; dd < 9; dd += MX_LPC) cnt9[((long long)row * g.nx + cg) * 9 + dd] = dcnt[c][dd];
@@ -524,6 +612,11 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
                 az[jp][ip] += __shfl_xor_sync(FULL, az[jp][ip], o);
             }
         }
+    // (the queue is consumed by every warp: the barrier of the overflow test is behind)
+    for (int e = tid; e < 65 * 8; e += MX_THREADS) {  // zero pad columns of the partials
+        const int r = e >> 3, q = e & 7;
+        cellpj[r][q < 4 ? q : MX_TW + q] = 0.f;
+    }
     if (sub == 0) {
         const int col = c + 4;
 #pragma unroll
@@ -538,7 +631,7 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
     __syncthreads();
     // node currents of the tile footprint (5 rows x (64+4) columns): node lx takes cell lx-ip's
     // entry ip, cells ascending; pad cells are zero.  Per-tile buffer [isp][jr][tile][3][5][MX_JW].
-    float *out = jtile + ((((long long)isp * g.ny + jr) * gridDim.x + tile) * 3) * 5 * MX_JW;
+    float *out = jtile + ((((long long)isp * g.ny + jr) * ((g.nx + MX_TW - 1) / MX_TW) + tile) * 3) * 5 * MX_JW;
     for (int e = tid; e < 5 * MX_JW; e += MX_THREADS) {
         const int ly = e / MX_JW, lx = e % MX_JW;
         float sx = 0.f, sy = 0.f, sz = 0.f;
@@ -555,6 +648,37 @@ __global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
         out[e] = sx;
         out[5 * MX_JW + e] = sy;
         out[10 * MX_JW + e] = sz;
+    }
+}
+
+template <int BC, bool GATHER>  // BC = WM_BC_*: the walls' code is compiled only where it runs
+__global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
+    k_mixed_push_deposit(WmGeom g, MxConst kc, MixedView a, MixedView b, const unsigned *__restrict__ perm,
+                         const __grid_constant__ CUtensorMap fmap, const int *__restrict__ cumcnt, unsigned *__restrict__ code,
+                         int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status, unsigned *ovf)
+{
+    mx_push_tile<BC, GATHER, true>(g, kc, a, b, perm, fmap, cumcnt, code, cnt9, jtile, status, ovf, blockIdx.x, blockIdx.y, blockIdx.z, 0u);
+}
+
+// The tiles whose queue of cell-changing particles overflowed, recomputed from the same inputs
+// with every particle deposited in the loop (the same pushed particles, codes and counts, and the
+// tile's currents in full); a persistent grid over the list ovf = {count, tiles...}, which
+// finishes at once when the list is empty.
+template <int BC, bool GATHER>
+__global__ void __launch_bounds__(MX_THREADS, WM_MX_MINB)
+    k_mixed_push_redo(WmGeom g, MxConst kc, MixedView a, MixedView b, const unsigned *__restrict__ perm,
+                      const __grid_constant__ CUtensorMap fmap, const int *__restrict__ cumcnt, unsigned *__restrict__ code,
+                      int *__restrict__ cnt9, float *__restrict__ jtile, unsigned *status, const unsigned *__restrict__ ovf)
+{
+    const unsigned n = ovf[0];
+    const int ntiles = (g.nx + MX_TW - 1) / MX_TW;
+    uint32_t parity = 0;
+    for (unsigned k = blockIdx.x; k < n; k += gridDim.x) {
+        const int t = (int)ovf[1 + k];
+        const int tile = t % ntiles, rw = t / ntiles;
+        mx_push_tile<BC, GATHER, false>(g, kc, a, b, perm, fmap, cumcnt, code, cnt9, jtile, status, nullptr, tile, rw % g.ny, rw / g.ny, parity);
+        parity ^= 1u;
+        __syncthreads();
     }
 }
 
@@ -865,8 +989,10 @@ int wm_launch_mixed_fields(const WmGeom &g, FView<6, false> uf, float *fcc, cuda
     return wm_check_launch("k_mixed_fields");
 }
 
+size_t wm_mixed_ovf_words(const WmGeom &g) { return 1 + (size_t)wm_mixed_ntiles(g) * g.nrows; }
+
 int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a, MixedView b, const unsigned *perm, const float *fcc,
-                                 const int *cumcnt, const WmRebinScratch &sc, int *cnt9, float *jtile, cudaStream_t st)
+                                 const int *cumcnt, const WmRebinScratch &sc, int *cnt9, float *jtile, unsigned *ovf, cudaStream_t st)
 {
     MxConst kc;
     for (int s = 0; s < WM_MAX_SP; ++s) {
@@ -898,7 +1024,20 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
         const unsigned box[3] = {MX_FTW, 3, 6};
         WM_TRY(wm_tensor_map(&fmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, fcc, dims, strides, box));
     }
-#define WM_MX_PUSH(BCV, GV) k_mixed_push_deposit<BCV, GV><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, perm, fmap, cumcnt, code, cnt9, jtile, sc.status)
+    static int redo_blocks = 0;  // a persistent grid of one wave for the recomputed tiles
+    if (redo_blocks == 0) {
+        int dev = 0, nsm = 0;
+        WM_CUDA(cudaGetDevice(&dev));
+        WM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        redo_blocks = std::max(1, nsm * WM_MX_MINB);
+    }
+    WM_CUDA(cudaMemsetAsync(ovf, 0, sizeof(unsigned), st));
+#define WM_MX_PUSH(BCV, GV)                                                                                                      \
+    do {                                                                                                                          \
+        k_mixed_push_deposit<BCV, GV><<<grid, MX_THREADS, 0, st>>>(g, kc, a, b, perm, fmap, cumcnt, code, cnt9, jtile, sc.status, ovf); \
+        WM_TRY(wm_check_launch("k_mixed_push_deposit"));                                                                       \
+        k_mixed_push_redo<BCV, GV><<<redo_blocks, MX_THREADS, 0, st>>>(g, kc, a, b, perm, fmap, cumcnt, code, cnt9, jtile, sc.status, ovf); \
+    } while (0)
     if (g.bc == WM_BC_RECONNECTION) {
         if (perm) WM_MX_PUSH(WM_BC_RECONNECTION, true);
         else WM_MX_PUSH(WM_BC_RECONNECTION, false);
@@ -910,7 +1049,7 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
         else WM_MX_PUSH(WM_BC_PERIODIC, false);
     }
 #undef WM_MX_PUSH
-    return wm_check_launch("k_mixed_push_deposit");
+    return wm_check_launch("k_mixed_push_redo");
 }
 
 int wm_launch_mixed_incoming(const WmGeom &g, const int *cnt9, int *off9, const WmRebinScratch &sc, cudaStream_t st)

@@ -126,6 +126,7 @@ struct wm_sim {
     DevBuf A[6], B[6];
     DevBuf rowbase[2], np2[2], cumcnt, stage, uf_aos, energy_partial, energy_out, jtile, fcc, stage2;
     DevBuf cumcnt_alt, mx_cnt9, mx_off9;  // mixed path: new cumcnt, per-cell direction counts and offsets
+    DevBuf mx_ovf;                        // mixed path: tiles of the push to recompute (queue overflow)
     // Mixed path, rebin by permutation (the default): after a step, set A holds the push output
     // and slot p of the cell-sorted order is at slot mx_perm[p] of A ("permuted"), its id at slot
     // mx_idperm[idp][p] of A[5] (the ids do not move while permuted); the next push reads through
@@ -305,6 +306,7 @@ struct wm_sim {
             WM_TRY(fcc.ensure(sizeof(float) * wm_mixed_fcc_floats(g)));
             WM_TRY(cumcnt_alt.ensure(sizeof(int) * (size_t)(g.nx + 1) * g.nrows));
             WM_TRY(mx_cnt9.ensure(sizeof(int) * 9 * (size_t)g.nx * g.nrows));
+            WM_TRY(mx_ovf.ensure(sizeof(unsigned) * wm_mixed_ovf_words(g)));
             WM_TRY(mx_off9.ensure(sizeof(int) * 9 * (size_t)g.nx * g.nrows));
             if (cap < (1LL << 32)) {
                 WM_TRY(mx_perm.ensure(sizeof(unsigned) * (size_t)cap));
@@ -348,7 +350,7 @@ struct wm_sim {
     {
         size_t t = 0;
         for (int c = 0; c < 6; ++c) t += A[c].bytes + B[c].bytes;
-        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &mx_perm, &mx_idperm[0], &mx_idperm[1], &f_uf, &f_uj, &f_df, &f_pj,
+        for (const DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &mx_ovf, &mx_perm, &mx_idperm[0], &mx_idperm[1], &f_uf, &f_uj, &f_df, &f_pj,
                                 &f_b, &f_r, &f_p, &f_ap, &f_partial, &rb_dir, &rb_ord, &rb_P, &rb_key, &rb_holes, &rb_nup,
                                 &rb_ndown, &rb_cellcnt, &rb_pairs})
             t += b->bytes;
@@ -362,7 +364,7 @@ struct wm_sim {
             A[c].release();
             B[c].release();
         }
-        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &mx_perm, &mx_idperm[0], &mx_idperm[1], &stage2,
+        for (DevBuf *b : {&rowbase[0], &rowbase[1], &np2[0], &np2[1], &cumcnt, &stage, &uf_aos, &energy_partial, &energy_out, &jtile, &fcc, &cumcnt_alt, &mx_cnt9, &mx_off9, &mx_ovf, &mx_perm, &mx_idperm[0], &mx_idperm[1], &stage2,
                           &mom_dev, &out_dev, &out_cnt, &inj_rows, &inj_ninc, &inj_nptot, &inj_tmp,
                           &f_uf, &f_uj, &f_df, &f_pj, &f_b, &f_r, &f_p, &f_ap, &f_partial, &f_ticket, &f_scal, &rb_dir, &rb_ord,
                           &rb_P, &rb_key, &rb_holes, &rb_nup, &rb_ndown, &rb_cellcnt, &rb_pairs, &rb_status})
@@ -544,7 +546,7 @@ struct wm_sim {
         WM_TRY(wm_launch_mixed_fields(g, uf(), fcc.as<float>(), st));
         ++nl;
         mark("fields");
-        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, nullptr, fcc.as<float>(), cumcnt.as<int>(), sc, mx_cnt9.as<int>(), jtile.as<float>(), st));
+        WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, nullptr, fcc.as<float>(), cumcnt.as<int>(), sc, mx_cnt9.as<int>(), jtile.as<float>(), mx_ovf.as<unsigned>(), st));
         ++nl;
         mark("push_deposit");
         WM_TRY(wm_launch_mixed_jfold(g, jtile.as<float>(), uj(), st));
@@ -598,7 +600,7 @@ struct wm_sim {
         ++nl;
         mark("fields");
         WM_TRY(wm_launch_mixed_push_deposit(g, k, va, vb, gather ? mx_perm.as<unsigned>() : nullptr, fcc.as<float>(), cumcnt.as<int>(), sc,
-                                            mx_cnt9.as<int>(), jtile.as<float>(), st));
+                                            mx_cnt9.as<int>(), jtile.as<float>(), mx_ovf.as<unsigned>(), st));
         ++nl;
         mark("push_deposit");
         // The rebin needs the push's counts and codes only: destination counts, scan, row bases and
