@@ -356,10 +356,10 @@ enum { WM_CNN_FWD_TRAIN = 0, WM_CNN_FWD_INFER = 1, WM_CNN_FWD_LINEAR = 2, WM_CNN
  * over three groups of 16 channels, as in the learned guess, and only the diagonal blocks are
  * computed (the other weights must be zero; their gradient is returned as zero). */
 enum { WM_CNN_GROUPED = 16 };
-/* The convolutions (all four modes) run on the 5th-generation tensor cores (tcgen05.mma,
- * accumulators in tensor memory) when h is a multiple of 16 and w of 8; OR-ing WM_CNN_MMA_SYNC
- * into the mode selects the warp-level mma.sync kernel instead (the one other shapes and the
- * weight gradient use). */
+/* The convolutions (all four modes) and the weight gradient run on the 5th-generation tensor
+ * cores (tcgen05.mma, accumulators in tensor memory) when h is a multiple of 16 and w of 8;
+ * OR-ing WM_CNN_MMA_SYNC into the mode (or the wgrad flags) selects the warp-level mma.sync
+ * kernel instead (the one other shapes use). */
 enum { WM_CNN_MMA_SYNC = 32 };
 
 /* One 3x3 convolution, (cin, cout) in {(16, 48), (48, 48), (48, 8)}.  Modes:
@@ -376,12 +376,19 @@ int wm_cnn_conv3x3(const void *in, const void *w, const float *bias, int cin, in
 int wm_cnn_status(int clear);
 /* Weight and bias gradients dw[9][cout][cin] (FP32), db[cout] from the layer input x [.][cin] and
  * the pre-activation gradient dz [.][coutp], (cin, coutp) in {(16, 48), (48, 48), (48, 16)},
- * cout <= coutp.  scratch: at least 9*coutp*cin + coutp floats per CTA used (up to 304 CTAs). */
+ * cout <= coutp.  scratch: at least 9*coutp*cin + coutp floats per CTA used (up to 304 CTAs for
+ * mma.sync, one per SM for tcgen05; fewer CTAs are used when scratch is smaller).  A timed-out
+ * wait of the tcgen05 kernel is reported by wm_cnn_status. */
 int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int cout, int nimg, int h, int wd, int flags, float *dw,
                          float *db, float *scratch, long long scratch_floats, void *stream);
 /* *loss = sum over pixels and the 3 outputs of 0.5 (pred - target)^2 / (3 npix); dz = its gradient
  * as BF16 [npix][16].  pred FP32 [npix][8], target FP32 [npix][3]; partial holds nblocks doubles. */
 int wm_cnn_mse(const float *pred, const float *target, long long npix, void *dz, double *partial, int nblocks, double *loss, void *stream);
+/* The same over the interior of nimg images of h x w pixels: pixels within `border` of an edge are
+ * left out of the loss and get a zero gradient (training on crops of a larger field, where the
+ * network's periodic padding does not see the field's true neighbours). */
+int wm_cnn_mse_interior(const float *pred, const float *target, int nimg, int h, int wd, int border, void *dz, double *partial, int nblocks,
+                        double *loss, void *stream);
 /* One Adam step (step = 1, 2, ...) on n FP32 parameters; mask (optional, n values) multiplies the
  * gradient, so parameters with mask 0 keep their value. */
 int wm_cnn_adam(float *p, const float *grad, const float *mask, float *m, float *v, long long n, float lr, float beta1, float beta2,

@@ -124,6 +124,7 @@ SIGNATURES = {
     "wm_cnn_status": [_I],
     "wm_cnn_conv3x3_wgrad": [_P, _P, _I, _I, _I, _I, _I, _I, _I, _P, _P, _P, ctypes.c_int64, _P],
     "wm_cnn_mse": [_P, _P, ctypes.c_int64, _P, _P, _I, _P, _P],
+    "wm_cnn_mse_interior": [_P, _P, _I, _I, _I, _I, _P, _P, _I, _P, _P],
     "wm_cnn_adam": [_P, _P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, _I, _P],
     "wm_cnn_prep_weights": [_P, _I, _I, _I, _P, _P, _P],
 }

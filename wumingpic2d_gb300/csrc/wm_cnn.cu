@@ -13,10 +13,10 @@
 // Channel counts are padded to the tensor-core tile: the 9 inputs to 16, the 3 outputs to 8 (16
 // for the output gradient), with zero weights on the padding.
 //
-// The convolutions (forward and input gradient) run on the 5th-generation tensor cores (tcgen05.mma,
-// wm_cnn_tc.cu) when the image is a multiple of 16 x 8 pixels.  The kernels here use
-// mma.sync.m16n8k16 BF16 with FP32 accumulation, operands staged in shared memory and read with
-// ldmatrix: the weight gradient, other shapes, and the convolutions on request (WM_CNN_MMA_SYNC, the
+// The convolutions (forward and input gradient) and the weight gradient run on the 5th-generation
+// tensor cores (tcgen05.mma, wm_cnn_tc.cu) when the image is a multiple of 16 x 8 pixels.  The
+// kernels here use mma.sync.m16n8k16 BF16 with FP32 accumulation, operands staged in shared memory
+// and read with ldmatrix: other shapes, and every convolution on request (WM_CNN_MMA_SYNC, the
 // cross-check of the tcgen05 kernels).  A CTA computes an 8 x 16 pixel tile for all output channels; it keeps
 // the layer's weights resident in shared memory and walks over tiles (persistent grid).
 #include <algorithm>
@@ -279,16 +279,23 @@ __global__ void k_reduce_wgrad(const float *__restrict__ part, int nparts, int c
 
 // Loss 0.5/count * sum (pred - target)^2 over the three real output channels; dz = dL/dpred as
 // BF16 [p][16] (zeros on the padding).  Per-block partial sums, then one block adds them in order.
-__global__ void k_mse(const float *__restrict__ pred, const float *__restrict__ target, long long npix, float scale,
+// border > 0: the pixels within `border` of an image edge ([.][H][W] images) are left out of the
+// loss and get dz = 0 (crops of a larger field, whose periodic padding is not the field's).
+__global__ void k_mse(const float *__restrict__ pred, const float *__restrict__ target, long long npix, int H, int W, int border, float scale,
                       __nv_bfloat16 *__restrict__ dz, double *__restrict__ partial)
 {
     __shared__ double red[256];
     double s = 0.0;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npix; p += (long long)gridDim.x * blockDim.x) {
+        bool in = true;
+        if (border > 0) {
+            const int x = (int)(p % W), y = (int)((p / W) % H);
+            in = x >= border && x < W - border && y >= border && y < H - border;
+        }
         float e[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            e[c] = pred[p * 8 + c] - target[p * 3 + c];
+            e[c] = in ? pred[p * 8 + c] - target[p * 3 + c] : 0.f;
             s += (double)e[c] * e[c];
         }
         const __nv_bfloat162 e01 = __floats2bfloat162_rn(scale * e[0], scale * e[1]);
@@ -585,6 +592,16 @@ int wm_cnn_conv3x3_wgrad(const void *x, const void *dz, int cin, int coutp, int 
 {
     if (!x || !dz || !dw || !db || !scratch || !shape_ok(nimg, h, wd) || cout < 1 || cout > coutp) return WM_ERR_BAD_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const bool shape_tc = (cin == 16 && coutp == 48) || (cin == 48 && (coutp == 48 || coutp == 16));
+    if (!(flags & WM_CNN_MMA_SYNC) && shape_tc && wm_cnn_tc_shape_ok(nimg, h, wd)) {  // tensor cores (tcgen05)
+        unsigned *status = cnn_status_word();
+        if (!status) return WM_ERR_CUDA;
+        int nparts = 0;
+        WM_TRY(wm_cnn_wgrad_tc(x, dz, cin, coutp, (flags & WM_CNN_GROUPED) != 0, nimg, h, wd, scratch, scratch_floats, &nparts, status, st));
+        const int nout = 9 * cout * cin + cout;
+        k_reduce_wgrad<<<(nout + 255) / 256, 256, 0, st>>>(scratch, nparts, cin, coutp, cout, dw, db);
+        return wm_check_launch("k_reduce_wgrad");
+    }
     if ((flags & WM_CNN_GROUPED) && cin == 48 && coutp == 48)
         return launch_wgrad<48, 48, true>(x, dz, nimg, h, wd, cout, dw, db, scratch, scratch_floats, st);
     if (cin == 16 && coutp == 48) return launch_wgrad<16, 48>(x, dz, nimg, h, wd, cout, dw, db, scratch, scratch_floats, st);
@@ -598,7 +615,21 @@ int wm_cnn_mse(const float *pred, const float *target, long long npix, void *dz,
     if (!pred || !target || !dz || !partial || !loss || npix <= 0 || nblocks < 1) return WM_ERR_BAD_ARG;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const double count = 3.0 * (double)npix;
-    k_mse<<<nblocks, 256, 0, st>>>(pred, target, npix, (float)(1.0 / count), static_cast<__nv_bfloat16 *>(dz), partial);
+    k_mse<<<nblocks, 256, 0, st>>>(pred, target, npix, 1, 1, 0, (float)(1.0 / count), static_cast<__nv_bfloat16 *>(dz), partial);
+    WM_TRY(wm_check_launch("k_mse"));
+    k_sum_in_order<<<1, 32, 0, st>>>(partial, nblocks, 0.5 / count, loss);
+    return wm_check_launch("k_sum_in_order");
+}
+
+int wm_cnn_mse_interior(const float *pred, const float *target, int nimg, int h, int wd, int border, void *dz, double *partial, int nblocks,
+                        double *loss, void *stream)
+{
+    if (!pred || !target || !dz || !partial || !loss || nimg < 1 || border < 0 || h <= 2 * border || wd <= 2 * border || nblocks < 1)
+        return WM_ERR_BAD_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const long long npix = (long long)nimg * h * wd;
+    const double count = 3.0 * (double)nimg * (h - 2 * border) * (wd - 2 * border);
+    k_mse<<<nblocks, 256, 0, st>>>(pred, target, npix, h, wd, border, (float)(1.0 / count), static_cast<__nv_bfloat16 *>(dz), partial);
     WM_TRY(wm_check_launch("k_mse"));
     k_sum_in_order<<<1, 32, 0, st>>>(partial, nblocks, 0.5 / count, loss);
     return wm_check_launch("k_sum_in_order");

@@ -1,7 +1,8 @@
-// wm_cnn_tc.cu -- the forward 3x3 convolutions of the learned CG guess (cout = 48) on the
-// 5th-generation tensor cores: tcgen05.mma with both operands in shared memory and the FP32
-// accumulator in tensor memory (TMEM), read back with tcgen05.ld for the epilogue (bias + GELU, or
-// GELU' for the input gradient of training).
+// wm_cnn_tc.cu -- the 3x3 convolutions of the learned CG guess on the 5th-generation tensor cores:
+// tcgen05.mma with both operands in shared memory and the FP32 accumulator in tensor memory (TMEM),
+// read back with tcgen05.ld for the epilogue (bias + GELU, or GELU' for the input gradient of
+// training).  The forward and input-gradient convolutions are described here; the weight gradient
+// (k_conv3x3_wgrad_tc) further down.
 //
 // Implicit GEMM per CTA tile of 16 rows x 8 pixels: M = 128 pixels, N = 48 output channels,
 // K = 9 taps x cin, one tcgen05.mma (M128 N48 K16) per tap and 16 input channels.  The tile's
@@ -34,8 +35,10 @@ constexpr int TC_HW = TC_TW + 2, TC_HPIX = (TC_TH + 2) * TC_HW;  // halo 18 x 10
 constexpr int TC_XP = 184;  // pixels per channel-group plane: 180 used, 2944 bytes keeps planes 128-byte aligned for TMA
 constexpr uint32_t TC_SPIN = 1u << 22;                // mbarrier polls before giving up
 
-// no-swizzle K-major shared-memory matrix descriptor: start address, leading (K-direction) and
-// stride (M/N-direction) byte offsets between 8 x 16-byte core matrices, descriptor version 1
+// no-swizzle shared-memory matrix descriptor: start address, leading (K-direction) and stride
+// (M/N-direction) byte offsets between 8 x 16-byte core matrices, descriptor version 1.  The same
+// fields serve K-major operands (a core-matrix row = 8 K elements) and MN-major ones (a row = 8 M
+// or N elements, the instruction descriptor's transpose bits set).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
 {
     return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) | ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) |
@@ -310,7 +313,198 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
     return wm_check_launch("k_conv3x3_tc");
 }
 
+// Weight gradient of training on tcgen05: dW(tap, co, ci) = sum_p dz(p, co) x(p + d_tap, ci) and
+// db(co) = sum_p dz(p, co), p over every pixel of every image.  A GEMM per tap with K = pixels:
+// D[co][ci] += A[co][k] B[ci][k] with A = dz^T and B = the shifted input x^T, both taken from
+// shared memory in the MN-major layout (8 channels of one pixel form a 16-byte core-matrix row,
+// 8 pixels = one tile row form the 8 K rows of a core matrix), so the NHWC data is staged as it
+// lies, without a transpose:
+//   dz of the tile's 128 pixels as [channel group][pixel][8]: the M (co) direction steps one
+//     channel group (2048 bytes), the K direction one tile row (128 bytes);
+//   the input halo as [halo row][channel group][halo column][8]: the N direction (ci) steps one
+//     channel group (160 bytes), and since a halo row holds every channel group, the next tap
+//     row (dy + 1) is the next N block at the same stride, so one MMA covers the three taps of a
+//     column dx (N = 3 cin); the K direction steps one halo row.
+// The shift of tap (dy, dx) is a start address moved by whole 16-byte rows.  M = 128 rows of
+// co: rows past coutp read whatever the shared memory holds beyond the staged channels, and their
+// accumulator lanes are never read (every D row depends on its own A row only).  Three FP32
+// accumulators in tensor memory (dx = -1, 0, 1; 3 cin columns each) sum the CTA's tiles; the
+// next tile is staged into the other buffer while the current tile's 24 MMAs (8 K steps of 16
+// pixels x 3 dx) run.  Per-CTA partials [cta][9][coutp][cin] + [coutp] as k_conv3x3_wgrad writes
+// them; k_reduce_wgrad sums them in CTA order.  Waits are bounded (WMDEV_TIMEOUT, TMEM freed).
+constexpr uint32_t WG_MARGIN = 32768;  // shared memory past the buffers: the M = 128 rows of the A operand stay inside it
+template <int CIN, int COUTP, bool GROUPED>
+__global__ void __launch_bounds__(128, 1) k_conv3x3_wgrad_tc(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ dz, int nimg,
+                                                             int H, int W, float *__restrict__ part, unsigned *status)
+{
+    constexpr int KG = CIN / 8, DG = COUTP / 8;
+    constexpr int N3 = 3 * CIN;                         // one accumulator: taps dy = -1, 0, 1 x cin, for one dx
+    constexpr uint32_t TCOLS = 9 * CIN > 256 ? 512 : 256;  // TMEM columns (a power of 2 >= 9 cin)
+    constexpr uint32_t ROW = KG * TC_HW * 16;           // bytes per halo row
+    constexpr uint32_t XB = (TC_TH + 2) * ROW;          // one halo buffer
+    constexpr uint32_t DB = DG * 2048;                  // one dz buffer: DG groups x 128 pixels x 16 bytes
+    // kind::f16: FP32 D, BF16 A and B, both MN-major (bits 15, 16), N = 3 cin, M = 128
+    constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) | ((uint32_t)(N3 >> 3) << 17) |
+                               ((uint32_t)(128 >> 4) << 24);
+    static_assert(N3 % 16 == 0 && N3 <= 256, "N of an M = 128 MMA");
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *dz_s = smem_raw;                              // [2][DG][128][8] BF16
+    unsigned char *x_s = smem_raw + 2 * DB;                      // [2][18][KG][10][8] BF16
+    uint64_t *bars = reinterpret_cast<uint64_t *>(x_s + 2 * XB);  // MMA completion of buffer 0, 1
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)), "r"(TCOLS) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bars + b)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = *tslot;
+
+    const int ntx = W / TC_TW, nty = H / TC_TH;
+    const long long ntiles = (long long)nimg * nty * ntx;
+    auto stage = [&](long long t, int b) {
+        const int n = (int)(t / ((long long)nty * ntx));
+        const int rem = (int)(t % ((long long)nty * ntx));
+        const int y0 = (rem / ntx) * TC_TH, x0 = (rem % ntx) * TC_TW;
+        unsigned char *xb = x_s + b * XB;
+        for (int e = tid; e < TC_HPIX * KG; e += 128) {  // periodic halo, [halo row][group][column][8]
+            const int kg = e % KG, pix = e / KG, hy = pix / TC_HW, hx = pix % TC_HW;
+            int yy = y0 - 1 + hy, xx = x0 - 1 + hx;
+            yy += (yy < 0) ? H : (yy >= H ? -H : 0);
+            xx += (xx < 0) ? W : (xx >= W ? -W : 0);
+            *reinterpret_cast<uint4 *>(xb + hy * ROW + kg * (TC_HW * 16) + hx * 16) =
+                *reinterpret_cast<const uint4 *>(x + (((long long)n * H + yy) * W + xx) * CIN + kg * 8);
+        }
+        unsigned char *db = dz_s + b * DB;
+        for (int e = tid; e < 128 * DG; e += 128) {  // the tile's pixels p = 8 r + c, [group][p][8]
+            const int g = e % DG, p = e / DG;
+            *reinterpret_cast<uint4 *>(db + g * 2048 + p * 16) =
+                *reinterpret_cast<const uint4 *>(dz + (((long long)n * H + y0 + (p >> 3)) * W + x0 + (p & 7)) * COUTP + g * 8);
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the staged tile, seen by the tensor core
+    };
+    float dbias = 0.f;
+    auto bias_sum = [&](int b) {  // db(co) over the tile's pixels, in pixel order
+        if (tid < COUTP) {
+            const __nv_bfloat16 *d = reinterpret_cast<const __nv_bfloat16 *>(dz_s + b * DB + (tid >> 3) * 2048) + (tid & 7);
+            for (int p = 0; p < 128; ++p) dbias += __bfloat162float(d[p * 8]);
+        }
+    };
+
+    uint32_t ph = 0u;  // bit b: phase of buffer b's MMA barrier
+    long long tile = blockIdx.x;
+    int it = 0;
+    int ncommit = 0;                  // tiles whose MMAs were issued (one commit each)
+    bool fail = false, stop = false;  // this thread's wait gave up; some thread's did (block-uniform)
+    if (tile < ntiles) stage(tile, 0);
+    __syncthreads();
+    if (tile < ntiles) bias_sum(0);
+    for (; tile < ntiles; tile += gridDim.x, ++it) {
+        const int b = it & 1;
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t da = saddr(dz_s + b * DB), xa = saddr(x_s + b * XB);
+#pragma unroll
+            for (int s = 0; s < TC_TH / 2; ++s) {  // K step s: tile rows 2s, 2s+1 (16 pixels)
+                const uint64_t ad = smem_desc(da + (uint32_t)(s * 256), 128, 2048);
+#pragma unroll
+                for (int dxi = 0; dxi < 3; ++dxi) {
+                    const uint64_t bd = smem_desc(xa + (uint32_t)(2 * s * ROW + dxi * 16), ROW, TC_HW * 16);
+                    mma_f16(tmem + (uint32_t)(dxi * N3), ad, bd, IDESC, (it | s) != 0 ? 1u : 0u);
+                }
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(bars + b)) : "memory");
+        }
+        ncommit = it + 1;
+        const long long nt = tile + gridDim.x;
+        if (nt < ntiles) {
+            if (it >= 1) {  // the previous tile's MMAs read the other buffer
+                fail = !mbar_wait(saddr(bars + (b ^ 1)), (ph >> (b ^ 1)) & 1u);
+                ph ^= 1u << (b ^ 1);
+            }
+            if (!fail) stage(nt, b ^ 1);
+        }
+        stop = __syncthreads_or(fail) != 0;
+        if (stop) break;
+        if (nt < ntiles) bias_sum(b ^ 1);
+    }
+    const int last = (ncommit - 1) & 1;  // the last commit covers every MMA issued before it
+    if (!stop && ncommit > 0) stop = __syncthreads_or(!mbar_wait(saddr(bars + last), (ph >> last) & 1u)) != 0;
+    if (stop) {  // the MMAs still in flight (bounded) before the TMEM goes; the partials are not written
+        if (tid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
+        if (ncommit > 0) mbar_wait(saddr(bars + last), (ph >> last) & 1u);
+    }
+    const bool ok = !stop;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    float *pw = part + (long long)blockIdx.x * (9 * COUTP * CIN + COUTP);
+    if (ok && warp * 32 < COUTP) {  // warp w reads TMEM lanes (co) 32w .. 32w+31
+        const int co = warp * 32 + lane;
+#pragma unroll 1
+        for (int q = 0; q < 9 * CIN / 16; ++q) {
+            float v[16];
+            tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(16 * q), v);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            const int col = 16 * q, dxi = col / N3, dyi = (col % N3) / CIN, ci0 = col % CIN;
+            const int tap = dyi * 3 + dxi;
+            if (co < COUTP) {
+                float *o = pw + ((long long)tap * COUTP + co) * CIN + ci0;
+#pragma unroll
+                for (int i = 0; i < 16; i += 4) {
+                    float4 w4 = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                    if (GROUPED && (co >> 4) != ((ci0 + i) >> 4)) w4 = make_float4(0.f, 0.f, 0.f, 0.f);  // off-block: zero
+                    *reinterpret_cast<float4 *>(o + i) = w4;
+                }
+            }
+        }
+    }
+    if (tid < COUTP) pw[9 * COUTP * CIN + tid] = dbias;
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TCOLS) : "memory");
+}
+
+template <int CIN, int COUTP, bool GROUPED>
+int launch_wgrad_tc(const void *x, const void *dz, int nimg, int H, int W, float *part, long long part_floats, int *nparts, unsigned *status,
+                    cudaStream_t st)
+{
+    constexpr uint32_t DB = (COUTP / 8) * 2048, XB = (TC_TH + 2) * (CIN / 8) * TC_HW * 16;
+    const size_t smem = 2 * (size_t)DB + 2 * (size_t)XB + 64 + WG_MARGIN;
+    WM_CUDA(cudaFuncSetAttribute(k_conv3x3_wgrad_tc<CIN, COUTP, GROUPED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        WM_CUDA(cudaGetDevice(&dev));
+        WM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    }
+    const long long ntiles = (long long)nimg * (H / TC_TH) * (W / TC_TW);
+    const long long per = 9LL * COUTP * CIN + COUTP;
+    const int grid = (int)std::min<long long>(std::min<long long>(ntiles, nsm), part_floats / per);
+    if (grid < 1) return WM_ERR_BAD_ARG;
+    k_conv3x3_wgrad_tc<CIN, COUTP, GROUPED><<<grid, 128, smem, st>>>(static_cast<const __nv_bfloat16 *>(x), static_cast<const __nv_bfloat16 *>(dz),
+                                                                     nimg, H, W, part, status);
+    *nparts = grid;
+    return wm_check_launch("k_conv3x3_wgrad_tc");
+}
+
 }  // namespace
+
+int wm_cnn_wgrad_tc(const void *x, const void *dz, int cin, int coutp, bool grouped, int nimg, int h, int wd, float *part, long long part_floats,
+                    int *nparts, unsigned *status, cudaStream_t st)
+{
+    if (!wm_cnn_tc_shape_ok(nimg, h, wd) || !status || !nparts) return WM_ERR_BAD_ARG;
+    if (grouped && cin == 48 && coutp == 48) return launch_wgrad_tc<48, 48, true>(x, dz, nimg, h, wd, part, part_floats, nparts, status, st);
+    if (cin == 16 && coutp == 48) return launch_wgrad_tc<16, 48, false>(x, dz, nimg, h, wd, part, part_floats, nparts, status, st);
+    if (cin == 48 && coutp == 48) return launch_wgrad_tc<48, 48, false>(x, dz, nimg, h, wd, part, part_floats, nparts, status, st);
+    if (cin == 48 && coutp == 16) return launch_wgrad_tc<48, 16, false>(x, dz, nimg, h, wd, part, part_floats, nparts, status, st);
+    return WM_ERR_UNSUPPORTED;
+}
 
 int wm_tensor_map(CUtensorMap *map, CUtensorMapDataType type, int rank, const void *base, const unsigned long long *dims,
                   const unsigned long long *strides, const unsigned *box)

@@ -364,48 +364,99 @@ struct PlaneView {
     }
 };
 
-// |b - A x|^2 per component for a candidate initial guess x (the residual of k_cg_resid).
-template <class V>
-__global__ void __launch_bounds__(CG_THREADS) k_guess_resid(WmGeom g, FieldK fk, V x, const double *__restrict__ b, double *partial,
-                                                            unsigned *ticket, double *out3)
+// |b - A x|^2 per component for both initial guesses in one pass over b: the network's candidate
+// (cand, [3][nx*ny]) into out6[0..2] and the previous step's dB (df) into out6[3..5] (the residual
+// of k_cg_resid).  Six partials per CTA, summed in CTA order by the last CTA.
+template <class FV6>
+__global__ void __launch_bounds__(CG_THREADS) k_guess_resid2(WmGeom g, FieldK fk, PlaneView cand, FV6 df, const double *__restrict__ b,
+                                                             double *partial, unsigned *ticket, double *out6)
 {
+    __shared__ bool is_last;
     const long long ncell = (long long)g.nx * g.ny;
-    double acc[3] = {0.0, 0.0, 0.0};
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (GridCell q(g.nx); q.e < ncell; q.next()) {
         const long long e = q.e;
         const int ci = q.c, cj = q.r;
         const int ym = wrapm(cj - 1, g.ny) + 2, yp = wrapm(cj + 1, g.ny) + 2, xx = ci + 2, yy = cj + 2;
 #pragma unroll
         for (int l = 0; l < 3; ++l) {
+            const double bl = b[l * ncell + e];
             double xl, xr;
-            x_neighbours(g, l, ci, [&](int c) { return x(l, c + 2, yy); }, xl, xr);
-            const double rv = b[l * ncell + e] + x(l, xx, ym) + xl - fk.f4 * x(l, xx, yy) + xr + x(l, xx, yp);
-            acc[l] += rv * rv;
+            x_neighbours(g, l, ci, [&](int c) { return cand(l, c + 2, yy); }, xl, xr);
+            const double rc = bl + cand(l, xx, ym) + xl - fk.f4 * cand(l, xx, yy) + xr + cand(l, xx, yp);
+            x_neighbours(g, l, ci, [&](int c) { return df(l, c + 2, yy); }, xl, xr);
+            const double rp = bl + df(l, xx, ym) + xl - fk.f4 * df(l, xx, yy) + xr + df(l, xx, yp);
+            acc[l] += rc * rc;
+            acc[3 + l] += rp * rp;
         }
     }
-    double tot[3];
-    if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot))
-        for (int l = 0; l < 3; ++l) out3[l] = tot[l];
+    block_sum3(acc[0], acc[1], acc[2]);
+    block_sum3(acc[3], acc[4], acc[5]);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) partial[k * gridDim.x + blockIdx.x] = acc[k];
+        __threadfence();
+        is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    double t[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) t[k] += __ldcg(&partial[k * gridDim.x + i]);
+    block_sum3(t[0], t[1], t[2]);
+    block_sum3(t[3], t[4], t[5]);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) out6[k] = t[k];
+        *ticket = 0u;
+    }
 }
 
-// Start each component from the candidate where its residual is the smaller one.
+// k_cg_resid for a solve that starts from the better of two guesses: component l starts from the
+// network's candidate where its residual (stats[l]) is below the previous step's (stats[3 + l]),
+// which is then copied into df(l); the residual, p and ||r||^2 are those of k_cg_resid on the
+// chosen start.  A component reads only cand or only df, so the copy races with no read.
+// stats[6 + l] = 1 where the candidate was taken, stats[9 + l] = ||b_l||^2.
 template <class FV6>
-__global__ void k_guess_pick(WmGeom g, FV6 df, const double *__restrict__ cand, const CgScal *scal, double *stats)
+__global__ void __launch_bounds__(CG_THREADS) k_cg_resid_pick(WmGeom g, FieldK fk, FV6 df, PlaneView cand, const double *__restrict__ b,
+                                                              double *__restrict__ r, double *__restrict__ p, double *partial,
+                                                              unsigned *ticket, CgScal *scal, double *stats)
 {
     const long long ncell = (long long)g.nx * g.ny;
     bool take[3];
 #pragma unroll
     for (int l = 0; l < 3; ++l) take[l] = stats[l] < stats[3 + l];
-    if (blockIdx.x == 0 && threadIdx.x < 3) {
-        stats[6 + threadIdx.x] = take[threadIdx.x] ? 1.0 : 0.0;
-        stats[9 + threadIdx.x] = scal[threadIdx.x].sum_g;
-    }
+    double acc[3] = {0.0, 0.0, 0.0};
     for (GridCell q(g.nx); q.e < ncell; q.next()) {
         const long long e = q.e;
-        const int ix = q.c + 2, iy = q.r + 2;
+        const int ci = q.c, cj = q.r;
+        const int ym = wrapm(cj - 1, g.ny) + 2, yp = wrapm(cj + 1, g.ny) + 2, x = ci + 2, y = cj + 2;
 #pragma unroll
-        for (int l = 0; l < 3; ++l)
-            if (take[l]) df(l, ix, iy) = cand[l * ncell + e];
+        for (int l = 0; l < 3; ++l) {
+            const bool tk = take[l];
+            auto at = [&](int ix, int iy) { return tk ? cand(l, ix, iy) : df(l, ix, iy); };
+            double xl, xr;
+            x_neighbours(g, l, ci, [&](int c) { return at(c + 2, y); }, xl, xr);
+            const double centre = at(x, y);
+            const double rv = b[l * ncell + e] + at(x, ym) + xl - fk.f4 * centre + xr + at(x, yp);
+            if (tk) df(l, x, y) = centre;
+            r[l * ncell + e] = rv;
+            p[l * ncell + e] = rv;
+            acc[l] += rv * rv;
+        }
+    }
+    double tot[3];
+    if (last_block_reduce3(acc[0], acc[1], acc[2], partial, ticket, tot)) {
+        for (int l = 0; l < 3; ++l) {
+            scal[l].sumr = tot[l];
+            scal[l].ite = 0;
+            scal[l].status = 0;
+            scal[l].active = (sqrt(tot[l]) > scal[l].eps) && (scal[l].sum_g > scal[l].eps);
+            stats[6 + l] = take[l] ? 1.0 : 0.0;
+            stats[9 + l] = scal[l].sum_g;
+        }
     }
 }
 
@@ -642,14 +693,16 @@ int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<
         WM_TRY(guess->run(guess->ctx, st));
         M("guess_net");
         const PlaneView cv{guess->cand, g.nx, g.ny};
-        k_guess_resid<PlaneView><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, cv, w.b, w.partial, w.ticket, guess->stats);
-        k_guess_resid<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.b, w.partial, w.ticket, guess->stats + 3);
-        k_guess_pick<FView<6, false>><<<grid_for((long long)g.nx * g.ny, 256), 256, 0, st>>>(g, df, guess->cand, w.scal, guess->stats);
-        WM_TRY(wm_check_launch("k_guess_pick"));
-        nl += 3;
+        k_guess_resid2<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, cv, df, w.b, w.partial, w.ticket, guess->stats);
+        WM_TRY(wm_check_launch("k_guess_resid2"));
+        k_cg_resid_pick<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, cv, w.b, w.r, w.p, w.partial, w.ticket, w.scal,
+                                                                            guess->stats);
+        WM_TRY(wm_check_launch("k_cg_resid_pick"));
+        nl += 1;
+    } else {
+        k_cg_resid<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.b, w.r, w.p, w.partial, w.ticket, w.scal);
+        WM_TRY(wm_check_launch("k_cg_resid"));
     }
-    k_cg_resid<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.b, w.r, w.p, w.partial, w.ticket, w.scal);
-    WM_TRY(wm_check_launch("k_cg_resid"));
     nl += 2;
     M("cg_setup");
     // cg_batch iterations (3 launches each) between host checks of the "still iterating" flags;

@@ -150,6 +150,10 @@ int wm_tensor_map(CUtensorMap *map, CUtensorMapDataType type, int rank, const vo
 bool wm_cnn_tc_shape_ok(int nimg, int H, int W);
 int wm_cnn_conv3x3_tc(const void *in, const void *w, const float *bias, int cin, int cout, int mode, int nimg, int h, int wd, void *out,
                       void *zout, const void *zprev, unsigned *status, cudaStream_t st);
+// the weight gradient on tcgen05, (cin, coutp) = (16, 48), (48, 48), (48, 16): per-CTA partials
+// [cta][9][coutp][cin] + [coutp] into part (*nparts CTAs, at most the SM count), summed by the caller
+int wm_cnn_wgrad_tc(const void *x, const void *dz, int cin, int coutp, bool grouped, int nimg, int h, int wd, float *part, long long part_floats,
+                    int *nparts, unsigned *status, cudaStream_t st);
 
 // wm_paraio.cu: the resident state in the order of the paraio files
 int wm_launch_mom_file(const WmGeom &g, const double *mom, FView<6, false> uf, double *out, cudaStream_t st);

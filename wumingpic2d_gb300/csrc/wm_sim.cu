@@ -327,7 +327,7 @@ struct wm_sim {
         WM_TRY(f_r.ensure(sizeof(double) * 3 * nc));
         WM_TRY(f_p.ensure(sizeof(double) * 3 * nc));
         WM_TRY(f_ap.ensure(sizeof(double) * 3 * nc));
-        WM_TRY(f_partial.ensure(sizeof(double) * 3 * wm_field_cg_blocks()));
+        WM_TRY(f_partial.ensure(sizeof(double) * 6 * wm_field_cg_blocks()));  // 6 sums: the two guesses' residuals
         WM_TRY(f_ticket.ensure(sizeof(unsigned)));
         WM_CUDA(cudaMemsetAsync(f_ticket.p, 0, sizeof(unsigned), st));
         WM_TRY(f_scal.ensure(wm_field_scal_bytes()));
