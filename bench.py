@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--rebin", default="permute", choices=["permute", "move"],
                    help="mixed path: the next push reads through the new order (permute) or the particles are moved every step")
     p.add_argument("--cnn-steps", type=int, default=5, help="repetitions of the network-alone leg (0 skips it)")
+    p.add_argument("--standalone-pairs", type=int, default=20000,
+                   help="training crops of the learned guess's standalone 4096^2 workload (0 skips the leg)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     return p.parse_args()
@@ -316,6 +318,21 @@ def shock_leg(args):
             "cg_iters_last_step": iters}
 
 
+def guess_standalone_leg(args):
+    """The learned guess on its own workload (wumingpic2d_gb300.guess_standalone): the implicit field
+    system of a 4096 x 4096 periodic Weibel plasma solved to 1e-10 from the previous step's dB and
+    from the network's guess, the network trained here on 20k solver-generated crops from runs of
+    the 2048^2 Weibel and 4096 x 2048 Harris workloads; iterations and time both ways, training and
+    inference throughput, and the break-even of the guess."""
+    if args.standalone_pairs <= 0:
+        return None
+    from wumingpic2d_gb300 import guess_standalone
+
+    r = guess_standalone.run(pairs=args.standalone_pairs, seed=args.seed)
+    r.pop("params")
+    return r
+
+
 def cnn_leg(args):
     """The learned guess's network alone: inference on one 4096 x 4096 image (its forward layers
     on the tcgen05 tensor cores) and training steps (forward, MSE, input and weight gradients, Adam)
@@ -362,7 +379,7 @@ def cnn_leg(args):
                           "tflops_dense": round(tflops, 1), "frac_of_bf16_peak": round(tflops / peaks["bf16_tflops"], 4),
                           "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops)", "kernels": "tcgen05 (forward layers)"},
             "training": {"batch": "8 x 512 x 512", "ms_per_step": round(ms_tr, 3), "pixels_per_s": 8 * 512 * 512 / (ms_tr / 1e3),
-                         "kernels": "forward and input gradient on tcgen05; weight gradient on mma.sync"},
+                         "kernels": "forward, input gradient and weight gradient on tcgen05"},
             "steps": args.cnn_steps}
 
 
@@ -609,6 +626,9 @@ def main():
         sh = shock_leg(args) if head == "mixed" else None
         if sh is not None:
             line["shock"] = sh
+        sa = guess_standalone_leg(args) if head == "mixed" else None
+        if sa:
+            line["guess_standalone"] = sa
         cl = cnn_leg(args) if head == "mixed" else None
         if cl is not None:
             line["cnn"] = cl

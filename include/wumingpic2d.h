@@ -219,7 +219,8 @@ int wm_sim_read_snapshot(wm_sim *s, const char *dir, const char *filename, int *
  *   harris  proj/reconnection/app.f90:353-470 (bc = WM_BC_RECONNECTION): nbg background and ncs
  *           sheet particles per cell, half-thickness lcs (cells), field b0, perturbation e1,
  *           thermal speeds vte/vti, temperature ratio rtemp = Te/Ti (drifts split by it)
- *   shock   proj/shock/app.f90:408-525 (bc = WM_BC_SHOCK) with the box at full size: n0 per cell,
+ *   shock   proj/shock/app.f90:408-525 (bc = WM_BC_SHOCK) over cells nxs+1 .. nxe-1 (nxe = nxge
+ *           unless wm_sim_set_expansion set a smaller box): n0 per cell,
  *           upstream four-velocity u0 (< 0), field b0 at angles theta_bn/phi_bn, damping length
  *           l_damp_ini, tracer window [xrs, xre] (positive ids) */
 int wm_sim_init_weibel(wm_sim *s, int ppc, double v_drift, double vth_e, double vth_i, uint64_t seed);
@@ -228,7 +229,7 @@ int wm_sim_init_harris(wm_sim *s, int nbg, int ncs, double lcs, double b0, doubl
 int wm_sim_init_shock(wm_sim *s, int n0, double u0, double vth_e, double vth_i, double b0, double theta_bn, double phi_bn,
                       double l_damp_ini, double xrs, double xre, uint64_t seed);
 /* Particle injection of the shock application (proj/shock/app.f90:695-850; bc = WM_BC_SHOCK,
- * box at full size): every step, after the sort, nginj = int(pflux) particles per species (one
+ * at the active nxe): every step, after the sort, nginj = int(pflux) particles per species (one
  * more with probability frac(pflux)), pflux = n0 |v0| dt dx ny, v0 = u0/gamma0 from the
  * configuration's u0, enter behind the rows -- nginj/ny per row, one more in nginj mod ny rows
  * drawn at random -- at x = nxe dx + (k+1/2)/n_j |v0| dt moved by (v0 + u_x) dt, Maxwellian
@@ -240,6 +241,18 @@ int wm_sim_init_shock(wm_sim *s, int n0, double u0, double vth_e, double vth_i, 
  * capacity injects nothing and returns WM_ERR_OVERFLOW. */
 int wm_sim_set_injection(wm_sim *s, int on, int n0, double vth_e, double vth_i, double b0, double theta_bn, double phi_bn,
                          double l_damp_ini, uint64_t seed);
+/* The shock application's expanding box (proj/shock/app.f90:277, :123-125, relocate :613-690;
+ * bc = WM_BC_SHOCK): nxe = nxgs + n_x_ini (3 <= n_x_ini <= nx - 1) instead of nxge, set before
+ * wm_sim_init_shock (whose plasma then fills nxs+1 .. nxe-1).  The particles, the injection
+ * boundary at nxe and the field solve (nxs..nxe, field.f90:319-461; the fields past nxe + 1 keep
+ * their values) follow nxe.  Every intvl_expand steps (0: never), after the injection, nxe grows by
+ * one cell while nxe < nxge: n0 (the injection's) particles per row and species enter the new cell
+ * nxe-1 at x = (nxe-1 + (k+1/2)/n0) dx, y = (j + U) dx, Maxwellian boosted by vprofile, ids
+ * negative after the species' count; np2 and cumcnt(nxe) grow by n0; the upstream field is set in
+ * columns nxe-1 and nxe.  The draws are Philox, keyed by the injection's seed and counted by the
+ * step number.  A snapshot stores nxe and a read restores it. */
+int wm_sim_set_expansion(wm_sim *s, int n_x_ini, int intvl_expand);
+int wm_sim_get_nxe(wm_sim *s, int *nxe);
 int wm_sim_set_step(wm_sim *s, int64_t it);
 int wm_sim_get_step(wm_sim *s, int64_t *it);
 int wm_sim_write_moments(wm_sim *s, const char *dir, int it);

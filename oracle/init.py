@@ -22,7 +22,7 @@ import numpy as np
 M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
 W0, W1 = 0x9E3779B9, 0xBB67AE85
 MASK = np.uint64(0xFFFFFFFF)
-TAG = {"weibel": 1, "harris": 2, "shock": 3, "inject": 4}
+TAG = {"weibel": 1, "harris": 2, "shock": 3, "inject": 4, "expand": 6}
 
 
 def philox4x32_10(c0, c1, c2, c3, k0, k1):
@@ -150,8 +150,9 @@ def vprofile(x, v0, l_damp_ini, nxgs, delx=1.0):
 
 
 def shock(d, n0, u0, vth_e, vth_i, b0, theta_bn, phi_bn, l_damp_ini, xrs, xre, seed, c=1.0, delx=1.0):
-    """proj/shock/app.f90:408-525 with nxs = nxgs, nxe = nxge (the full box)."""
-    nxs, nxe = d.nxgs, d.nxge
+    """proj/shock/app.f90:408-525 with nxs = nxgs and nxe = d.nxe (nxge, or nxgs + n_x_ini for the
+    expanding box of app.f90:277); the fields over the whole box (:416-426)."""
+    nxs, nxe = d.nxgs, d.nxe
     n_row = n0 * (nxe - nxs - 1)  # app.f90:335
     i, jr, idx = _rows(d, n_row)
     t = TAG["shock"]
@@ -213,8 +214,8 @@ def inject_counts(seed, it, pflux, ny):
 def inject(d, up, uf, np2, cumcnt, it, seed, n0, u0, vth_e, vth_i, b0, theta_bn, phi_bn, l_damp_ini, delt, c=1.0, delx=1.0):
     """proj/shock/app.f90:695-850 on reference-layout arrays, in place: the new particles behind each
     row, np2 and cumcnt(nxe) advanced (the row total column is left as the Fortran leaves it),
-    the upstream field at columns nxe-1 and nxe."""
-    nxe = d.nxge
+    the upstream field at columns nxe-1 and nxe (nxe = d.nxe)."""
+    nxe = d.nxe
     gam0 = math.sqrt(1 + u0 * u0 / (c * c))
     v0 = u0 / gam0
     pflux = n0 * abs(v0) * delt * delx * (d.nyge - d.nygs + 1)
@@ -261,3 +262,56 @@ def inject(d, up, uf, np2, cumcnt, it, seed, n0, u0, vth_e, vth_i, b0, theta_bn,
     uf[1, i2, :] = by0
     uf[2, i2, :] = bz0
     return inj
+
+
+def relocate(d, up, uf, np2, cumcnt, it, seed, n0, u0, vth_e, vth_i, b0, theta_bn, phi_bn, l_damp_ini, c=1.0, delx=1.0):
+    """proj/shock/app.f90:613-690 (relocate) on reference-layout arrays, in place, for one rank: the
+    box grows by one cell (nxe -> nxe + 1, nothing while nxe = nxge); n0 particles per row and
+    species enter cell nxe_new - 1 at x = (nxe_new - 1 + (ii - 1/2)/n0) dx, y = (j + U) dx shared by
+    the species, Maxwellian in the fluid rest frame boosted by vprofile(x), behind the row's
+    particles, ids -(ii + (j - nygs) n0 + the species' count); np2 += n0; cumcnt(nxe_new) =
+    cumcnt(nxe_new - 1) + n0; the upstream field at columns nxe_new - 1 and nxe_new.  The draws
+    (random_number in the Fortran) are the Philox stream of this library: counter (row * n0 + k,
+    step), tag "expand".  Returns the Dims of the grown box."""
+    from dataclasses import replace
+    if d.nxe >= d.nxge:
+        return d
+    nxe = d.nxe + 1
+    gam0 = math.sqrt(1 + u0 * u0 / (c * c))
+    v0 = u0 / gam0
+    nptot = [int(np2[:, isp].sum()) for isp in range(d.nsp)]
+    t = TAG["expand"]
+    k = np.arange(n0, dtype=np.int64)
+    x = (nxe - 1) * delx + (k + 0.5) / n0 * delx
+    v1 = vprofile(x, v0, l_damp_ini, d.nxgs, delx)
+    gam1 = 1 / np.sqrt(1 - (v1 / c) ** 2)
+    for jr in range(d.ny):
+        q = jr * n0 + k
+        uy_draw, _ = uniform2(seed, q, 4 * it + 0, t)
+        n1, n2 = normal2(seed, q, 4 * it + 1, t)
+        n3, n4 = normal2(seed, q, 4 * it + 2, t)
+        n5, n6 = normal2(seed, q, 4 * it + 3, t)
+        y = (d.nys + jr + uy_draw) * delx
+        for isp, sd, u in ((0, vth_i, (n1, n2, n3)), (1, vth_e, (n4, n5, n6))):
+            ux, uyy, uz = sd * u[0], sd * u[1], sd * u[2]
+            gamp = np.sqrt(1 + (ux ** 2 + uyy ** 2 + uz ** 2) / c ** 2)
+            s0 = int(np2[jr, isp])
+            up[0, s0:s0 + n0, jr, isp] = x
+            up[1, s0:s0 + n0, jr, isp] = y
+            up[2, s0:s0 + n0, jr, isp] = gam1 * (ux + v1 * gamp)
+            up[3, s0:s0 + n0, jr, isp] = uyy
+            up[4, s0:s0 + n0, jr, isp] = uz
+            up[5, s0:s0 + n0, jr, isp] = (-(k + 1 + jr * n0 + nptot[isp])).view(np.float64)
+    for isp in range(d.nsp):
+        np2[:, isp] += n0
+        cumcnt[nxe - d.nxgs, :, isp] = cumcnt[nxe - 1 - d.nxgs, :, isp] + n0
+    by0 = b0 * math.sin(theta_bn) * math.cos(phi_bn)
+    bz0 = b0 * math.sin(theta_bn) * math.sin(phi_bn)
+    i1, i2 = nxe - 1 - (d.nxgs - 2), nxe - (d.nxgs - 2)
+    uf[1, i1, :] = by0
+    uf[2, i1, :] = bz0
+    uf[4, i1, :] = +v0 * bz0 / c
+    uf[5, i1, :] = -v0 * by0 / c
+    uf[1, i2, :] = by0
+    uf[2, i2, :] = bz0
+    return replace(d, nxe_act=nxe)

@@ -276,3 +276,100 @@ def test_tensor_core_input_gradient_matches_mma_sync(gpu, cin, shape):
     e_mma, e_exact = rel_err(outs[False], outs[True]), rel_err(outs[False], ref)
     print(f"\ninput gradient tcgen05 vs mma.sync {e_mma:.2e}, vs exact {e_exact:.2e}")
     assert e_mma <= BF16_ULP and e_exact <= BF16_ULP
+
+
+@pytest.mark.parametrize("cin,coutp,cout,grouped", [(16, 48, 48, False), (48, 48, 48, True), (48, 48, 48, False), (48, 16, 3, False)])
+@pytest.mark.parametrize("shape", [(2, 32, 48), (1, 64, 80)])
+def test_tensor_core_weight_gradient_matches_mma_sync(gpu, cin, coutp, cout, grouped, shape):
+    """The weight and bias gradients of training on tcgen05 (dz and the shifted input as MN-major
+    operands, one FP32 accumulator per tap column in tensor memory) against the mma.sync kernel and
+    against exact float64 sums of the same BF16 operands.  Both kernels sum exact BF16 products in
+    FP32, in different orders: 1e-5 normwise.  Grouped: the off-block gradients are returned as
+    zero.  The last layer's shape (cin 48, coutp 16, cout 3) reads 16 gradient channels and
+    returns 3."""
+    import ctypes
+
+    from wumingpic2d_gb300._native import check, lib
+
+    rng = np.random.default_rng(cin + coutp + 5 * grouped + shape[1])
+    n, H, W = shape
+    xb = C.bf16(rng.standard_normal((n, H, W, cin)))
+    dzb = C.bf16(rng.standard_normal((n, H, W, coutp)))
+    x_d = torch.tensor(xb, dtype=torch.float32).to("cuda", torch.bfloat16)
+    dz_d = torch.tensor(dzb, dtype=torch.float32).to("cuda", torch.bfloat16)
+    scratch = torch.empty(cnn.WGRAD_SCRATCH, dtype=torch.float32, device="cuda")
+    outs = {}
+    for legacy in (False, True):
+        dw = torch.full((9 * cout * cin,), float("nan"), device="cuda")
+        db = torch.full((cout,), float("nan"), device="cuda")
+        flags = (cnn.GROUPED if grouped else 0) | (32 if legacy else 0)
+        check(lib().wm_cnn_conv3x3_wgrad(ctypes.c_void_p(x_d.data_ptr()), ctypes.c_void_p(dz_d.data_ptr()), cin, coutp, cout, n, H, W, flags,
+                                         ctypes.c_void_p(dw.data_ptr()), ctypes.c_void_p(db.data_ptr()), ctypes.c_void_p(scratch.data_ptr()),
+                                         scratch.numel(), None), "wm_cnn_conv3x3_wgrad")
+        torch.cuda.synchronize()
+        outs[legacy] = (dw.cpu().numpy().reshape(9, cout, cin), db.cpu().numpy())
+    check(lib().wm_cnn_status(1), "wm_cnn_status")
+    ref = np.zeros((9, cout, cin))
+    for tap in range(9):
+        dy, dx = tap // 3 - 1, tap % 3 - 1
+        xs = np.roll(xb, (-dy, -dx), axis=(1, 2)).astype(np.float64)
+        ref[tap] = np.einsum("nhwo,nhwc->oc", dzb[..., :cout].astype(np.float64), xs)
+    off = np.zeros((9, cout, cin), dtype=bool)  # the off-block entries of a grouped layer
+    if grouped:
+        for go in range(3):
+            for gi in range(3):
+                if go != gi:
+                    off[:, 16 * go:16 * go + 16, 16 * gi:16 * gi + 16] = True
+        ref[off] = 0.0
+    rdb = dzb[..., :cout].astype(np.float64).sum(axis=(0, 1, 2))
+    (dw_tc, db_tc), (dw_mma, db_mma) = outs[False], outs[True]
+    e_mma, e_exact, e_db = rel_err(dw_tc, dw_mma), rel_err(dw_tc, ref), rel_err(db_tc, rdb)
+    print(f"\nweight gradient tcgen05 vs mma.sync {e_mma:.2e}, vs exact {e_exact:.2e}; bias gradient vs exact {e_db:.2e}")
+    assert np.isfinite(dw_tc).all() and np.isfinite(db_tc).all()
+    assert e_mma <= 1e-5 and e_exact <= 1e-5 and e_db <= 1e-5
+    assert not dw_tc[off].any()
+
+
+def test_interior_loss_leaves_the_crop_border_out(gpu):
+    """wm_cnn_mse_interior: the loss over the interior of each image and a zero gradient within
+    `border` pixels of its edges (training on crops of a larger field)."""
+    import ctypes
+
+    from wumingpic2d_gb300._native import check, lib
+
+    rng = np.random.default_rng(5)
+    n, H, W, b = 3, 32, 48, 8
+    pred = rng.standard_normal((n, H, W, 8)).astype(np.float32)
+    tgt = rng.standard_normal((n, H, W, 3)).astype(np.float32)
+    p_d, t_d = torch.tensor(pred, device="cuda"), torch.tensor(tgt, device="cuda")
+    dz = torch.full((n, H, W, 16), 1.0, dtype=torch.bfloat16, device="cuda")
+    part = torch.empty(64, dtype=torch.float64, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float64, device="cuda")
+    check(lib().wm_cnn_mse_interior(ctypes.c_void_p(p_d.data_ptr()), ctypes.c_void_p(t_d.data_ptr()), n, H, W, b,
+                                    ctypes.c_void_p(dz.data_ptr()), ctypes.c_void_p(part.data_ptr()), 64, ctypes.c_void_p(loss.data_ptr()),
+                                    None), "wm_cnn_mse_interior")
+    torch.cuda.synchronize()
+    e = (pred[..., :3].astype(np.float64) - tgt)[:, b:H - b, b:W - b]
+    count = e.size
+    assert abs(loss.item() - 0.5 * np.sum(e * e) / count) <= 1e-6 * loss.item()
+    g = dz.float().cpu().numpy()
+    inner = np.zeros((n, H, W), dtype=bool)
+    inner[:, b:H - b, b:W - b] = True
+    assert not g[~inner].any() and not g[..., 3:].any()
+    assert rel_err(g[inner][:, :3], (e / count).reshape(-1, 3)) <= BF16_ULP
+
+
+def test_standalone_guess_workload_runs(gpu):
+    """The standalone learned-guess workload end to end on small boxes: crops from a Weibel and a
+    Harris run, training with the interior loss on the tensor-core kernels, and CG iterations at
+    1e-10 both ways on a periodic Weibel system; the guess changes only the iteration count."""
+    from wumingpic2d_gb300 import guess_standalone as G
+
+    r = G.run(pairs=96, size=48, steps=20, every=10, train_steps=40, batch=8, n=128, ppc=8, warm=5, measure_steps=3,
+              weibel=(128, 8), harris=(256, 128))
+    print("\n" + str({k: v for k, v in r.items() if k != "params"}))
+    assert r["pairs"]["count"] == 96
+    assert all(np.isfinite(l) for _, l in r["training"]["loss_history"])
+    for mode in ("previous_step", "learned"):
+        assert r["cg"][mode]["cg_iters_per_step"] > 0
+    assert np.isfinite(r["params"]).all()

@@ -109,6 +109,8 @@ SIGNATURES = {
     "wm_sim_init_harris": [_P, _I, _I, _D, _D, _D, _D, _D, _D, ctypes.c_uint64],
     "wm_sim_init_shock": [_P, _I, _D, _D, _D, _D, _D, _D, _D, _D, _D, ctypes.c_uint64],
     "wm_sim_set_injection": [_P, _I, _I, _D, _D, _D, _D, _D, _D, ctypes.c_uint64],
+    "wm_sim_set_expansion": [_P, _I, _I],
+    "wm_sim_get_nxe": [_P, _P],
     "wm_sim_set_step": [_P, ctypes.c_int64],
     "wm_sim_get_step": [_P, _P],
     "wm_sim_write_particles": [_P, ctypes.c_char_p, _I, _I],

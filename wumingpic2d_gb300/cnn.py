@@ -176,8 +176,9 @@ class Trainer:
     """Adam on the mean squared error, all steps on the device; the gradient mask keeps the
     network block-diagonal."""
 
-    def __init__(self, net: GuessNet, lr: float = 1e-3, betas=(0.9, 0.999), eps: float = 1e-8, masked: bool = True):
+    def __init__(self, net: GuessNet, lr: float = 1e-3, betas=(0.9, 0.999), eps: float = 1e-8, masked: bool = True, border: int = 0):
         self.net, self.lr, self.betas, self.eps = net, lr, betas, eps
+        self.border = border  # > 0: samples are crops; the loss covers their interior only
         dev = net.device
         self.m = torch.zeros_like(net.params)
         self.v = torch.zeros_like(net.params)
@@ -194,8 +195,12 @@ class Trainer:
         pred, cache = self.net.forward(x, train=True)
         n, H, W, _ = x.shape
         dz = torch.empty((n, H, W, GRAD_CH), dtype=torch.bfloat16, device=self.net.device)
-        check(lib().wm_cnn_mse(_p(pred), _p(target), n * H * W, _p(dz), _p(self.partial), self.nblocks, _p(self.loss), _stream()),
-              "wm_cnn_mse")
+        if self.border:
+            check(lib().wm_cnn_mse_interior(_p(pred), _p(target), n, H, W, self.border, _p(dz), _p(self.partial), self.nblocks,
+                                            _p(self.loss), _stream()), "wm_cnn_mse_interior")
+        else:
+            check(lib().wm_cnn_mse(_p(pred), _p(target), n * H * W, _p(dz), _p(self.partial), self.nblocks, _p(self.loss), _stream()),
+                  "wm_cnn_mse")
         self.net.backward(cache, dz, self.grad, self.scratch)
         return self.loss
 
@@ -237,6 +242,49 @@ def capture_pairs(sim, nsteps: int, every: int = 1):
     return np.stack(xs), np.stack(ys)
 
 
+def capture_crops(sim, nsteps: int, every: int, ncrops: int, size: int, rng: np.random.Generator, wrap_x: bool = True):
+    """Step a resident Simulation nsteps times; every `every` steps cut ncrops random size x size
+    crops out of the (input, converged dB) pair, each group normalised by its root mean square over
+    the whole grid (as the inference inside the step does).  Crops wrap around the periodic y edges,
+    and around x only if wrap_x (walls in x: crops lie inside the box).  Returns device tensors:
+    BF16 inputs [k][size][size][16] and FP32 targets [k][size][size][3]."""
+    d = sim.dims
+    dev = "cuda"
+    xs, ys = [], []
+    src = torch.tensor(PACKED_SOURCE, device=dev)
+    grp = torch.tensor(PACKED_GROUP, device=dev)
+    ar = torch.arange(size, device=dev)
+    for k in range(nsteps):
+        take = k % every == 0
+        if take:
+            uf = torch.from_numpy(sim.fields().T).to(dev)  # (ny+4, nx+4, 6): the reference layout read as C order
+        sim.step(1)
+        if not take:
+            continue
+        df, uj = sim.get_work()
+        uj = torch.from_numpy(uj.T).to(dev)
+        df = torch.from_numpy(df.T).to(dev)
+        inner = (slice(2, d.ny + 2), slice(2, d.nx + 2))
+        raw = torch.cat([uf[inner][..., 3:6], uf[inner][..., 0:3], uj[inner][..., 0:3]], dim=-1)  # (ny, nx, 9): E, B, J
+        packed = raw[..., src]  # (ny, nx, 11)
+        ss = torch.zeros(3, dtype=torch.float64, device=dev).index_add_(0, grp, (packed ** 2).mean(dim=(0, 1)))
+        cnt = torch.bincount(grp, minlength=3).to(torch.float64)
+        s = torch.sqrt(ss / cnt)
+        inv = torch.where(s > 0, 1.0 / torch.where(s > 0, s, torch.ones_like(s)), torch.zeros_like(s))
+        packed = packed * inv[grp]
+        target = df[inner][..., 0:3] * inv
+        y0 = torch.from_numpy(rng.integers(0, d.ny, ncrops)).to(dev)
+        x0 = torch.from_numpy(rng.integers(0, d.nx if wrap_x else d.nx - size + 1, ncrops)).to(dev)
+        rows = (y0[:, None] + ar[None, :]) % d.ny  # (k, size)
+        cols = (x0[:, None] + ar[None, :]) % d.nx
+        ri, ci = rows[:, :, None], cols[:, None, :]
+        xc = torch.zeros((ncrops, size, size, LAYERS[0][0]), dtype=torch.bfloat16, device=dev)
+        xc[..., :len(PACKED_SOURCE)] = packed[ri, ci].to(torch.bfloat16)
+        xs.append(xc)
+        ys.append(target[ri, ci].to(torch.float32))
+    return torch.cat(xs), torch.cat(ys)
+
+
 def group_scales(xs: np.ndarray) -> np.ndarray:
     """Per sample, the root mean square of each group's raw inputs: [n][3]."""
     xs = np.asarray(xs, dtype=np.float64)
@@ -266,13 +314,14 @@ def to_device(xs: np.ndarray, ys: np.ndarray, device: str = "cuda"):
 
 
 def train(net: GuessNet, x: torch.Tensor, y: torch.Tensor, steps: int, batch: int = 8, lr: float = 2e-3, seed: int = 0,
-          log_every: int = 0):
+          log_every: int = 0, border: int = 0):
     """Adam with a cosine learning-rate decay over random mini-batches.  The targets are divided by
     their per-component root mean square over the samples while training, and that factor is then
-    folded into the last layer.  Returns the loss history [(step, loss)] on the scaled targets."""
+    folded into the last layer.  border > 0: the samples are crops and the loss covers their
+    interior.  Returns the loss history [(step, loss)] on the scaled targets."""
     sigma = torch.sqrt(torch.mean(y.double() ** 2, dim=(0, 1, 2))).clamp_min(1e-300)
     ys = (y / sigma.float()).contiguous()
-    tr = Trainer(net, lr=lr)
+    tr = Trainer(net, lr=lr, border=border)
     rng = np.random.Generator(np.random.Philox(seed))
     hist = []
     n = x.shape[0]

@@ -34,6 +34,7 @@ int make_geom(WmGeom &g, int ndim, int np, int nsp, int nxgs, int nxge, int nygs
     g.nxw = g.nx + 4;
     g.nyw = g.ny + 4;
     g.bc = WM_BC_PERIODIC;  // the boundary module's init sets its own kind
+    g.nxa = g.nx;
     return WM_OK;
 }
 

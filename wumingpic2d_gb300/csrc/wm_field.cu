@@ -271,7 +271,11 @@ __device__ __forceinline__ int wrapm(int a, int n) { return a < 0 ? a + n : (a >
 // The x neighbours of interior cell ci (0-based) of component l (0 = Bx) of a CG vector, read
 // through at(c) = value at interior column c of the same row: periodic wrap, or the walls' halo
 // (boundary_reconnection__phi / boundary_shock__phi): Bx odd about nxs - 1/2, By and Bz even
-// about nxs, zero beyond nxe.
+// about nxs, zero beyond nxe (the last active cell, nxa - 1).
+//
+// Cells past nxe (ci >= nxa: the shock's expanding box) are outside the solve of field.f90:319-461,
+// which runs over nxs..nxe: the kernels below give them b = r = ap = delta-E = 0, so every CG vector
+// and dfield stays zero there and the fields past nxe + 1 keep their values, as in the reference.
 template <class F>
 __device__ __forceinline__ void x_neighbours(const WmGeom &g, int l, int ci, const F &at, double &left, double &right)
 {
@@ -281,7 +285,7 @@ __device__ __forceinline__ void x_neighbours(const WmGeom &g, int l, int ci, con
         return;
     }
     left = ci > 0 ? at(ci - 1) : (l == 0 ? -at(0) : at(1));
-    right = ci < g.nx - 1 ? at(ci + 1) : 0.0;
+    right = ci < g.nxa - 1 ? at(ci + 1) : 0.0;
 }
 
 // gkl (field.f90:125-146), b = f5*gkl and ||b||^2 (:351-364).
@@ -304,7 +308,8 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_rhs(WmGeom g, FieldK fk, FV6 
         const double g3 = +fk.f2 * (+uf(2, x, y - 1) + uf(2, x - 1, y) - 4. * uf(2, x, y) + uf(2, x + 1, y) + uf(2, x, y + 1)
                                     + fk.f3 * (-uj(1, x - 1, y) + uj(1, x, y) + uj(0, x, y - 1) - uj(0, x, y)))
                           - fk.f1 * (-uf(4, x - 1, y) + uf(4, x, y) + uf(3, x, y - 1) - uf(3, x, y));
-        const double b1 = fk.f5 * g1, b2 = fk.f5 * g2, b3 = fk.f5 * g3;
+        const bool on = ci < g.nxa;
+        const double b1 = on ? fk.f5 * g1 : 0.0, b2 = on ? fk.f5 * g2 : 0.0, b3 = on ? fk.f5 * g3 : 0.0;
         b[0 * ncell + e] = b1;
         b[1 * ncell + e] = b2;
         b[2 * ncell + e] = b3;
@@ -337,7 +342,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_resid(WmGeom g, FieldK fk, FV
         for (int l = 0; l < 3; ++l) {
             double xl, xr;
             x_neighbours(g, l, ci, [&](int c) { return df(l, c + 2, y); }, xl, xr);
-            const double rv = b[l * ncell + e] + df(l, x, ym) + xl - fk.f4 * df(l, x, y) + xr + df(l, x, yp);
+            const double rv = ci < g.nxa ? b[l * ncell + e] + df(l, x, ym) + xl - fk.f4 * df(l, x, y) + xr + df(l, x, yp) : 0.0;
             r[l * ncell + e] = rv;
             p[l * ncell + e] = rv;
             acc[l] += rv * rv;
@@ -386,8 +391,9 @@ __global__ void __launch_bounds__(CG_THREADS) k_guess_resid2(WmGeom g, FieldK fk
             const double rc = bl + cand(l, xx, ym) + xl - fk.f4 * cand(l, xx, yy) + xr + cand(l, xx, yp);
             x_neighbours(g, l, ci, [&](int c) { return df(l, c + 2, yy); }, xl, xr);
             const double rp = bl + df(l, xx, ym) + xl - fk.f4 * df(l, xx, yy) + xr + df(l, xx, yp);
-            acc[l] += rc * rc;
-            acc[3 + l] += rp * rp;
+            const bool on = ci < g.nxa;
+            acc[l] += on ? rc * rc : 0.0;
+            acc[3 + l] += on ? rp * rp : 0.0;
         }
     }
     block_sum3(acc[0], acc[1], acc[2]);
@@ -440,7 +446,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_resid_pick(WmGeom g, FieldK f
             double xl, xr;
             x_neighbours(g, l, ci, [&](int c) { return at(c + 2, y); }, xl, xr);
             const double centre = at(x, y);
-            const double rv = b[l * ncell + e] + at(x, ym) + xl - fk.f4 * centre + xr + at(x, yp);
+            const double rv = ci < g.nxa ? b[l * ncell + e] + at(x, ym) + xl - fk.f4 * centre + xr + at(x, yp) : 0.0;
             if (tk) df(l, x, y) = centre;
             r[l * ncell + e] = rv;
             p[l * ncell + e] = rv;
@@ -499,7 +505,7 @@ __global__ void __launch_bounds__(CG_THREADS, CG_BLOCKS / 152 + 1) k_cg_phase(Wm
                 const double pc = pl[e];
                 double xl, xr;
                 x_neighbours(g, l, ci, [&](int c) { return pl[row + c]; }, xl, xr);
-                const double a = -pl[es] - xl + fk.f4 * pc - xr - pl[en];
+                const double a = ci < g.nxa ? -pl[es] - xl + fk.f4 * pc - xr - pl[en] : 0.0;
                 ap[o] = a;
                 acc[l] += pc * a;
             } else if (ph[l] == 1) {
@@ -546,6 +552,12 @@ __global__ void k_efield(WmGeom g, FieldK fk, FV6 df, FV6 uf, FV3 uj)
     const long long ncell = (long long)g.nx * g.ny;
     for (GridCell q(g.nx); q.e < ncell; q.next()) {
         const int x = q.c + 2, y = q.r + 2;
+        if (q.c >= g.nxa) {  // past nxe: no field update (:156)
+            df(3, x, y) = 0.0;
+            df(4, x, y) = 0.0;
+            df(5, x, y) = 0.0;
+            continue;
+        }
         df(3, x, y) = +fk.f1 * (+fk.gfac * (-df(2, x, y) + df(2, x, y + 1)) + (-uf(2, x, y) + uf(2, x, y + 1))) - fk.pi4dt * uj(0, x, y);
         df(4, x, y) = -fk.f1 * (+fk.gfac * (-df(2, x, y) + df(2, x + 1, y)) + (-uf(2, x, y) + uf(2, x + 1, y))) - fk.pi4dt * uj(1, x, y);
         df(5, x, y) = +fk.f1 * (+fk.gfac * (-df(1, x, y) + df(1, x + 1, y) + df(0, x, y) - df(0, x, y + 1))

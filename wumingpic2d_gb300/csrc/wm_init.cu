@@ -82,7 +82,7 @@ __global__ void k_init_particles(WmGeom g, WmInitArgs a, double *__restrict__ st
         put(s0, x, y, sdi * n1, sdi * n2, sdi * n3 + a.f1 * drift, -(1 + idx));
         put(s1, x, y, sde * n4, sde * n5, sde * n6 + a.f2 * drift, -(1 + idx));
     } else {  // shock
-        const int nxs = g.nxgs, nxe = g.nxge;
+        const int nxs = g.nxgs, nxe = g.nxgs + g.nxa - 1;  // nxe = nxgs + n_x_ini (proj/shock/app.f90:277)
         // evenly over the cells nxs+1..nxe-1 that np2 = n0 (nxe-nxs-1) and the initial cumcnt
         // (app.f90:335-349) give n0 each; app.f90:437 spreads them over [nxs, nxe), which puts a
         // few behind the wall at nxs+1, where the first reflection moves them by more than a cell
@@ -177,7 +177,7 @@ __global__ void k_inject_counts(WmGeom g, WmInjectArgs a, const int *__restrict_
     }
     __syncthreads();
     long long nginj = s_nginj;
-    if ((long long)(tot[0] + tot[1]) + 2 * nginj > a.cap) {  // no room: nothing enters, the step reports it
+    if ((long long)(tot[0] + tot[1]) + 2 * (nginj + (long long)a.n_expand * ny) > a.cap) {  // no room: nothing enters, the step reports it
         if (threadIdx.x == 0) atomicOr(status, (unsigned)WMDEV_OVERFLOW);
         nginj = 0;
     }
@@ -200,10 +200,10 @@ __global__ void k_inject_counts(WmGeom g, WmInjectArgs a, const int *__restrict_
     }
 }
 
-__global__ void k_inject_reserve(WmGeom g, const int *__restrict__ np2, const int *__restrict__ inj, int *__restrict__ tmp)
+__global__ void k_inject_reserve(WmGeom g, const int *__restrict__ np2, const int *__restrict__ inj, int extra, int *__restrict__ tmp)
 {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r < g.nrows) tmp[r] = np2[r] + inj[r % g.ny];
+    if (r < g.nrows) tmp[r] = np2[r] + inj[r % g.ny] + extra;
 }
 
 __device__ __forceinline__ void put_particle(const SoAView &v, long long p, const WmGeom &, int, int, double x, double y, double ux, double uy,
@@ -285,6 +285,63 @@ __global__ void k_inject_finish(WmGeom g, WmInjectArgs a, int *__restrict__ np2,
     for (int ci = a.cell + 2; ci <= g.nx; ++ci) cc[ci] += n;  // and the row total with it
 }
 
+// proj/shock/app.f90:613-690 (relocate), the box growing by one cell (nxe -> nxe + 1), for one
+// rank: n0 = a.n_expand particles per row and species in the cell nxe (interior cell a.cell + 1),
+// x = nxe dx + (k + 1/2)/n0 dx, y = (j + U) dx shared by the species, a Maxwellian in the fluid
+// rest frame boosted by vprofile(x); they go behind the row's sorted and injected particles
+// (np2 already counts the injected ones) and are counted in that cell; the ids continue after the
+// species' count including this step's injection.  The draws are Philox with counter
+// (row * n0 + k, step) under their own tag.  perm != null: as k_inject_particles, past the
+// injected particles' fresh slots.
+template <class PV>
+__global__ void k_expand_particles(WmGeom g, WmInjectArgs a, PV dst, const int *__restrict__ np2, const int *__restrict__ inj,
+                                   const long long *__restrict__ ninc, const long long *__restrict__ nptot, unsigned *__restrict__ perm,
+                                   unsigned *__restrict__ idperm, const long long *__restrict__ phys0)
+{
+    const int jr = blockIdx.y;
+    const int n0 = a.n_expand;
+    const long long step_inj = ninc[g.ny - 1] + inj[g.ny - 1];  // this step's injected particles per species
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n0; k += gridDim.x * blockDim.x) {
+        const long long q = (long long)jr * n0 + k;
+        double uy_draw, unused, n1, n2, n3, n4, n5, n6;
+        wm_rng_uniform2(a.seed, q, (uint32_t)(4 * a.it + 0), WM_RNG_EXPAND, uy_draw, unused);
+        wm_rng_normal2(a.seed, q, (uint32_t)(4 * a.it + 1), WM_RNG_EXPAND, n1, n2);
+        wm_rng_normal2(a.seed, q, (uint32_t)(4 * a.it + 2), WM_RNG_EXPAND, n3, n4);
+        wm_rng_normal2(a.seed, q, (uint32_t)(4 * a.it + 3), WM_RNG_EXPAND, n5, n6);
+        const double delx = a.delx;
+        const double x = a.xe + (k + 0.5) / n0 * delx;
+        const double y = (g.nys + jr + uy_draw) * delx;
+        const double c2 = a.c * a.c;
+        const double v1 = vprofile(x, a.v0, a.l_damp_ini, a.nxgs_delx);
+        const double gam1 = 1 / sqrt(1 - (v1 / a.c) * (v1 / a.c));
+        for (int isp = 0; isp < 2; ++isp) {
+            const double sd = isp == 0 ? a.vth_i : a.vth_e;
+            const double ux = sd * (isp == 0 ? n1 : n4), uy = sd * (isp == 0 ? n2 : n5), uz = sd * (isp == 0 ? n3 : n6);
+            const double gamp = sqrt(1 + (ux * ux + uy * uy + uz * uz) / c2);
+            const int row = isp * g.ny + jr;
+            long long p = dst.idx(row, np2[row] + k);
+            if (perm) {
+                const long long ph = *phys0 + 2 * step_inj + isp * (long long)g.ny * n0 + q;
+                perm[p] = (unsigned)ph;
+                idperm[p] = (unsigned)ph;
+                p = ph;
+            }
+            put_particle(dst, p, g, a.cell + 1, jr, x, y, gam1 * (ux + v1 * gamp), uy, uz, -(k + 1 + (long long)jr * n0 + nptot[isp] + step_inj));
+        }
+    }
+}
+
+// np2 += n0; cumcnt(nxe + 1) = cumcnt(nxe) + n0 (app.f90:674) and the row total with it
+__global__ void k_expand_finish(WmGeom g, WmInjectArgs a, int *__restrict__ np2, int *__restrict__ cumcnt)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= g.nrows) return;
+    const int n = a.n_expand;
+    np2[r] += n;
+    int *cc = cumcnt + (long long)r * (g.nx + 1);
+    for (int ci = a.cell + 2; ci <= g.nx; ++ci) cc[ci] += n;
+}
+
 __global__ void k_inject_fields(WmGeom g, WmInjectArgs a, FView<6, false> uf)
 {
     const int iy = blockIdx.x * blockDim.x + threadIdx.x;
@@ -308,9 +365,9 @@ int wm_launch_inject_counts(const WmGeom &g, const WmInjectArgs &a, const int *n
     return wm_check_launch("k_inject_counts");
 }
 
-int wm_launch_inject_reserve(const WmGeom &g, const int *np2, const int *inj, int *tmp, cudaStream_t st)
+int wm_launch_inject_reserve(const WmGeom &g, const WmInjectArgs &a, const int *np2, const int *inj, int *tmp, cudaStream_t st)
 {
-    k_inject_reserve<<<wm_div_up(g.nrows, 256), 256, 0, st>>>(g, np2, inj, tmp);
+    k_inject_reserve<<<wm_div_up(g.nrows, 256), 256, 0, st>>>(g, np2, inj, a.n_expand, tmp);
     return wm_check_launch("k_inject_reserve");
 }
 
@@ -330,6 +387,21 @@ template int wm_launch_inject_particles<SoAView>(const WmGeom &, const WmInjectA
 template int wm_launch_inject_particles<MixedView>(const WmGeom &, const WmInjectArgs &, MixedView, int *, int *, const int *,
                                                    const long long *, const long long *, cudaStream_t, unsigned *, unsigned *,
                                                    const long long *);
+
+template <class PV>
+int wm_launch_expand_particles(const WmGeom &g, const WmInjectArgs &a, PV dst, int *np2, int *cumcnt, const int *inj, const long long *ninc,
+                               const long long *nptot, cudaStream_t st, unsigned *perm, unsigned *idperm, const long long *phys0)
+{
+    if (a.n_expand < 1 || a.cell + 2 > g.nx) return WM_ERR_BAD_ARG;
+    k_expand_particles<PV><<<dim3(1, g.ny), 128, 0, st>>>(g, a, dst, np2, inj, ninc, nptot, perm, idperm, phys0);
+    WM_TRY(wm_check_launch("k_expand_particles"));
+    k_expand_finish<<<wm_div_up(g.nrows, 256), 256, 0, st>>>(g, a, np2, cumcnt);
+    return wm_check_launch("k_expand_finish");
+}
+template int wm_launch_expand_particles<SoAView>(const WmGeom &, const WmInjectArgs &, SoAView, int *, int *, const int *, const long long *,
+                                                 const long long *, cudaStream_t, unsigned *, unsigned *, const long long *);
+template int wm_launch_expand_particles<MixedView>(const WmGeom &, const WmInjectArgs &, MixedView, int *, int *, const int *, const long long *,
+                                                   const long long *, cudaStream_t, unsigned *, unsigned *, const long long *);
 
 int wm_launch_inject_fields(const WmGeom &g, const WmInjectArgs &a, FView<6, false> uf, cudaStream_t st)
 {

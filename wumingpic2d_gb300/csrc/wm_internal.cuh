@@ -21,6 +21,8 @@ struct WmGeom {
     int nx, ny, nrows;  // nrows = nsp * ny
     int nxw, nyw;       // ghosted extents nx+4, ny+4
     int bc;             // WM_BC_*: boundary module of the application (x direction; y is periodic in all three)
+    int nxa;            // active cells in x, nxe - nxgs + 1: the particles' range, the field solve's extent and the
+                        // place of the x boundaries; nx but while the shock application's box expands
 };
 
 struct WmConst {

@@ -189,14 +189,15 @@ struct WmInjectArgs {
     int cell;                  // interior cell the new particles are counted in (nxe-1)
     long long cap;             // particle capacity of the sets
     double by0, bz0;           // upstream field
+    int n_expand;              // particles per row and species the box's expansion adds this step (0: none)
 };
 constexpr int WM_INJECT_MAX_ROWS = 12288;
 // counts per row (inj[ny]), their exclusive prefix (ninc[ny]) and the species totals before the
 // injection (nptot[2]); reads the new row counts np2
 int wm_launch_inject_counts(const WmGeom &g, const WmInjectArgs &a, const int *np2, int *inj, long long *ninc, long long *nptot,
                             unsigned *status, cudaStream_t st);
-// tmp[row] = np2[row] + inj[row % ny]: row counts with room for the new particles
-int wm_launch_inject_reserve(const WmGeom &g, const int *np2, const int *inj, int *tmp, cudaStream_t st);
+// tmp[row] = np2[row] + inj[row % ny] + a.n_expand: row counts with room for the new particles
+int wm_launch_inject_reserve(const WmGeom &g, const WmInjectArgs &a, const int *np2, const int *inj, int *tmp, cudaStream_t st);
 // write the new particles behind each row's sorted ones, then np2 += inj, cumcnt(nxe), total += inj;
 // with perm (a permuted mixed state): the particles go to fresh slots from *phys0 on and perm /
 // idperm of their cell-sorted slots point there
@@ -205,3 +206,10 @@ int wm_launch_inject_particles(const WmGeom &g, const WmInjectArgs &a, PV dst, i
                                const long long *ninc, const long long *nptot, cudaStream_t st, unsigned *perm = nullptr,
                                unsigned *idperm = nullptr, const long long *phys0 = nullptr);
 int wm_launch_inject_fields(const WmGeom &g, const WmInjectArgs &a, FView<6, false> uf, cudaStream_t st);
+// the box's expansion (relocate): a.n_expand particles per row and species in the cell after
+// a.cell, behind the rows' particles (after the injection's), np2 and cumcnt advanced; the caller
+// then moves nxe on (g.nxa, a.cell, a.xe) and sets the boundary columns (wm_launch_inject_fields)
+template <class PV>
+int wm_launch_expand_particles(const WmGeom &g, const WmInjectArgs &a, PV dst, int *np2, int *cumcnt, const int *inj, const long long *ninc,
+                               const long long *nptot, cudaStream_t st, unsigned *perm = nullptr, unsigned *idperm = nullptr,
+                               const long long *phys0 = nullptr);

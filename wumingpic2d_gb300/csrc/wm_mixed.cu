@@ -1007,8 +1007,8 @@ int wm_launch_mixed_push_deposit(const WmGeom &g, const WmConst &k, MixedView a,
     kc.inv_c2 = (float)(1.0 / (k.c * k.c));
     kc.c2 = (float)(k.c * k.c);
     kc.bc = g.bc;
-    {  // xend of boundary_shock.f90:266 in interior cells
-        const double xend = g.nxge * k.delx + k.u0 / sqrt(1 + (k.u0 * k.u0) / (k.c * k.c)) * k.delt;
+    {  // xend of boundary_shock.f90:266 in interior cells, at the active nxe
+        const double xend = (g.nxgs + g.nxa - 1) * k.delx + k.u0 / sqrt(1 + (k.u0 * k.u0) / (k.c * k.c)) * k.delt;
         const double xe = xend / k.delx - g.nxgs;
         kc.xe_cell = (int)floor(xe);
         kc.xe_off = (float)(xe - kc.xe_cell);

@@ -91,6 +91,7 @@ extern "C" int wm_deposit_current_noalloc(const double *up, const double *gp, co
     g.nrows = nsp * ny;
     g.nxw = nx + 4;
     g.nyw = ny + 4;
+    g.nxa = nx;
     WmConst k{};
     k.delx = delx;
     k.delt = delt;

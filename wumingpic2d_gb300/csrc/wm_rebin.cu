@@ -76,7 +76,7 @@ WallsX walls_x_params(const WmGeom &g, double delx, double delt, double c, int i
     WallsX w;
     w.delx = delx;
     w.nxs = g.nxgs;
-    w.nxe = g.nxge;
+    w.nxe = g.nxgs + g.nxa - 1;  // the active nxe (nxge but while the shock's box expands)
     w.xl = (double)(2.0f * (float)(w.nxs + 1)) * delx;
     w.xr = (double)(2.0f * (float)(w.nxe - 1)) * delx;
     w.xend = w.nxe * delx + u0 / sqrt(1 + (u0 * u0) / (c * c)) * delt;

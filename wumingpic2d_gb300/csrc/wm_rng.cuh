@@ -48,7 +48,7 @@ WM_HD double wm_uniform53(uint32_t a, uint32_t b)
     return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
 }
 
-enum { WM_RNG_WEIBEL = 1, WM_RNG_HARRIS = 2, WM_RNG_SHOCK = 3, WM_RNG_INJECT = 4, WM_RNG_INJECT_COUNT = 5 };
+enum { WM_RNG_WEIBEL = 1, WM_RNG_HARRIS = 2, WM_RNG_SHOCK = 3, WM_RNG_INJECT = 4, WM_RNG_INJECT_COUNT = 5, WM_RNG_EXPAND = 6 };
 
 // Draw `call` of particle `idx`: two uniforms in [0, 1).
 WM_HD void wm_rng_uniform2(uint64_t seed, long long idx, uint32_t call, uint32_t tag, double &u1, double &u2)

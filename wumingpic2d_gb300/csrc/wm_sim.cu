@@ -140,6 +140,38 @@ struct wm_sim {
     bool inject_on = false;
     WmInjectArgs inj{};
     long long it = 0;  // steps taken: the counter of the injection draws
+    // the shock box's expansion (proj/shock/app.f90:123-125, relocate :613-690): every
+    // expand_every steps (0: never), after the injection, nxe (g.nxa) grows by one cell and
+    // inj_n0 particles per row and species enter the new cell
+    int expand_every = 0, inj_n0 = 0;
+    bool expanding_now() const { return inject_on && expand_every > 0 && (it + 1) % expand_every == 0 && g.nxa < g.nx; }
+    // the injection boundary at the active nxe: cell nxe-1 counts the new particles, x = nxe dx
+    void sync_inject_boundary()
+    {
+        inj.cell = g.nxa - 2;
+        inj.xe = (g.nxgs + g.nxa - 1) * k.delx;
+        inj.n_expand = expanding_now() ? inj_n0 : 0;
+    }
+    // after this step's injection: the expansion's particles (on stream s), then, once the field
+    // update has run (finish_expansion), nxe moves on and the new boundary columns take the
+    // upstream field
+    template <class PV>
+    int expand_write(PV dst, int *np2_new, int *cumcnt_new, cudaStream_t s, unsigned *perm = nullptr, unsigned *idperm = nullptr,
+                     const long long *phys0 = nullptr)
+    {
+        if (inj.n_expand == 0) return WM_OK;
+        return wm_launch_expand_particles(g, inj, dst, np2_new, cumcnt_new, inj_rows.as<int>(), inj_ninc.as<long long>(),
+                                          inj_nptot.as<long long>(), s, perm, idperm, phys0);
+    }
+    int finish_expansion()
+    {
+        if (inj.n_expand == 0) return WM_OK;
+        g.nxa += 1;
+        inj.cell = g.nxa - 2;
+        inj.xe = (g.nxgs + g.nxa - 1) * k.delx;
+        inj.n_expand = 0;
+        return wm_launch_inject_fields(g, inj, uf(), st);
+    }
     DevBuf inj_rows, inj_ninc, inj_nptot, inj_tmp;
     // host -> device particle rows in chunks on a second stream, overlapped with the unpack
     // kernels on the main one (host buffers mapped into the device's address space)
@@ -504,9 +536,10 @@ struct wm_sim {
         if (!inject_on) return wm_launch_rowbase(g.nrows, sc.np2_new, sc.rowbase_new, s);
         inj.it = (int)it;
         inj.cap = cap;
+        sync_inject_boundary();
         WM_TRY(wm_launch_inject_counts(g, inj, sc.np2_new, inj_rows.as<int>(), inj_ninc.as<long long>(), inj_nptot.as<long long>(),
                                        sc.status, s));
-        WM_TRY(wm_launch_inject_reserve(g, sc.np2_new, inj_rows.as<int>(), inj_tmp.as<int>(), s));
+        WM_TRY(wm_launch_inject_reserve(g, inj, sc.np2_new, inj_rows.as<int>(), inj_tmp.as<int>(), s));
         return wm_launch_rowbase(g.nrows, inj_tmp.as<int>(), sc.rowbase_new, s);
     }
     // second half (after the move): the new particles behind the sorted ones, np2 and cumcnt
@@ -517,7 +550,9 @@ struct wm_sim {
         if (!inject_on) return WM_OK;
         WM_TRY(wm_launch_inject_particles(g, inj, dst, sc.np2_new, cumcnt_new, inj_rows.as<int>(), inj_ninc.as<long long>(),
                                           inj_nptot.as<long long>(), st));
-        return wm_launch_inject_fields(g, inj, uf(), st);
+        WM_TRY(expand_write(dst, sc.np2_new, cumcnt_new, st));
+        WM_TRY(wm_launch_inject_fields(g, inj, uf(), st));
+        return finish_expansion();
     }
 
     // The cell-sorted state in set A again (ids in A[5]): gather the push output through mx_perm
@@ -625,6 +660,9 @@ struct wm_sim {
             rs = wm_launch_inject_particles(g, inj, mview(B, 1 - cur, 0), sc.np2_new, cumcnt_alt.as<int>(), inj_rows.as<int>(),
                                             inj_ninc.as<long long>(), inj_nptot.as<long long>(), st2, mx_perm.as<unsigned>(),
                                             mx_idperm[1 - idp].as<unsigned>(), rowbase[cur].as<long long>() + g.nrows);
+        if (rs == WM_OK && inject_on)  // the box's expansion: its particles past the injected ones
+            rs = expand_write(mview(B, 1 - cur, 0), sc.np2_new, cumcnt_alt.as<int>(), st2, mx_perm.as<unsigned>(),
+                              mx_idperm[1 - idp].as<unsigned>(), rowbase[cur].as<long long>() + g.nrows);
         WM_CUDA(cudaEventRecord(rb_done, st2));
         nl += (inject_on ? 7 : 4);
         WM_TRY(wm_launch_mixed_jfold(g, jtile.as<float>(), uj(), st));
@@ -638,6 +676,8 @@ struct wm_sim {
         if (inject_on) {  // the upstream field at the boundary columns, after the solve's field update
             WM_TRY(wm_launch_inject_fields(g, inj, uf(), st));
             ++nl;
+            if (inj.n_expand) nl += 3;
+            WM_TRY(finish_expansion());
         }
         mark("rebin_wait");
         // set B now holds the pushed particles in the old cell order: it becomes set A (the ids
@@ -728,6 +768,7 @@ int wm_sim_create(const wm_sim_config *cfg, wm_sim **out)
     g.nrows = g.nsp * g.ny;
     g.nxw = g.nx + 4;
     g.nyw = g.ny + 4;
+    g.nxa = g.nx;  // the whole box unless the shock's expansion is set
     WmConst &k = s->k;
     k.delx = cfg->delx;
     k.delt = cfg->delt;
@@ -888,7 +929,7 @@ int wm_sim_init_shock(wm_sim *s, int n0, double u0, double vth_e, double vth_i, 
     const double c = s->k.c;
     WmInitArgs a{};
     a.tag = WM_RNG_SHOCK;
-    a.n_row = n0 * (g.nxge - g.nxgs - 1);  // np2 = n0*(nxe-nxs-1), proj/shock/app.f90:335, nxs = nxgs, nxe = nxge
+    a.n_row = n0 * (g.nxa - 2);  // np2 = n0*(nxe-nxs-1), proj/shock/app.f90:335, nxs = nxgs, nxe = nxgs + nxa - 1
     a.seed = seed;
     a.vth_e = vth_e;
     a.vth_i = vth_i;
@@ -923,12 +964,12 @@ int wm_sim_set_injection(wm_sim *s, int on, int n0, double vth_e, double vth_i, 
     a.delx = delx;
     a.pflux = n0 * fabs(a.v0) * delt * delx * (g.nyge - g.nygs + 1);  // app.f90:725
     a.x0 = fabs(a.v0) * delt;
-    a.xe = g.nxge * delx;
+    a.xe = (g.nxgs + g.nxa - 1) * delx;
     a.vth_e = vth_e;
     a.vth_i = vth_i;
     a.l_damp_ini = l_damp_ini;
     a.nxgs_delx = g.nxgs * delx;
-    a.cell = g.nx - 2;  // nxe-1 with nxe = nxge
+    a.cell = g.nxa - 2;  // nxe-1
     a.by0 = b0 * sin(theta_bn) * cos(phi_bn);
     a.bz0 = b0 * sin(theta_bn) * sin(phi_bn);
     WM_TRY(s->inj_rows.ensure(sizeof(int) * g.ny));
@@ -936,7 +977,24 @@ int wm_sim_set_injection(wm_sim *s, int on, int n0, double vth_e, double vth_i, 
     WM_TRY(s->inj_nptot.ensure(sizeof(long long) * 2));
     WM_TRY(s->inj_tmp.ensure(sizeof(int) * g.nrows));
     s->inj = a;
+    s->inj_n0 = n0;
     s->inject_on = true;
+    return WM_OK;
+}
+
+int wm_sim_set_expansion(wm_sim *s, int n_x_ini, int intvl_expand)
+{
+    if (!s || s->g.bc != WM_BC_SHOCK || n_x_ini < 3 || n_x_ini > s->g.nx - 1 || intvl_expand < 0) return WM_ERR_BAD_ARG;
+    s->g.nxa = n_x_ini + 1;  // nxe = nxgs + n_x_ini (proj/shock/app.f90:277)
+    s->expand_every = intvl_expand;
+    s->sync_inject_boundary();
+    return WM_OK;
+}
+
+int wm_sim_get_nxe(wm_sim *s, int *nxe)
+{
+    if (!s || !nxe) return WM_ERR_BAD_ARG;
+    *nxe = s->g.nxgs + s->g.nxa - 1;
     return WM_OK;
 }
 
@@ -998,7 +1056,7 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
     std::vector<int> cnt;
     int maxc;
     WM_TRY(sim_row_counts(s, cnt, maxc));
-    if (maxc > g.np) return WM_ERR_OVERFLOW;
+    if (up && maxc > g.np) return WM_ERR_OVERFLOW;  // a row does not fit the host array's np slots
     s->pmark("store_start");
     if (up) {
         const size_t rowb = sizeof(double) * 6 * maxc, hrowb = sizeof(double) * 6 * g.np;
@@ -1202,7 +1260,7 @@ int wm_sim_write_snapshot(wm_sim *s, const char *dir, const char *filename, int 
     const wmpio::Params P = sim_pio_params(s);
     wmpio::Writer w;
     WM_TRY(w.open(dir, filename));
-    WM_TRY(wmpio::write_head(w, P, it, {{"nxs", g.nxgs}, {"nxe", g.nxge}}));
+    WM_TRY(wmpio::write_head(w, P, it, {{"nxs", g.nxgs}, {"nxe", g.nxgs + g.nxa - 1}}));
     WM_TRY(w.dataset("up", "f8", {6, g.np, g.ny, g.nsp, 1}, "particles"));
     WM_TRY(wmpio::write_rows_from_device(w, s->stage.p, sizeof(double) * 6 * maxc, sizeof(double) * 6 * g.np, g.nrows, s->st));
     WM_TRY(w.dataset("np2", "i4", {g.ny, g.nsp, 1}, "number of active particles"));
@@ -1233,7 +1291,9 @@ int wm_sim_read_snapshot(wm_sim *s, const char *dir, const char *filename, int *
     WM_TRY(rd.read_i4("it", *it));
     WM_TRY(rd.read_i4("nxs", nxs));
     WM_TRY(rd.read_i4("nxe", nxe));
-    if (nxs != g.nxgs || nxe != g.nxge) return WM_ERR_UNSUPPORTED;
+    if (nxs != g.nxgs || nxe > g.nxge || (nxe != g.nxge && g.bc != WM_BC_SHOCK) || nxe < g.nxgs + 3) return WM_ERR_UNSUPPORTED;
+    s->g.nxa = nxe - g.nxgs + 1;  // the shock box's extent at the snapshot
+    s->sync_inject_boundary();
     wmpio::Entry e_up, e_np2, e_uf;
     WM_TRY(rd.find("dataset", "up", e_up));
     WM_TRY(rd.find("dataset", "np2", e_np2));

@@ -30,6 +30,7 @@ class Dims:
     ndim: int = 6
     nxgs: int = 2
     nygs: int = 2
+    nxe_act: int = 0  # the active right end nxe when the shock's box expands (0: nxge)
 
     @property
     def nxge(self) -> int:
@@ -53,7 +54,7 @@ class Dims:
 
     @property
     def nxe(self) -> int:
-        return self.nxge
+        return self.nxe_act if self.nxe_act else self.nxge
 
     # ---- allocation in the reference layout
     def alloc_up(self) -> np.ndarray:

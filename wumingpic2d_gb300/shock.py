@@ -4,8 +4,9 @@ load_config (:230-287) and init (:292-336): u0 = -|u_inject| is the upstream fou
 gam0 = sqrt(1 + u0^2/c^2), v0 = u0/gam0; wpe = omega_pe, wge = omega_pe sqrt(sigma_e),
 wpi = wpe/sqrt(mass_ratio), wgi = wge/mass_ratio; r = (mass_ratio, 1);
 q(1) = +sqrt(gam0 r1 / (4 pi n0/delx^2)) wpi, q(2) = -sqrt(gam0 r2 / (4 pi n0/delx^2)) wpe;
-b0 = r1 c / q1 * wgi * gam0; angles given in degrees.  The box here is at full size from the
-start (n_x_ini = nx - 1, so nxe = nxge and no expansion), np2 = n0 (nxe - nxs - 1) per row.
+b0 = r1 c / q1 * wgi * gam0; angles given in degrees.  The box starts at nxe = nxgs + n_x_ini
+(n_x_ini = 0 here: the full box, nxe = nxge), np2 = n0 (nxe - nxs - 1) per row, and grows by one
+cell every intvl_expand steps (0: never) until nxe = nxge.
 """
 from __future__ import annotations
 
@@ -38,6 +39,8 @@ class ShockConfig:
     gfac: float = 0.501
     slack: float = 2.0        # slots per row = slack * n_ppc * nx (the reference allots 5x)
     seed: int = 11
+    n_x_ini: int = 0          # initial box nxe = nxgs + n_x_ini (app.f90:277); 0: the full box, nx - 1
+    intvl_expand: int = 0     # nxe grows by one cell every intvl_expand steps (app.f90:123-125); 0: never
 
     @property
     def delt(self):

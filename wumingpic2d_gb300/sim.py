@@ -122,10 +122,21 @@ class Simulation:
               "wm_sim_init_harris")
 
     def init_shock(self, cfg, inject: bool = True) -> None:
-        """The shock application's upstream plasma for a shock.ShockConfig (full box), with the
-        application's particle injection at the right boundary switched on (inject=True)."""
+        """The shock application's upstream plasma for a shock.ShockConfig, with the application's
+        particle injection at the right boundary switched on (inject=True).  cfg.n_x_ini and
+        cfg.intvl_expand set the expanding box (proj/shock/app.f90:277, :123-125): the plasma fills
+        nxs+1 .. nxe-1 with nxe = nxgs + n_x_ini, and nxe grows by one cell every intvl_expand steps."""
+        n_x_ini = cfg.n_x_ini if cfg.n_x_ini else self.dims.nx - 1
+        check(lib().wm_sim_set_expansion(self._h, int(n_x_ini), int(cfg.intvl_expand)), "wm_sim_set_expansion")
         check(lib().wm_sim_init_shock(self._h, *cfg.init_args()), "wm_sim_init_shock")
         self.set_injection(cfg if inject else None)
+
+    @property
+    def nxe(self) -> int:
+        """The active right end of the box (nxge unless the shock's box is expanding)."""
+        v = ctypes.c_int()
+        check(lib().wm_sim_get_nxe(self._h, ctypes.byref(v)), "wm_sim_get_nxe")
+        return v.value
 
     def set_injection(self, cfg) -> None:
         """Inject the upstream plasma of a shock.ShockConfig every step (None: off)."""

@@ -6,9 +6,9 @@ The same seeded state (generated on the GPU) runs on the FP64 path and on the mi
 each, the energies of proj/weibel/app.f90:507-541 every `every` steps, the growth rate of the
 magnetic energy over the linear phase, and the drift of div E - 4 pi rho (second-order shape,
 which the Esirkepov deposit conserves exactly) between the first and the last step on a strip of
-rows.  Prints one JSON object: per path the total-energy drift and the history, and the mixed
-path against the FP64 one (largest relative difference of the total energy at the samples, ratio
-of the growth rates).
+rows.  Prints one JSON object (and writes it to --out): per path the total-energy drift and the
+history, and the mixed path against the FP64 one (largest relative difference of the total energy
+at the samples, ratio of the growth rates).
 """
 from __future__ import annotations
 
@@ -82,6 +82,8 @@ def run(cfg: WeibelConfig, precision: str, steps: int, every: int, strip=(0, 16)
         "growth_rate": gamma, "growth_window": [t_lo, t_hi],
         "gauss_drift_rel": float(np.max(np.abs(g1 - g0)) / scale),
         "gauss_strip_rows": list(strip),
+        "energy_history": {"step": [int(v) for v in t], "columns": "kinetic per species, electric, magnetic",
+                           "values": hist.tolist()},
     })
     return out, t, hist
 
@@ -95,6 +97,7 @@ def main(argv=None):
     p.add_argument("--every", type=int, default=20)
     p.add_argument("--seed", type=int, default=2024)
     p.add_argument("--paths", default="fp64,mixed")
+    p.add_argument("--out", default=None, help="also write the result object to this JSON file")
     args = p.parse_args(argv)
     cfg = WeibelConfig(nx=args.nx, ny=args.ny, ppc=args.ppc, seed=args.seed, slack=3.0)  # rows bunch up in the filaments
     res, hists = {"workload": f"Weibel {args.nx}x{args.ny}, {args.ppc} ppc/species, {args.steps} steps"}, {}
@@ -111,6 +114,10 @@ def main(argv=None):
             "growth_rate_ratio": float(res["mixed"]["growth_rate"] / res["fp64"]["growth_rate"]),
         }
     print(json.dumps(res), flush=True)
+    if args.out:
+        res["command"] = "python -m wumingpic2d_gb300.validate " + " ".join(argv if argv is not None else __import__("sys").argv[1:])
+        with open(args.out, "w") as f:
+            json.dump(res, f, indent=1)
 
 
 if __name__ == "__main__":
