@@ -16,14 +16,19 @@
  *    array arguments to the GPU, runs the hand-written sm_103a kernels and copies the results
  *    back; elements the reference routine does not write keep their values.  MPI arguments
  *    (mnpi, mnpr, ncomw, opsum, nerr, nstat, nup, ndown) are accepted and ignored: one process
- *    owns the whole periodic domain (nys = nygs, nye = nyge).  A Fortran application binds these
+ *    owns the whole periodic domain (nys = nygs, nye = nyge).  The x range arguments take
+ *    nxs = nxgs and nxe = nxge, or, under the shock's boundary module, a smaller nxe (its growing
+ *    box, proj/shock/app.f90:277 and relocate :613-690): the procedures then work over nxs..nxe as
+ *    the Fortran does (cells, cumcnt(nxs:nxe+1), the field solve and ghosts at nxe+1, phi sized by
+ *    nxe) and leave the rest of the arrays as they are.  A Fortran application binds these
  *    through ISO_C_BINDING; where the reference calls `stop`, these return a nonzero status.
  *
  * 2. Resident simulation (wm_sim_*).  Particles and fields stay on the GPU across steps in a
  *    compact structure-of-arrays layout sorted by (species, row, cell); host arrays in the
  *    reference layout are read at load and written at store.  wm_sim_step runs the main-loop
  *    body of proj/weibel/app.f90:102-107 (particle__solv, field__fdtd_i, bc__particle_x,
- *    bc__particle_y, sort__bucket) with periodic boundaries.
+ *    bc__particle_y, sort__bucket), or the reconnection / shock applications' bodies (their wall
+ *    modules; the shock's injection and expanding box).
  *
  * Every function returns WM_OK (0) or one of the WM_ERR_* codes; wm_status_string names them.
  */

@@ -178,3 +178,47 @@ def test_expanding_box_mixed_tracks_fp64(gpu):
     de = abs(out["mixed"][1].sum() - out["fp64"][1].sum()) / out["fp64"][1].sum()
     print(f"\nexpanding shock box, mixed vs fp64 after 12 steps: x {errs[0]:.1e} y {errs[1]:.1e} u {max(errs[2:]):.1e} energy {de:.1e}")
     assert max(errs) <= 1e-5 and de <= 1e-6
+
+
+def test_expanding_box_dropin_matches_oracle(gpu):
+    """The shock application's own loop (proj/shock/app.f90:110-125) through the drop-in module
+    procedures with a growing nxe: particle__solv, boundary_shock__injection, field__fdtd_i,
+    boundary_shock__particle_y and sort__bucket on the host arrays over nxs..nxe, the
+    application's inject and relocate between the steps (its own code, restated in oracle/init.py,
+    on the host arrays).  Against the oracle's same loop: row counts, the whole cumcnt (entries past
+    nxe + 1 left as they were) and ids exact; positions, momenta and fields to 1e-11."""
+    from dataclasses import replace
+
+    from wumingpic2d_gb300 import api
+
+    cfg = expand_config()
+    steps = 4
+    d_o, up_o, uf_o, np2_o, cc_o = oracle_expand_run(cfg, steps)
+    d = replace(cfg.dims(), nxe_act=cfg.dims().nxgs + cfg.n_x_ini)
+    a = cfg.init_args()
+    up0, uf, np2 = I.shock(d, *a[:-1], seed=a[-1])
+    par = O.make_par(d, cfg.delt, cfg.charge, cfg.mass, bc="shock", u0=cfg.u0)
+    up, cc = d.alloc_up(), d.alloc_cumcnt()
+    assert O.sort_bucket(par, d, up, up0, cc, np2) == 0
+    gp = up.copy(order="F")
+    api.init_all(d, cfg.delt, cfg.charge, cfg.mass, bc="shock")
+    for it in range(steps):
+        api.particle__solv(gp, up, uf, cc, d.nxs, d.nxe)
+        api.boundary_shock__injection(gp, np2, d.nxs, d.nxe, cfg.u0)
+        api.field__fdtd_i(uf, up, gp, cc, d.nxs, d.nxe, api.boundary_shock__dfield, api.boundary_shock__curre,
+                          api.boundary_shock__phi)
+        api.boundary_shock__particle_y(gp, np2)
+        api.sort__bucket(up, gp, cc, np2, d.nxs, d.nxe)
+        I.inject(d, up, uf, np2, cc, it, a[-1], a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], cfg.delt)
+        if (it + 1) % cfg.intvl_expand == 0:
+            d = I.relocate(d, up, uf, np2, cc, it, a[-1], a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7])
+    assert d.nxe == d_o.nxe
+    assert np.array_equal(np2, np2_o) and np.array_equal(cc, cc_o)
+    for isp in range(d.nsp):
+        for j in range(d.ny):
+            m = int(np2[j, isp])
+            assert np.array_equal(up[5, :m, j, isp].view(np.int64), up_o[5, :m, j, isp].view(np.int64))
+            for k in range(5):
+                assert rel_err(up[k, :m, j, isp], up_o[k, :m, j, isp]) <= 1e-11, (isp, j, k)
+    for k in range(6):
+        assert rel_err(uf[k], uf_o[k]) <= 1e-11, k

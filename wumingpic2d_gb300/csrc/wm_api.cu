@@ -243,10 +243,23 @@ int wm_particle_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, in
     return WM_OK;
 }
 
-static int push_dropin(const WmGeom &g, const WmConst &k, double *gp, const double *up, const double *uf, const int *cumcnt,
+// The x range nxs..nxe of a call: nxs = nxgs and nxgs + 3 <= nxe <= nxge, nxe below nxge for the
+// shock application's growing box (proj/shock/app.f90:277, relocate :613-690); the boundary and
+// field procedures take it under the shock's boundary module only (walls_only).  The call's
+// geometry follows nxe (nxa = nxe - nxgs + 1 active cells).
+static int active_range(WmGeom &g, int nxs, int nxe, bool walls_only)
+{
+    if (nxs != g.nxgs || nxe > g.nxge || nxe < g.nxgs + 3) return WM_ERR_UNSUPPORTED;
+    if (nxe != g.nxge && walls_only && g.bc != WM_BC_SHOCK) return WM_ERR_UNSUPPORTED;
+    g.nxa = nxe - g.nxgs + 1;
+    return WM_OK;
+}
+
+static int push_dropin(const WmGeom &g0, const WmConst &k, double *gp, const double *up, const double *uf, const int *cumcnt,
                        int nxs, int nxe, int half)
 {
-    if (nxs != g.nxgs || nxe != g.nxge) return WM_ERR_UNSUPPORTED;
+    WmGeom g = g0;  // cells nxs..nxe (particle.f90:86)
+    WM_TRY(active_range(g, nxs, nxe, false));
     WM_TRY(M.stream());
     cudaStream_t st = M.st;
     const size_t nup = up_doubles(g) * sizeof(double);
@@ -299,7 +312,7 @@ int wm_field_fdtd_i(double *uf, const double *up, const double *gp, const int *c
     if (!M.bc_ok) return WM_ERR_NOT_INIT;  // the boundary procedures: those of the module initialised last
     WmGeom g = M.gfield;
     g.bc = M.bc_kind;
-    if (nxs != g.nxgs || nxe != g.nxge) return WM_ERR_UNSUPPORTED;
+    WM_TRY(active_range(g, nxs, nxe, true));  // deposit, solve and update over nxs..nxe (field.f90:121-184)
     WM_TRY(field_work_ready(g));
     cudaStream_t st = M.st;
     const size_t nup = up_doubles(g) * sizeof(double);
@@ -336,8 +349,8 @@ int wm_sort_init(int ndim, int np, int nsp, int nxgs, int nxge, int nygs, int ny
 int wm_sort_bucket(double *gp, const double *up, int *cumcnt, const int *np2, int nxs, int nxe)
 {
     if (!M.sort_ok) return WM_ERR_NOT_INIT;
-    const WmGeom &g = M.gsort;
-    if (nxs != g.nxgs || nxe != g.nxge) return WM_ERR_UNSUPPORTED;
+    WmGeom g = M.gsort;
+    WM_TRY(active_range(g, nxs, nxe, false));  // cumcnt(nxs:nxe+1) (sort.f90:57-70): the rest of the rows untouched
     if ((long long)g.np * g.nrows >= (1LL << 32)) return WM_ERR_UNSUPPORTED;
     for (int r = 0; r < g.nrows; ++r)
         if (np2[r] < 0 || np2[r] > g.np) return WM_ERR_BAD_ARG;
@@ -361,7 +374,12 @@ int wm_sort_bucket(double *gp, const double *up, int *cumcnt, const int *np2, in
     if (map_status(dev) != WM_OK) return map_status(dev);
     WM_TRY(wm_launch_sort_move(g, va, vb, M.np2.as<int>(), maxc, M.cc.as<int>(), sc, st));
     WM_TRY(d2h(gp, M.b, nup, st));
-    WM_TRY(d2h(cumcnt, M.cc, sizeof(int) * cc_ints(g), st));
+    if (g.nxa == g.nx) {
+        WM_TRY(d2h(cumcnt, M.cc, sizeof(int) * cc_ints(g), st));
+    } else {
+        const size_t pitch = sizeof(int) * (g.nx + 1);
+        WM_CUDA(cudaMemcpy2DAsync(cumcnt, pitch, M.cc.p, pitch, sizeof(int) * (g.nxa + 1), g.nrows, cudaMemcpyDeviceToHost, st));
+    }
     return finish(st);
 }
 
@@ -413,8 +431,8 @@ static int bc_init(int kind, int ndim, int np, int nsp, int nxgs, int nxge, int 
 static int walls_x_dropin(double *up, const int *np2, int nxs, int nxe, int inject, double u0)
 {
     if (!M.bc_ok) return WM_ERR_NOT_INIT;
-    const WmGeom &g = M.gbc;
-    if (nxs != g.nxgs || nxe != g.nxge) return WM_ERR_UNSUPPORTED;
+    WmGeom g = M.gbc;
+    WM_TRY(active_range(g, nxs, nxe, false));
     for (int r = 0; r < g.nrows; ++r)
         if (np2[r] < 0 || np2[r] > g.np) return WM_ERR_BAD_ARG;
     WM_TRY(M.stream());
@@ -522,11 +540,10 @@ int wm_bc_periodic_particle_y(double *up, int *np2)
     return finish(st);
 }
 
-static int check_range_args(const WmGeom &g, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
+static int check_range_args(WmGeom &g, int nxs, int nxe, int nys, int nye, int nxgs, int nxge)
 {
-    if (nxs != g.nxgs || nxe != g.nxge || nys != g.nys || nye != g.nye || nxgs != g.nxgs || nxge != g.nxge)
-        return WM_ERR_UNSUPPORTED;
-    return WM_OK;
+    if (nys != g.nys || nye != g.nye || nxgs != g.nxgs || nxge != g.nxge) return WM_ERR_UNSUPPORTED;
+    return active_range(g, nxs, nxe, true);
 }
 
 // The ghost routines of the three boundary modules share one implementation each; kind selects
@@ -562,13 +579,15 @@ static int curre_impl(int kind, double *uj, int nxs, int nxe, int nys, int nye, 
 static int phi_impl(int kind, double *phi, int nxs, int nxe, int nys, int nye, int l)
 {
     if (!M.bc_ok) return WM_ERR_NOT_INIT;
-    const WmGeom &g = M.gbc;
-    if (nxs != g.nxgs || nxe != g.nxge || nys != g.nys || nye != g.nye) return WM_ERR_UNSUPPORTED;
+    WmGeom g = M.gbc;
+    g.bc = kind;
+    if (nys != g.nys || nye != g.nye) return WM_ERR_UNSUPPORTED;
+    WM_TRY(active_range(g, nxs, nxe, true));  // phi(nxs-1:nxe+1, nys-1:nye+1)
     if (l < 1 || l > 3) return WM_ERR_BAD_ARG;
     WM_TRY(M.stream());
-    const size_t bytes = sizeof(double) * (size_t)(g.nx + 2) * (g.ny + 2);
+    const size_t bytes = sizeof(double) * (size_t)(g.nxa + 2) * (g.ny + 2);
     WM_TRY(h2d(M.phi, phi, bytes, M.st));
-    WM_TRY(wm_launch_phi_bc(g.nx, g.ny, M.phi.as<double>(), kind, l, M.st));
+    WM_TRY(wm_launch_phi_bc(g.nxa, g.ny, M.phi.as<double>(), kind, l, M.st));
     WM_TRY(d2h(phi, M.phi, bytes, M.st));
     return finish(M.st);
 }

@@ -119,11 +119,14 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __nv_bfloat16 *w_s = reinterpret_cast<__nv_bfloat16 *>(smem_raw);        // [9][KG][NOUT][8]
     __nv_bfloat16 *x_all = w_s + 9 * KG * NOUT * 8;                           // [group][2][KG][TC_XP][8]
-    uint64_t *bar_all = reinterpret_cast<uint64_t *>(x_all + TC_GROUPS * 2 * KG * TC_XP * 8);  // [group][halo 0, halo 1, MMA]
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar_all + 3 * TC_GROUPS);
+    uint64_t *bar_all = reinterpret_cast<uint64_t *>(x_all + TC_GROUPS * 2 * KG * TC_XP * 8);  // [group][halo 0, halo 1, MMA 0, MMA 1]
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bar_all + 4 * TC_GROUPS);
     __shared__ int give_up[TC_GROUPS];
+    __shared__ float bias_s[NOUT];  // the layer's biases, read by every epilogue from shared memory
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int grp = tid >> 7, gtid = tid & 127, gwarp = warp & 3;  // group, thread and warp in the group
+    if constexpr (EPI != 3)
+        for (int e = tid; e < NOUT; e += blockDim.x) bias_s[e] = e < COUT ? bias[e] : 0.f;
 
     for (int e = tid; e < 9 * NOUT * KG; e += blockDim.x) {  // [9][COUT][CIN] -> core-matrix rows, zero rows past COUT
         const int kg = e % KG, co = (e / KG) % NOUT, tap = e / (KG * NOUT);
@@ -131,12 +134,12 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
             co < COUT ? *reinterpret_cast<const uint4 *>(wk + ((long long)tap * COUT + co) * CIN + kg * 8) : make_uint4(0u, 0u, 0u, 0u);
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)), "r"(TC_GROUPS * TMEM_COLS)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(tslot)), "r"(TC_GROUPS * 2 * TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        for (int b = 0; b < 3 * TC_GROUPS; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar_all + b)) : "memory");
+        for (int b = 0; b < 4 * TC_GROUPS; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bar_all + b)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         for (int g2 = 0; g2 < TC_GROUPS; ++g2) give_up[g2] = 0;
     }
@@ -144,10 +147,9 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    const uint32_t tmem = *tslot + (uint32_t)(grp * TMEM_COLS);  // this group's accumulator columns
-    uint64_t *bars = bar_all + 3 * grp;
+    const uint32_t tmem = *tslot + (uint32_t)(grp * 2 * TMEM_COLS);  // this group's two accumulators
+    uint64_t *bars = bar_all + 4 * grp;                                  // [halo 0, halo 1, MMA 0, MMA 1]
     __nv_bfloat16 *x_s = x_all + grp * 2 * KG * TC_XP * 8;
-    const uint32_t mma_bar = saddr(bars + 2);
     const uint32_t ws_a = saddr(w_s);
     auto xs = [&](int buf) { return saddr(x_s + buf * KG * TC_XP * 8); };
     auto gsync = [&]() { asm volatile("bar.sync %0, 128;\n" ::"r"(1 + grp) : "memory"); };
@@ -162,55 +164,46 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
         x0 = (rem % ntx) * TC_TW;
     };
     auto inside = [&](int y0, int x0) { return y0 >= 1 && y0 + TC_TH + 1 <= H && x0 >= 1 && x0 + TC_TW + 1 <= W; };
-    uint32_t pending = 0u, hph = 0u, mph = 0u;  // bit b: a TMA halo copy in flight into buffer b, its barrier's phase
-    auto issue = [&](int buf, int n, int y0, int x0) {  // one thread
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(bars + buf)), "r"((uint32_t)(KG * TC_HPIX * 16))
-                     : "memory");
+    // bit b: a TMA halo copy in flight into buffer b, its barrier's phase; MMAs committed to MMA
+    // barrier b and not yet waited for, that barrier's phase
+    uint32_t pending = 0u, hph = 0u, mma_out = 0u, mph = 0u;
+    auto issue = [&](int buf, long long t) {  // all threads: the TMA copy of tile t's halo (one thread issues it)
+        int n, y0, x0;
+        coords(t, n, y0, x0);
+        if (!inside(y0, x0)) return;  // periodic halo across the image edges: plain loads later
+        if (gtid == 0) {
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(saddr(bars + buf)), "r"((uint32_t)(KG * TC_HPIX * 16))
+                         : "memory");
 #pragma unroll
-        for (int kg = 0; kg < KG; ++kg) tma_halo(xs(buf) + (uint32_t)(kg * TC_XP * 16), &tmap, kg * 8, x0 - 1, y0 - 1, n, saddr(bars + buf));
+            for (int kg = 0; kg < KG; ++kg) tma_halo(xs(buf) + (uint32_t)(kg * TC_XP * 16), &tmap, kg * 8, x0 - 1, y0 - 1, n, saddr(bars + buf));
+        }
+        pending |= 1u << buf;
     };
-    if (tfirst < ntiles) {
-        int n, y0, x0;
-        coords(tfirst, n, y0, x0);
-        if (inside(y0, x0)) {
-            if (gtid == 0) issue(0, n, y0, x0);
-            pending |= 1u;
-        }
-    }
-    int buf = 0;
-    for (long long tile = tfirst; tile < ntiles; tile += tstride, buf ^= 1) {
-        int n, y0, x0;
-        coords(tile, n, y0, x0);
-        const long long nt = tile + tstride;  // the next tile's halo into the other buffer
-        if (nt < ntiles) {
-            int n1, y1, x1;
-            coords(nt, n1, y1, x1);
-            if (inside(y1, x1)) {
-                if (gtid == 0) issue(buf ^ 1, n1, y1, x1);
-                pending |= 1u << (buf ^ 1);
-            }
-        }
-        if (pending & (1u << buf)) {  // this tile's halo came by TMA
-            if (!mbar_wait(saddr(bars + buf), (hph >> buf) & 1u)) give_up[grp] = 1;
+    auto halo_ready = [&](int buf, long long t) -> bool {  // all threads: tile t's halo in buffer buf
+        if (pending & (1u << buf)) {  // it came by TMA
+            const bool ok = mbar_wait(saddr(bars + buf), (hph >> buf) & 1u);
             hph ^= 1u << buf;
             pending &= ~(1u << buf);
-        } else {  // periodic halo across the image edges: plain loads
-            __nv_bfloat16 *xb = x_s + buf * KG * TC_XP * 8;
-            for (int e = gtid; e < TC_HPIX * KG; e += 128) {
-                const int kg = e % KG, pix = e / KG, hy = pix / TC_HW, hx = pix % TC_HW;
-                int yy = y0 - 1 + hy, xx = x0 - 1 + hx;
-                yy += (yy < 0) ? H : (yy >= H ? -H : 0);
-                xx += (xx < 0) ? W : (xx >= W ? -W : 0);
-                *reinterpret_cast<uint4 *>(xb + (kg * TC_XP + pix) * 8) =
-                    *reinterpret_cast<const uint4 *>(in + (((long long)n * H + yy) * W + xx) * CIN + kg * 8);
-            }
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the halo stores, seen by the tensor core
+            return ok;
         }
-        gsync();
-        if (give_up[grp]) break;
+        int n, y0, x0;
+        coords(t, n, y0, x0);
+        __nv_bfloat16 *xb = x_s + buf * KG * TC_XP * 8;
+        for (int e = gtid; e < TC_HPIX * KG; e += 128) {
+            const int kg = e % KG, pix = e / KG, hy = pix / TC_HW, hx = pix % TC_HW;
+            int yy = y0 - 1 + hy, xx = x0 - 1 + hx;
+            yy += (yy < 0) ? H : (yy >= H ? -H : 0);
+            xx += (xx < 0) ? W : (xx >= W ? -W : 0);
+            *reinterpret_cast<uint4 *>(xb + (kg * TC_XP + pix) * 8) =
+                *reinterpret_cast<const uint4 *>(in + (((long long)n * H + yy) * W + xx) * CIN + kg * 8);
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the halo stores, seen by the tensor core
+        return true;
+    };
+    auto issue_mma = [&](int buf) {  // tile in halo buffer buf -> accumulator buf, committed to MMA barrier buf
         if (gtid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            const uint32_t xa = xs(buf);
+            const uint32_t xa = xs(buf), acc = tmem + (uint32_t)(buf * TMEM_COLS);
 #pragma unroll
             for (int tap = 0; tap < 9; ++tap) {
                 const int dy = tap / 3 - 1, dx = tap % 3 - 1;
@@ -218,24 +211,52 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
                 for (int ks = 0; ks < KG / 2; ++ks) {
                     const uint64_t ad = smem_desc(xa + (uint32_t)((2 * ks * TC_XP + (dy + 1) * TC_HW + dx + 1) * 16), TC_XP * 16, TC_HW * 16);
                     const uint64_t bd = smem_desc(ws_a + (uint32_t)(((tap * KG + 2 * ks) * NOUT) * 16), NOUT * 16, 8 * 16);
-                    mma_f16(tmem, ad, bd, IDESC, (tap | ks) != 0 ? 1u : 0u);
+                    mma_f16(acc, ad, bd, IDESC, (tap | ks) != 0 ? 1u : 0u);
                 }
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mma_bar) : "memory");
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(bars + 2 + buf))
+                         : "memory");
         }
-        if (!mbar_wait(mma_bar, mph)) give_up[grp] = 1;
-        mph ^= 1u;
+        mma_out |= 1u << buf;
+    };
+    // Tile i of the group: halo buffer and accumulator i & 1.  Tile i+1's MMAs are issued before
+    // tile i's epilogue, so they run while it reads the other accumulator; tile i+2's halo copy
+    // starts once tile i's MMAs are done with its buffer.
+    if (tfirst < ntiles) {
+        issue(0, tfirst);
+        if (tfirst + tstride < ntiles) issue(1, tfirst + tstride);
+        if (!halo_ready(0, tfirst)) give_up[grp] = 1;
+        gsync();
+        if (!give_up[grp]) issue_mma(0);
+    }
+    int i = 0;
+    for (long long tile = tfirst; tile < ntiles && !give_up[grp]; tile += tstride, ++i) {
+        const int b = i & 1;
+        int n, y0, x0;
+        coords(tile, n, y0, x0);
+        const long long nt = tile + tstride;
+        if (nt < ntiles) {  // the next tile's MMAs into the other accumulator (its epilogue of tile i-1 ended at the last barrier)
+            if (!halo_ready(b ^ 1, nt)) give_up[grp] = 1;
+            gsync();
+            if (give_up[grp]) break;
+            issue_mma(b ^ 1);
+        }
+        if (!mbar_wait(saddr(bars + 2 + b), (mph >> b) & 1u)) give_up[grp] = 1;
+        mph ^= 1u << b;
+        mma_out &= ~(1u << b);
+        if (tile + 2 * tstride < ntiles) issue(b, tile + 2 * tstride);  // buffer b is free: tile i's MMAs are done
         gsync();
         if (give_up[grp]) break;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         // epilogue, 16 columns at a time: warp w of the group holds TMEM lanes 32w..32w+31 = MMA
         // rows m = 8 r + c
+        const uint32_t acc = tmem + (uint32_t)(b * TMEM_COLS);
         const int m = 32 * gwarp + lane, r = m >> 3, c = m & 7;
         const long long p = ((long long)n * H + y0 + r) * W + x0 + c;
 #pragma unroll
         for (int q = 0; q < NOUT / 16; ++q) {
             float v[16];
-            tmem_ld16(tmem + ((uint32_t)(32 * gwarp) << 16) + (uint32_t)(16 * q), v);
+            tmem_ld16(acc + ((uint32_t)(32 * gwarp) << 16) + (uint32_t)(16 * q), v);
             asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             if constexpr (EPI == 3) {
 #pragma unroll
@@ -245,11 +266,11 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
                     const uint32_t zw[4] = {zz.x, zz.y, zz.z, zz.w};
                     uint32_t ga[4];
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const __nv_bfloat162 zp = *reinterpret_cast<const __nv_bfloat162 *>(&zw[i]);
-                        const __nv_bfloat162 gg = __floats2bfloat162_rn(v[8 * h + 2 * i] * gelu_grad_tc(__bfloat162float(zp.x)),
-                                                                        v[8 * h + 2 * i + 1] * gelu_grad_tc(__bfloat162float(zp.y)));
-                        ga[i] = *reinterpret_cast<const uint32_t *>(&gg);
+                    for (int i2 = 0; i2 < 4; ++i2) {
+                        const __nv_bfloat162 zp = *reinterpret_cast<const __nv_bfloat162 *>(&zw[i2]);
+                        const __nv_bfloat162 gg = __floats2bfloat162_rn(v[8 * h + 2 * i2] * gelu_grad_tc(__bfloat162float(zp.x)),
+                                                                        v[8 * h + 2 * i2 + 1] * gelu_grad_tc(__bfloat162float(zp.y)));
+                        ga[i2] = *reinterpret_cast<const uint32_t *>(&gg);
                     }
                     *reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + p * NOUT + co) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
                 }
@@ -257,19 +278,19 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
                 float *o = static_cast<float *>(out) + p * COUT;
 #pragma unroll
                 for (int h = 0; h < COUT / 4; ++h)
-                    *reinterpret_cast<float4 *>(o + 4 * h) = make_float4(v[4 * h] + bias[4 * h], v[4 * h + 1] + bias[4 * h + 1],
-                                                                         v[4 * h + 2] + bias[4 * h + 2], v[4 * h + 3] + bias[4 * h + 3]);
+                    *reinterpret_cast<float4 *>(o + 4 * h) = make_float4(v[4 * h] + bias_s[4 * h], v[4 * h + 1] + bias_s[4 * h + 1],
+                                                                         v[4 * h + 2] + bias_s[4 * h + 2], v[4 * h + 3] + bias_s[4 * h + 3]);
             } else {
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int co = 16 * q + 8 * h;
                     uint32_t za[4], ga[4];
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const float z0 = v[8 * h + 2 * i] + bias[co + 2 * i], z1 = v[8 * h + 2 * i + 1] + bias[co + 2 * i + 1];
+                    for (int i2 = 0; i2 < 4; ++i2) {
+                        const float z0 = v[8 * h + 2 * i2] + bias_s[co + 2 * i2], z1 = v[8 * h + 2 * i2 + 1] + bias_s[co + 2 * i2 + 1];
                         const __nv_bfloat162 zz = __floats2bfloat162_rn(z0, z1), gg = __floats2bfloat162_rn(gelu_tc(z0), gelu_tc(z1));
-                        za[i] = *reinterpret_cast<const uint32_t *>(&zz);
-                        ga[i] = *reinterpret_cast<const uint32_t *>(&gg);
+                        za[i2] = *reinterpret_cast<const uint32_t *>(&zz);
+                        ga[i2] = *reinterpret_cast<const uint32_t *>(&gg);
                     }
                     if constexpr (EPI == 0) *reinterpret_cast<uint4 *>(zout + p * NOUT + co) = make_uint4(za[0], za[1], za[2], za[3]);
                     *reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(out) + p * NOUT + co) = make_uint4(ga[0], ga[1], ga[2], ga[3]);
@@ -277,17 +298,18 @@ __global__ void __launch_bounds__(128 * TC_GROUPS, 2) k_conv3x3_tc(const __grid_
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        gsync();  // TMEM read before the group's next MMAs
+        gsync();  // accumulator b read before the MMAs of tile i+2 go into it
     }
     if (give_up[grp]) {  // the copies and MMAs still in flight, if any (bounded), before the TMEM goes
         if (gtid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < 2; ++b) {
             if (pending & (1u << b)) mbar_wait(saddr(bars + b), (hph >> b) & 1u);
-        mbar_wait(mma_bar, mph ^ 1u);
+            if (mma_out & (1u << b)) mbar_wait(saddr(bars + 2 + b), (mph >> b) & 1u);
+        }
     }
     __syncthreads();
     if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(*tslot), "r"(TC_GROUPS * TMEM_COLS) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(*tslot), "r"(TC_GROUPS * 2 * TMEM_COLS) : "memory");
 }
 
 template <int CIN, int NOUT, int COUT, int EPI>
@@ -300,10 +322,10 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
     const unsigned long long gstride[3] = {(unsigned long long)CIN * 2, (unsigned long long)W * CIN * 2, (unsigned long long)H * W * CIN * 2};
     const unsigned box[4] = {8, TC_HW, TC_TH + 2, 1};
     WM_TRY(wm_tensor_map(&tmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, in, gdim, gstride, box));
-    const size_t smem = 16 * (size_t)(9 * KG * NOUT + TC_GROUPS * 2 * KG * TC_XP) + 8 * 3 * TC_GROUPS + 16;
+    const size_t smem = 16 * (size_t)(9 * KG * NOUT + TC_GROUPS * 2 * KG * TC_XP) + 8 * 4 * TC_GROUPS + 16;
     WM_CUDA(cudaFuncSetAttribute(k_conv3x3_tc<CIN, NOUT, COUT, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long ntiles = (long long)nimg * (H / TC_TH) * (W / TC_TW);
-    // resident CTAs per SM: at most 2 (registers; 2 x 2 x 64 TMEM columns of 512), within the shared memory
+    // resident CTAs per SM: at most 2 (registers; 2 x 2 groups x 2 accumulators x 64 TMEM columns = all 512), within the shared memory
     const int per_sm = std::max(1, std::min(2, (int)(233472 / (smem + 2048))));  // 228 KB per SM, 2 KB per CTA for the static part and the system
     const int grid = (int)std::min<long long>((ntiles + TC_GROUPS - 1) / TC_GROUPS, 152LL * per_sm);
     k_conv3x3_tc<CIN, NOUT, COUT, EPI><<<grid, 128 * TC_GROUPS, smem, st>>>(tmap, static_cast<const __nv_bfloat16 *>(in),
@@ -329,10 +351,11 @@ int launch_tc(const void *in, const void *wk, const float *bias, int nimg, int H
 // co: rows past coutp read whatever the shared memory holds beyond the staged channels, and their
 // accumulator lanes are never read (every D row depends on its own A row only).  Three FP32
 // accumulators in tensor memory (dx = -1, 0, 1; 3 cin columns each) sum the CTA's tiles; the
-// next tile is staged into the other buffer while the current tile's 24 MMAs (8 K steps of 16
-// pixels x 3 dx) run.  Per-CTA partials [cta][9][coutp][cin] + [coutp] as k_conv3x3_wgrad writes
+// next two tiles are copied in (cp.async, three buffers) while the current tile's 24 MMAs (8 K
+// steps of 16 pixels x 3 dx) run.  Per-CTA partials [cta][9][coutp][cin] + [coutp] as k_conv3x3_wgrad writes
 // them; k_reduce_wgrad sums them in CTA order.  Waits are bounded (WMDEV_TIMEOUT, TMEM freed).
 constexpr uint32_t WG_MARGIN = 32768;  // shared memory past the buffers: the M = 128 rows of the A operand stay inside it
+constexpr int WG_NB = 3;               // staging buffers: a tile in use, two being copied in
 template <int CIN, int COUTP, bool GROUPED>
 __global__ void __launch_bounds__(128, 1) k_conv3x3_wgrad_tc(const __nv_bfloat16 *__restrict__ x, const __nv_bfloat16 *__restrict__ dz, int nimg,
                                                              int H, int W, float *__restrict__ part, unsigned *status)
@@ -348,10 +371,10 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_wgrad_tc(const __nv_bfloat16
                                ((uint32_t)(128 >> 4) << 24);
     static_assert(N3 % 16 == 0 && N3 <= 256, "N of an M = 128 MMA");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char *dz_s = smem_raw;                              // [2][DG][128][8] BF16
-    unsigned char *x_s = smem_raw + 2 * DB;                      // [2][18][KG][10][8] BF16
-    uint64_t *bars = reinterpret_cast<uint64_t *>(x_s + 2 * XB);  // MMA completion of buffer 0, 1
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + 2);
+    unsigned char *dz_s = smem_raw;                                   // [WG_NB][DG][128][8] BF16
+    unsigned char *x_s = smem_raw + WG_NB * DB;                       // [WG_NB][18][KG][10][8] BF16
+    uint64_t *bars = reinterpret_cast<uint64_t *>(x_s + WG_NB * XB);  // MMA completion of each buffer's tile
+    uint32_t *tslot = reinterpret_cast<uint32_t *>(bars + WG_NB);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (warp == 0) {
@@ -359,7 +382,7 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_wgrad_tc(const __nv_bfloat16
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        for (int b = 0; b < 2; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bars + b)) : "memory");
+        for (int b = 0; b < WG_NB; ++b) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(bars + b)) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -369,7 +392,11 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_wgrad_tc(const __nv_bfloat16
 
     const int ntx = W / TC_TW, nty = H / TC_TH;
     const long long ntiles = (long long)nimg * nty * ntx;
-    auto stage = [&](long long t, int b) {
+    auto cp16 = [](void *dst, const void *src) {
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(saddr(dst)), "l"(src) : "memory");
+    };
+    auto commit = []() { asm volatile("cp.async.commit_group;\n" ::: "memory"); };
+    auto stage = [&](long long t, int b) {  // tile t into buffer b by asynchronous 16-byte copies
         const int n = (int)(t / ((long long)nty * ntx));
         const int rem = (int)(t % ((long long)nty * ntx));
         const int y0 = (rem / ntx) * TC_TH, x0 = (rem % ntx) * TC_TW;
@@ -379,35 +406,49 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_wgrad_tc(const __nv_bfloat16
             int yy = y0 - 1 + hy, xx = x0 - 1 + hx;
             yy += (yy < 0) ? H : (yy >= H ? -H : 0);
             xx += (xx < 0) ? W : (xx >= W ? -W : 0);
-            *reinterpret_cast<uint4 *>(xb + hy * ROW + kg * (TC_HW * 16) + hx * 16) =
-                *reinterpret_cast<const uint4 *>(x + (((long long)n * H + yy) * W + xx) * CIN + kg * 8);
+            cp16(xb + hy * ROW + kg * (TC_HW * 16) + hx * 16, x + (((long long)n * H + yy) * W + xx) * CIN + kg * 8);
         }
         unsigned char *db = dz_s + b * DB;
         for (int e = tid; e < 128 * DG; e += 128) {  // the tile's pixels p = 8 r + c, [group][p][8]
             const int g = e % DG, p = e / DG;
-            *reinterpret_cast<uint4 *>(db + g * 2048 + p * 16) =
-                *reinterpret_cast<const uint4 *>(dz + (((long long)n * H + y0 + (p >> 3)) * W + x0 + (p & 7)) * COUTP + g * 8);
+            cp16(db + g * 2048 + p * 16, dz + (((long long)n * H + y0 + (p >> 3)) * W + x0 + (p & 7)) * COUTP + g * 8);
         }
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // the staged tile, seen by the tensor core
     };
     float dbias = 0.f;
-    auto bias_sum = [&](int b) {  // db(co) over the tile's pixels, in pixel order
+    auto bias_sum = [&](int b) {  // db(co) over the tile's pixels: four interleaved partial sums, added in a fixed order
         if (tid < COUTP) {
             const __nv_bfloat16 *d = reinterpret_cast<const __nv_bfloat16 *>(dz_s + b * DB + (tid >> 3) * 2048) + (tid & 7);
-            for (int p = 0; p < 128; ++p) dbias += __bfloat162float(d[p * 8]);
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll 8
+            for (int p = 0; p < 128; p += 4) {
+                s0 += __bfloat162float(d[p * 8]);
+                s1 += __bfloat162float(d[(p + 1) * 8]);
+                s2 += __bfloat162float(d[(p + 2) * 8]);
+                s3 += __bfloat162float(d[(p + 3) * 8]);
+            }
+            dbias += (s0 + s1) + (s2 + s3);
         }
     };
 
-    uint32_t ph = 0u;  // bit b: phase of buffer b's MMA barrier
+    // Tile it of the CTA lives in buffer it % WG_NB; tiles it+1 and it+2 are being copied in
+    // meanwhile.  The MMAs of tile it commit to barrier it % WG_NB; buffer (it+2) % WG_NB is
+    // refilled once the MMAs of tile it-1, its last reader, are done.
+    uint32_t ph = 0u;  // bit b: phase of MMA barrier b
     long long tile = blockIdx.x;
     int it = 0;
     int ncommit = 0;                  // tiles whose MMAs were issued (one commit each)
     bool fail = false, stop = false;  // this thread's wait gave up; some thread's did (block-uniform)
-    if (tile < ntiles) stage(tile, 0);
-    __syncthreads();
-    if (tile < ntiles) bias_sum(0);
+    for (int k = 0; k < 2; ++k) {
+        const long long t = tile + (long long)k * gridDim.x;
+        if (t < ntiles) stage(t, k);
+        commit();
+    }
     for (; tile < ntiles; tile += gridDim.x, ++it) {
-        const int b = it & 1;
+        const int b = it % WG_NB;
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");          // this tile's copies are in
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // and visible to the tensor core
+        __syncthreads();
+        bias_sum(b);
         if (tid == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const uint32_t da = saddr(dz_s + b * DB), xa = saddr(x_s + b * XB);
@@ -423,20 +464,20 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3_wgrad_tc(const __nv_bfloat16
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(saddr(bars + b)) : "memory");
         }
         ncommit = it + 1;
-        const long long nt = tile + gridDim.x;
-        if (nt < ntiles) {
-            if (it >= 1) {  // the previous tile's MMAs read the other buffer
-                fail = !mbar_wait(saddr(bars + (b ^ 1)), (ph >> (b ^ 1)) & 1u);
-                ph ^= 1u << (b ^ 1);
-            }
-            if (!fail) stage(nt, b ^ 1);
+        if (it >= 1) {  // tile it-1's MMAs: the last readers of the buffer refilled next
+            const int pb = (it - 1) % WG_NB;
+            fail = !mbar_wait(saddr(bars + pb), (ph >> pb) & 1u);
+            ph ^= 1u << pb;
         }
+        const long long t2 = tile + 2LL * gridDim.x;
+        if (!fail && t2 < ntiles) stage(t2, (it + 2) % WG_NB);
+        commit();  // (empty groups keep the count that the wait above relies on)
         stop = __syncthreads_or(fail) != 0;
         if (stop) break;
-        if (nt < ntiles) bias_sum(b ^ 1);
     }
-    const int last = (ncommit - 1) & 1;  // the last commit covers every MMA issued before it
+    const int last = (ncommit - 1) % WG_NB;  // the last commit covers every MMA issued before it
     if (!stop && ncommit > 0) stop = __syncthreads_or(!mbar_wait(saddr(bars + last), (ph >> last) & 1u)) != 0;
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
     if (stop) {  // the MMAs still in flight (bounded) before the TMEM goes; the partials are not written
         if (tid == 0) atomicOr(status, (unsigned)WMDEV_TIMEOUT);
         if (ncommit > 0) mbar_wait(saddr(bars + last), (ph >> last) & 1u);
@@ -475,7 +516,7 @@ int launch_wgrad_tc(const void *x, const void *dz, int nimg, int H, int W, float
                     cudaStream_t st)
 {
     constexpr uint32_t DB = (COUTP / 8) * 2048, XB = (TC_TH + 2) * (CIN / 8) * TC_HW * 16;
-    const size_t smem = 2 * (size_t)DB + 2 * (size_t)XB + 64 + WG_MARGIN;
+    const size_t smem = WG_NB * ((size_t)DB + XB) + 64 + WG_MARGIN;
     WM_CUDA(cudaFuncSetAttribute(k_conv3x3_wgrad_tc<CIN, COUTP, GROUPED>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     static int nsm = 0;
     if (!nsm) {

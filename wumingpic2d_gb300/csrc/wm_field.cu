@@ -29,7 +29,7 @@ constexpr int CG_BLOCKS = 152 * 4;  // one wave: 4 CTAs of 256 threads on each o
 template <class FV>
 __global__ void k_curre_bc_y(WmGeom g, FV uj)
 {
-    const int nxr = g.nx + 4;
+    const int nxr = g.nxa + 4;  // columns nxs-2 .. nxe+2
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nxr * 3) return;
     const int ix = t % nxr, k = t / nxr;
@@ -69,8 +69,8 @@ template <class FV>
 __global__ void k_dfield_bc_y(WmGeom g, FV df)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= g.nx * 6) return;
-    const int ix = 2 + t % g.nx, k = t / g.nx;  // interior columns only (:263-345)
+    if (t >= g.nxa * 6) return;
+    const int ix = 2 + t % g.nxa, k = t / g.nxa;  // interior columns nxs..nxe only (:263-345)
     df(k, ix, g.ny + 2) = df(k, ix, 2);
     df(k, ix, g.ny + 3) = df(k, ix, 3);
     df(k, ix, 0) = df(k, ix, g.ny);
@@ -98,8 +98,8 @@ __global__ void k_dfield_bc_x(WmGeom g, FV df)
     if (g.bc == WM_BC_RECONNECTION) {  // conducting wall at nxe (ghosted nx+1), mirror of the left
         if (k == 0 || k >= 4) df(k, g.nx + 1, iy) = -df(k, g.nx, iy);
         else df(k, g.nx + 2, iy) = df(k, g.nx, iy);
-    } else {  // shock: zero beyond the injection boundary
-        df(k, g.nx + 2, iy) = 0.0;
+    } else {  // shock: zero beyond the injection boundary, column nxe+1
+        df(k, g.nxa + 2, iy) = 0.0;
     }
 }
 

@@ -30,7 +30,8 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push(WmGeom g, WmConst kc, PV 
     __shared__ int cc[WM_MAX_SP][PUSH_TW + 1];
     const int j = g.nys + blockIdx.y;
     const int i0 = g.nxgs + blockIdx.x * PUSH_TW;
-    const int ncell = min(PUSH_TW, g.nxge + 1 - i0);
+    const int ncell = min(PUSH_TW, g.nxgs + g.nxa - i0);  // cells nxs..nxe (particle.f90:86)
+    if (ncell <= 0) return;                             // past nxe: the shock's box has not reached this tile
     const int tw = ncell + 2;
 
     // cell-centred fields tmp(1:6, i0-1:i0+ncell, j-1:j+1), particle.f90:68-81
@@ -155,7 +156,8 @@ __global__ void __launch_bounds__(DEP_THREADS) k_deposit_cells(WmGeom g, WmConst
     for (int isp = 0; isp < g.nsp; ++isp) {
         const int row = isp * g.ny + cj;
         const long long ccb = (long long)(g.nx + 1) * row;
-        const int s_beg = cumcnt[ccb + ci], s_end = cumcnt[ccb + ci + 1];
+        // cells nxs..nxe (field.f90:213); past nxe cumcnt is not maintained (the shock's box)
+        const int s_beg = ci < g.nxa ? cumcnt[ccb + ci] : 0, s_end = ci < g.nxa ? cumcnt[ccb + ci + 1] : 0;
         const double qs = kc.q[isp];
         const double mqdd = -(qs * kc.delx * d_delt);
         for (int s = s_beg; s < s_end; ++s) {
