@@ -51,6 +51,13 @@ __global__ void __launch_bounds__(PUSH_THREADS) k_push(WmGeom g, WmConst kc, PV 
         cc[isp][c] = cumcnt[(i0 + c - g.nxgs) + (long long)(g.nx + 1) * row];
     }
     __syncthreads();
+    // Each cell's particles are cumcnt(i)+1 .. cumcnt(i+1) (particle.f90:86-88), none where that
+    // range is reversed: the shock application's injection raises cumcnt(nxe) alone, and past a
+    // growing nxe the entry cumcnt(nxe+1) is not maintained.  The running maximum turns the
+    // starts into one ascending sequence with the same cells.
+    if (threadIdx.x < g.nsp)
+        for (int c = 1; c <= ncell; ++c) cc[threadIdx.x][c] = max(cc[threadIdx.x][c], cc[threadIdx.x][c - 1]);
+    __syncthreads();
 
     const double d_delx = 1. / kc.delx;
     const double delt = half_step ? kc.delt * 0.5 : kc.delt;
