@@ -199,6 +199,7 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
     float4(*xq4)[MX_XQ] = reinterpret_cast<float4(*)[MX_XQ]>(qpj);                           // old dx, dy; new dx, dy
     float2(*xq2)[MX_XQ] = reinterpret_cast<float2(*)[MX_XQ]>(qpj + MX_TW * MX_XQ * 16);      // q vz; increments + 1 (2-bit fields)
     __shared__ int cc[MX_TW + 1];
+    __shared__ unsigned char cord[MX_TW];  // the tile's cells by particle count, most first: lane group g takes cell cord[g]
     __shared__ float spc[5];
     __shared__ float4 pbuf4[MX_NBUF][MX_THREADS];   // each lane's next particles, MX_PFD ahead: (dx, dy, ux, uy)
     __shared__ float pbufz[MX_NBUF][MX_THREADS];    // and uz
@@ -271,10 +272,23 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
         }
     }
     for (int e = tid; e < MX_TW * 9; e += MX_THREADS) (&dcnt[0][0])[e] = 0;
+    // A warp runs as many iterations as its fullest cell needs, so the cells are dealt to the
+    // lane groups in order of their particle counts: each warp gets cells of similar counts and
+    // fewer lanes run past the end of theirs.  (Only the warp a cell lands in changes: its lanes,
+    // their particles and every sum stay the same.)
+    if (tid < MX_TW) {
+        const int nme = tid < ncell ? cc[tid + 1] - cc[tid] : -1;
+        int rank = 0;
+        for (int o = 0; o < MX_TW; ++o) {
+            const int no = o < ncell ? cc[o + 1] - cc[o] : -1;
+            rank += (no > nme) || (no == nme && o < tid);
+        }
+        cord[rank] = (unsigned char)tid;
+    }
     __syncthreads();
 
     const float fac1 = spc[0], txxx = spc[1], fac2 = spc[2], mqdd = spc[3], qs = spc[4];
-    const int c = tid / MX_LPC, sub = tid % MX_LPC, lane = tid & 31;
+    const int c = cord[tid / MX_LPC], sub = tid % MX_LPC, lane = tid & 31;
     const bool has_cell = c < ncell;
     const int s_beg = has_cell ? cc[c] : 0, s_end = has_cell ? cc[c + 1] : 0;
     const int nmine = (s_end - s_beg > sub) ? (s_end - s_beg - sub + MX_LPC - 1) / MX_LPC : 0;
