@@ -191,7 +191,7 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
                                              unsigned *ovf, int tile, int jr, int isp, uint32_t parity)
 {
     __shared__ int dcnt[MX_TW][9];  // per cell: particles so far that move in direction d
-    __shared__ __align__(16) float fcell[MX_TW][MX_FS];  // [cell][(b*3 + a)*6 + m]
+    __shared__ __align__(16) float fcell[MX_TW][MX_FS];  // [lane group][(b*3 + a)*6 + m]
     // per-cell partials after the loop (the first rows hold the node sums); during the loop (SPLIT)
     // the same bytes hold the per-cell queue of particles that changed cell
     __shared__ __align__(16) unsigned char qpj[SPLIT && MX_XQ_BYTES > MX_PJ_BYTES ? MX_XQ_BYTES : MX_PJ_BYTES];
@@ -199,7 +199,7 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
     float4(*xq4)[MX_XQ] = reinterpret_cast<float4(*)[MX_XQ]>(qpj);                           // old dx, dy; new dx, dy
     float2(*xq2)[MX_XQ] = reinterpret_cast<float2(*)[MX_XQ]>(qpj + MX_TW * MX_XQ * 16);      // q vz; increments + 1 (2-bit fields)
     __shared__ int cc[MX_TW + 1];
-    __shared__ unsigned char cord[MX_TW];  // the tile's cells by particle count, most first: lane group g takes cell cord[g]
+    __shared__ unsigned char cord[MX_TW], crank[MX_TW];  // the tile's cells by particle count, most first: group g takes cell cord[g]
     __shared__ float spc[5];
     __shared__ float4 pbuf4[MX_NBUF][MX_THREADS];   // each lane's next particles, MX_PFD ahead: (dx, dy, ux, uy)
     __shared__ float pbufz[MX_NBUF][MX_THREADS];    // and uz
@@ -239,6 +239,21 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
             }
     }
     __syncthreads();
+    // A warp runs as many iterations as its fullest cell needs, so the cells are dealt to the lane
+    // groups in order of their particle counts: each warp gets cells of similar counts and fewer
+    // lanes run past the end of theirs.  (Only the warp a cell lands in changes: its lanes, their
+    // particles and every sum stay the same.)  A group's field coefficients sit in the slot of the
+    // group, not of the cell, so a warp's eight 16-byte reads still fall on 32 different banks.
+    if (tid < MX_TW) {
+        const int nme = tid < ncell ? cc[tid + 1] - cc[tid] : -1;
+        int rank = 0;
+        for (int o = 0; o < MX_TW; ++o) {
+            const int no = o < ncell ? cc[o + 1] - cc[o] : -1;
+            rank += (no > nme) || (no == nme && o < tid);
+        }
+        cord[rank] = (unsigned char)tid;
+        crank[tid] = (unsigned char)rank;
+    }
     // Every thread waits (bounded) for the field tile.  If any gave up, the CTA records the timeout
     // (the step then fails), waits once more (bounded) so that the copy is not left writing into
     // this CTA's shared memory after it exits, and pushes with zero fields rather than from a
@@ -264,31 +279,20 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
             P[b][1] = 0.5f * (t2 - t0);
             P[b][2] = 0.5f * t0 - t1 + 0.5f * t2;
         }
+        const int slot = crank[c];
 #pragma unroll
         for (int p = 0; p < 3; ++p) {
-            fcell[c][(0 * 3 + p) * 6 + m] = 0.125f * P[0][p] + 0.75f * P[1][p] + 0.125f * P[2][p];
-            fcell[c][(1 * 3 + p) * 6 + m] = 0.5f * (P[2][p] - P[0][p]);
-            fcell[c][(2 * 3 + p) * 6 + m] = 0.5f * P[0][p] - P[1][p] + 0.5f * P[2][p];
+            fcell[slot][(0 * 3 + p) * 6 + m] = 0.125f * P[0][p] + 0.75f * P[1][p] + 0.125f * P[2][p];
+            fcell[slot][(1 * 3 + p) * 6 + m] = 0.5f * (P[2][p] - P[0][p]);
+            fcell[slot][(2 * 3 + p) * 6 + m] = 0.5f * P[0][p] - P[1][p] + 0.5f * P[2][p];
         }
     }
     for (int e = tid; e < MX_TW * 9; e += MX_THREADS) (&dcnt[0][0])[e] = 0;
-    // A warp runs as many iterations as its fullest cell needs, so the cells are dealt to the
-    // lane groups in order of their particle counts: each warp gets cells of similar counts and
-    // fewer lanes run past the end of theirs.  (Only the warp a cell lands in changes: its lanes,
-    // their particles and every sum stay the same.)
-    if (tid < MX_TW) {
-        const int nme = tid < ncell ? cc[tid + 1] - cc[tid] : -1;
-        int rank = 0;
-        for (int o = 0; o < MX_TW; ++o) {
-            const int no = o < ncell ? cc[o + 1] - cc[o] : -1;
-            rank += (no > nme) || (no == nme && o < tid);
-        }
-        cord[rank] = (unsigned char)tid;
-    }
     __syncthreads();
 
     const float fac1 = spc[0], txxx = spc[1], fac2 = spc[2], mqdd = spc[3], qs = spc[4];
-    const int c = cord[tid / MX_LPC], sub = tid % MX_LPC, lane = tid & 31;
+    const int grp = tid / MX_LPC;  // lane group: cell cord[grp], field coefficients in slot grp
+    const int c = cord[grp], sub = tid % MX_LPC, lane = tid & 31;
     const bool has_cell = c < ncell;
     const int s_beg = has_cell ? cc[c] : 0, s_end = has_cell ? cc[c + 1] : 0;
     const int nmine = (s_end - s_beg > sub) ? (s_end - s_beg - sub + MX_LPC - 1) / MX_LPC : 0;
@@ -296,7 +300,7 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) nwarp = max(nwarp, __shfl_xor_sync(FULL, nwarp, o));
     const long long rbase = a.rowbase[row];
-    const ulonglong2 *stencil = reinterpret_cast<const ulonglong2 *>(&fcell[has_cell ? c : 0][0]);
+    const ulonglong2 *stencil = reinterpret_cast<const ulonglong2 *>(&fcell[grp][0]);
     const int cg = c0 + c;
 
     float ax[5][4], ay[4][5], az[5][5];
