@@ -836,19 +836,33 @@ __device__ __forceinline__ double f2d_exact(float f)
     return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
+// A compensated FP32 sum (Knuth's TwoSum: hi + lo carries the sum to about 2^-48 of the sum of
+// magnitudes, near FP64's rounding) with no FP64 instruction until the end: GB300's FP64 pipe
+// runs about 2 operations per clock per SM, its FP32 pipes 128.
+struct Sum2f {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float x)
+    {
+        const float s = hi + x, bb = s - hi;
+        lo += (hi - (s - bb)) + (x - bb);
+        hi = s;
+    }
+    __device__ __forceinline__ double value() const { return f2d_exact(hi) + f2d_exact(lo); }
+};
+
 // uj(k, ix, iy) over the ghosted grid = sum of the tile currents that cover the node, in the
-// order (species, cell row, tile), accumulated in FP64.  A node is covered by the tiles of at most
-// 5 cell rows (iy-4 .. iy) and, in the first 4 columns of every tile but the first, by 2 tiles
-// (ix/32 - 1 and ix/32).  The threads take those two-tile columns first and the one-tile columns
-// after, so a warp's lanes agree on the number of tiles and the FP64 pipe issues no adds that are
-// switched off; all of a node's loads are issued before its sums.
+// order (species, cell row, tile), accumulated as a compensated FP32 sum and rounded once to FP64.
+// A node is covered by the tiles of at most 5 cell rows (iy-4 .. iy) and, in the first 4 columns
+// of every tile but the first, by 2 tiles (ix/32 - 1 and ix/32).  The threads take those two-tile
+// columns first and the one-tile columns after, so a warp's lanes agree on the number of tiles;
+// all of a node's loads are issued before its sums.
 template <bool PAIR>
 __device__ __forceinline__ void jfold_node(const WmGeom &g, int ntiles, const float *__restrict__ jtile, FView<3, false> &uj, int ix, int iy)
 {
     const long long tstride = 3LL * 5 * MX_JW;  // floats per tile
     const int th = min(ntiles - 1, ix / MX_TW);
     const int lx1 = ix - th * MX_TW, lx0 = lx1 + MX_TW;  // column in tile th and (PAIR) in tile th-1
-    double s[3] = {0.0, 0.0, 0.0};
+    Sum2f s[3];
     for (int isp = 0; isp < g.nsp; ++isp) {
         float v[5][2][3];
 #pragma unroll
@@ -868,14 +882,14 @@ __device__ __forceinline__ void jfold_node(const WmGeom &g, int ntiles, const fl
             if (cj < 0 || cj >= g.ny) continue;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                if constexpr (PAIR) s[k] += f2d_exact(v[r][0][k]);
-                s[k] += f2d_exact(v[r][1][k]);
+                if constexpr (PAIR) s[k].add(v[r][0][k]);
+                s[k].add(v[r][1][k]);
             }
         }
     }
-    uj(0, ix, iy) = s[0];
-    uj(1, ix, iy) = s[1];
-    uj(2, ix, iy) = s[2];
+    uj(0, ix, iy) = s[0].value();
+    uj(1, ix, iy) = s[1].value();
+    uj(2, ix, iy) = s[2].value();
 }
 
 __global__ void k_mixed_jfold(WmGeom g, int ntiles, const float *__restrict__ jtile, FView<3, false> uj)
