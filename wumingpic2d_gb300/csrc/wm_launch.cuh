@@ -116,8 +116,11 @@ int wm_launch_mixed_jfold(const WmGeom &g, const float *jtile, FView<3, false> u
 // rows row0 .. row0+nrows-1 of the stage (nrows < 0: to the last row)
 int wm_launch_mixed_unpack(const WmGeom &g, const double *stage, int pitch, const int *np2, MixedView dst, const WmRebinScratch &sc,
                            cudaStream_t st, int row0 = 0, int nrows = -1);
+// mixed set -> reference-layout rows: pitch slots written per row (slots past np2 zero), rows
+// rstride slots apart (rstride < 0: pitch); with perm/idperm, the permuted state read through them
 int wm_launch_mixed_pack(const WmGeom &g, MixedView src, const int *np2, const int *cumcnt, int pitch, double *stage, cudaStream_t st,
-                         int row0 = 0, int nrows = -1);
+                         int row0 = 0, int nrows = -1, long long rstride = -1, const unsigned *perm = nullptr,
+                         const unsigned *idperm = nullptr);
 
 // wm_cnn.cu: the learned-guess network inside the solve (layer shapes are padded channel counts)
 constexpr int WM_CNN_LAYERS = 6;

@@ -955,15 +955,20 @@ constexpr int PACK_THREADS = 256;
 // One CTA per (64-cell tile, row) writes the tile's particles, in slot order, as reference-layout
 // records (x, y, ux, uy, uz, id as 6 doubles) -- the cell comes from cumcnt, searched in shared
 // memory -- through a shared-memory buffer, so the stage is written in 16-byte vectors; the CTA
-// past the last tile zeroes the row's slots from np2 to the pitch.
+// past the last tile zeroes the row's slots from np2 to the pitch.  Rows are rstride slots apart
+// (rstride >= pitch: the stage may be the caller's mapped host array, whose rows hold np slots).
+// With perm, slot p's particle is read from slot perm[p] of src and its id from slot idperm[p]:
+// the permuted state packed without first gathering it into cell order.
 __global__ void __launch_bounds__(PACK_THREADS) k_mixed_pack(WmGeom g, MixedView src, const int *__restrict__ np2,
-                                                             const int *__restrict__ cumcnt, int pitch, double *__restrict__ stage, int row0)
+                                                             const int *__restrict__ cumcnt, int pitch, long long rstride,
+                                                             double *__restrict__ stage, int row0, const unsigned *__restrict__ perm,
+                                                             const unsigned *__restrict__ idperm)
 {
     __shared__ int cc[PACK_TW + 1];
     __shared__ __align__(16) double buf[PACK_THREADS * 6];
     const int row = row0 + blockIdx.y;
     const int jr = row % g.ny;
-    const long long rs = (long long)row * pitch;  // the row's first slot in the stage
+    const long long rs = (long long)row * rstride;  // the row's first slot in the stage
     const int ntile = (g.nx + PACK_TW - 1) / PACK_TW;
     if ((int)blockIdx.x == ntile) {  // zero tail
         const int n = np2[row];
@@ -987,15 +992,15 @@ __global__ void __launch_bounds__(PACK_THREADS) k_mixed_pack(WmGeom g, MixedView
                 if (cc[mid] <= s) lo = mid;
                 else hi = mid - 1;
             }
-            const long long p = rb + s;
+            const long long p = rb + s, q = perm ? (long long)perm[p] : p;  // (perm: as k_mixed_gather reads it)
             double *a = buf + 6 * threadIdx.x;
-            const float4 r = src.XYUV(p);
+            const float4 r = src.XYUV(q);
             a[0] = (double)(g.nxgs + c0 + lo) + (double)r.x;
             a[1] = (double)(g.nys + jr) + (double)r.y;
             a[2] = r.z;
             a[3] = r.w;
-            a[4] = src.UZ(p);
-            a[5] = __longlong_as_double(src.getpid(p));
+            a[4] = src.UZ(q);
+            a[5] = __longlong_as_double(src.getpid(idperm ? (long long)idperm[p] : p));
         }
         __syncthreads();
         const int nv = 3 * min(PACK_THREADS, end - s0);  // 16-byte words of this chunk
@@ -1137,10 +1142,11 @@ int wm_launch_mixed_unpack(const WmGeom &g, const double *stage, int pitch, cons
 }
 
 int wm_launch_mixed_pack(const WmGeom &g, MixedView src, const int *np2, const int *cumcnt, int pitch, double *stage, cudaStream_t st,
-                         int row0, int nrows)
+                         int row0, int nrows, long long rstride, const unsigned *perm, const unsigned *idperm)
 {
     if (nrows < 0) nrows = g.nrows - row0;
+    if (rstride < 0) rstride = pitch;
     dim3 grid((g.nx + PACK_TW - 1) / PACK_TW + 1, nrows);
-    k_mixed_pack<<<grid, PACK_THREADS, 0, st>>>(g, src, np2, cumcnt, pitch, stage, row0);
+    k_mixed_pack<<<grid, PACK_THREADS, 0, st>>>(g, src, np2, cumcnt, pitch, rstride, stage, row0, perm, idperm);
     return wm_check_launch("k_mixed_pack");
 }

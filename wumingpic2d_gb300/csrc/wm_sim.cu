@@ -1060,10 +1060,23 @@ int wm_sim_store(wm_sim *s, double *up, double *uf, int *np2_h, int *cumcnt_h)
     s->pmark("store_start");
     if (up) {
         const size_t rowb = sizeof(double) * 6 * maxc, hrowb = sizeof(double) * 6 * g.np;
-        WM_TRY(s->stage.ensure(rowb * g.nrows));
-        WM_TRY(sim_pack_stage(s, maxc));
-        s->pmark("copy_out_pack");
-        WM_TRY(copy_rows(up, hrowb, s->stage.p, rowb, rowb, g.nrows, true, s->st));
+        if (s->mixed() && rows_mapped(up, up, hrowb, up, hrowb, rowb)) {
+            // host rows mapped into the device's address space: the pack writes them directly,
+            // reading a permuted state through its permutations (the link is the bound; a staged
+            // pack then a copy, or a gather into cell order first, costs those on top)
+            s->pmark("copy_out_pack");
+            if (s->permuted)
+                WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), maxc, up, s->st, 0,
+                                            -1, g.np, s->mx_perm.as<unsigned>(), s->mx_idperm[s->idp].as<unsigned>()));
+            else
+                WM_TRY(wm_launch_mixed_pack(g, s->mview(s->A, s->cur, s->pid_cur), s->np2[s->cur].as<int>(), s->cumcnt.as<int>(), maxc, up,
+                                            s->st, 0, -1, g.np));
+        } else {
+            WM_TRY(s->stage.ensure(rowb * g.nrows));
+            WM_TRY(sim_pack_stage(s, maxc));
+            s->pmark("copy_out_pack");
+            WM_TRY(copy_rows(up, hrowb, s->stage.p, rowb, rowb, g.nrows, true, s->st));
+        }
         s->pmark("copy_out_d2h");
     }
     if (uf) {
