@@ -318,10 +318,10 @@ int wm_sim_set_work(wm_sim *s, const double *df);
  * loads the library until exit.  All calls share that scratch, so calls that overlap on the GPU
  * race.  The first call on a device looks the scratch up (cudaGetSymbolAddress); under CUDA's
  * default lazy module loading that first call is also when the array is placed in device memory,
- * which is an allocation: make it at start-up, before any stream capture begins, so that the
- * memory is committed then and later calls allocate nothing.  stream: a cudaStream_t, or NULL for
- * the default stream.  The call is synchronous: it reads a status word back and waits for the
- * stream, then returns WM_OK, or WM_ERR_CELL if a particle moved more than one cell. */
+ * which is an allocation: make it at start-up, so that the memory is committed then and later
+ * calls allocate nothing.  stream: a cudaStream_t, or NULL for the default stream.  The call is
+ * synchronous: it reads a status word back and waits for the stream, so no call can be captured
+ * into a CUDA graph.  Returns WM_OK, or WM_ERR_CELL if a particle moved more than one cell. */
 int wm_deposit_current_noalloc(const double *up, const double *gp, const int *cumcnt, double *uj, int ndim, int np, int nsp,
                                int nxgs, int nxge, int nygs, int nyge, double delx, double delt, double c, const double *q,
                                void *stream);
