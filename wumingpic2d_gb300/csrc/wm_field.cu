@@ -24,6 +24,9 @@ namespace {
 constexpr unsigned FULL = 0xffffffffu;
 constexpr int CG_THREADS = 256;
 constexpr int CG_BLOCKS = 152 * 4;  // one wave: 4 CTAs of 256 threads on each of the 152 SMs
+// k_cg_phase: 5 CTAs per SM (measured at 2048^2 x 64 ppc: CG iterations 3.09 ms per step with 4, 2.86
+// with 5, 3.19 with 3); the set-up kernels keep 4 (0.67 ms against 0.73 with 5)
+constexpr int CG_PHASE_BLOCKS = 152 * 5;
 
 // ------------------------------------------------------------ ghost patterns
 template <class FV>
@@ -477,7 +480,7 @@ __global__ void __launch_bounds__(CG_THREADS) k_cg_resid_pick(WmGeom g, FieldK f
 // Registers are bounded for one CTA per SM more than the grid places, so that the mixed step's
 // rebin kernels, which run on a second stream beside the field solve, find room on every SM.
 template <class FV6>
-__global__ void __launch_bounds__(CG_THREADS, CG_BLOCKS / 152 + 1) k_cg_phase(WmGeom g, FieldK fk, FV6 df, double *__restrict__ p, double *__restrict__ r,
+__global__ void __launch_bounds__(CG_THREADS, CG_PHASE_BLOCKS / 152 + 1) k_cg_phase(WmGeom g, FieldK fk, FV6 df, double *__restrict__ p, double *__restrict__ r,
                                                          double *__restrict__ ap, double *partial, unsigned *ticket, CgScal *scal, int t)
 {
     const long long ncell = (long long)g.nx * g.ny;
@@ -663,7 +666,7 @@ int wm_launch_soa_to_aos(int nc, long long npts, const double *s, double *a, cud
 }
 
 // --------------------------------------------------------------- field solve
-int wm_field_cg_blocks() { return CG_BLOCKS; }
+int wm_field_cg_blocks() { return CG_BLOCKS > CG_PHASE_BLOCKS ? CG_BLOCKS : CG_PHASE_BLOCKS; }  // the partials of the largest grid
 size_t wm_field_scal_bytes() { return sizeof(CgScal) * 3; }
 
 static FieldK make_fk(const WmConst &k)
@@ -726,7 +729,7 @@ int wm_field_solve(const WmGeom &g, const WmConst &k, FView<6, false> uf, FView<
         const bool any = w.scal_host[0].active || w.scal_host[1].active || w.scal_host[2].active;
         if (!any || t >= t_max) break;
         for (int b = 0; b < 3 * cg_batch; ++b, ++t) {
-            k_cg_phase<FView<6, false>><<<CG_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.p, w.r, w.ap, w.partial, w.ticket, w.scal, t);
+            k_cg_phase<FView<6, false>><<<CG_PHASE_BLOCKS, CG_THREADS, 0, st>>>(g, fk, df, w.p, w.r, w.ap, w.partial, w.ticket, w.scal, t);
             ++nl;
         }
         WM_TRY(wm_check_launch("cg iteration"));
