@@ -578,15 +578,22 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
             incx = cn - cg;
         }
         // direction d = (dy+1)*3 + dx+1 and the rank among this cell's particles moving that way,
-        // in particle order: the lanes of a cell with the same d this round, plus earlier rounds
-        // (a step of more than one cell is flagged above; the clamp keeps the move in bounds)
+        // in particle order: the cell's lanes before this one with the same d this round (three
+        // shuffles within the cell's lane group; a lane past its cell matches none), plus earlier
+        // rounds; the cell's last lane with that d advances the count.  (A step of more than one
+        // cell is flagged above; the clamp keeps the move in bounds.)
         const int d = (min(max(incy, -1), 1) + 1) * 3 + (min(max(incx, -1), 1) + 1);
-        const unsigned peers = __match_any_sync(FULL, valid ? (c << 4) | d : (int)(0x7fff0000u | (unsigned)lane));
-        const int leader = __ffs(peers) - 1;
-        int base = (lane == leader && valid) ? dcnt[c][d] : 0;
-        base = __shfl_sync(FULL, base, leader);
-        const int rank = base + __popc(peers & lanemask_lt());
-        if (lane == leader && valid) dcnt[c][d] = base + __popc(peers);
+        const int dv = valid ? d : -1 - sub;
+        int below = 0, above = 0;
+#pragma unroll
+        for (int k = 1; k < MX_LPC; ++k) {
+            const int ou = __shfl_up_sync(FULL, dv, k, MX_LPC), od = __shfl_down_sync(FULL, dv, k, MX_LPC);
+            below += (sub >= k) && (ou == dv);
+            above += (sub + k < MX_LPC) && (od == dv);
+        }
+        const int rank = (valid ? dcnt[c][d] : 0) + below;
+        __syncwarp();
+        if (valid && above == 0) dcnt[c][d] = rank + 1;
         __syncwarp();
         bad |= valid & (rank >= (1 << (28 - MX_CB)));
         store_particle(b, p, nx1, ny1, u1, u2, u3, code, ((unsigned)rank << (4 + MX_CB)) | ((unsigned)c << 4) | (unsigned)d, valid);
