@@ -8,8 +8,9 @@
 // boundary_periodic.f90:61-96 and :143-165 as integer cell arithmetic, and the destination cell key
 // and row direction the rebin needs.  The tile's cell-centred fields arrive as one TMA box; four
 // lanes share a cell, so the cell's (dx, dy, ux, uy) records move as two full 32-byte sectors per
-// step of the loop; each lane's next two particles (the 16-byte record and uz) are copied into
-// shared memory (cp.async) while the current one is pushed.  The TSC-weighted 3x3 gather of
+// particle round; each step of the loop pushes two particles per lane (the cell's field
+// coefficients read once for both) while the lane's next two (the 16-byte record and uz) are
+// copied into shared memory (cp.async).  The TSC-weighted 3x3 gather of
 // each field is a biquadratic in the particle's offsets, so the kernel stages its nine
 // coefficients per cell and field and evaluates it by Horner's rule, two fields per packed
 // fma.rn.f32x2.  Each lane keeps the cell's 5x5x3 partial currents in registers (the cell's
@@ -42,12 +43,6 @@ constexpr int MX_FTW = MX_TW + 4;           // columns of the staged field tile:
 constexpr int MX_CB = 6;                    // bits of the tile cell in a move code: rank << 10 | cell << 4 | direction
 static_assert(MX_TW <= (1 << MX_CB), "a tile's cells fit the move code");
 constexpr unsigned FULL = 0xffffffffu;
-#ifndef WM_MX_PFD
-#define WM_MX_PFD 2  // particles each lane has in flight (cp.async) ahead of the one it pushes (2: 2 % faster than 1)
-#endif
-constexpr int MX_PFD = WM_MX_PFD;
-constexpr int MX_NBUF = MX_PFD + 1;
-constexpr int MX_PR = MX_PFD + 2;  // perm entries each lane holds (GATHER): iterations it+MX_PFD .. it+2 MX_PFD+1
 #ifndef WM_MX_XQ
 #define WM_MX_XQ 16
 #endif
@@ -170,8 +165,9 @@ __device__ __forceinline__ bool mx_bar_wait(uint32_t bar, uint32_t parity)
 
 // One CTA per (tile of MX_TW cells, row, species); MX_LPC lanes per cell.  The loop body has no branches:
 // a lane past the end of its cell runs on a zero particle with zero deposit weights and its stores
-// switched off.  Each lane's next particle is copied into shared memory (cp.async) while the
-// current one is pushed.
+// switched off.  A step of the loop pushes the lane's particles k and k+1 (rounds k and k+1 of the
+// cell: the order of every sum, rank and queue entry is that of one particle per step) while
+// particles k+2 and k+3 are copied into shared memory (cp.async).
 #ifndef WM_MX_MINB
 #define WM_MX_MINB (512 / MX_THREADS)  // resident CTAs per SM the register budget is sized for
 #endif
@@ -201,9 +197,9 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
     __shared__ int cc[MX_TW + 1];
     __shared__ unsigned char cord[MX_TW], crank[MX_TW];  // the tile's cells by particle count, most first: group g takes cell cord[g]
     __shared__ float spc[5];
-    __shared__ float4 pbuf4[MX_NBUF][MX_THREADS];   // each lane's next particles, MX_PFD ahead: (dx, dy, ux, uy)
-    __shared__ float pbufz[MX_NBUF][MX_THREADS];    // and uz
-    __shared__ unsigned permring[GATHER ? MX_PR : 1][MX_THREADS];
+    __shared__ float4 pbuf4[4][MX_THREADS];   // each lane's particles k .. k+3 (slot k & 3): (dx, dy, ux, uy)
+    __shared__ float pbufz[4][MX_THREADS];    // and uz
+    __shared__ unsigned permring[GATHER ? 8 : 1][MX_THREADS];  // perm entries, slot k & 7
     __shared__ __align__(128) float tmp[6][3][MX_FTW];  // the tile's cell-centred fields (one TMA box)
     __shared__ __align__(8) uint64_t fbar;
     const int row = isp * g.ny + jr;
@@ -400,76 +396,58 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
     const unsigned cellmask = ((1u << MX_LPC) - 1u) << (lane & ~(MX_LPC - 1));  // this cell's lanes in the warp
     int xn = 0;  // particles of this cell that changed cell so far (the same in all its lanes)
     unsigned bad = 0;
-    // lane's particle of iteration it (at slot q of set a) -> pbuf[slot]; a lane past its cell copies zeros.
-    // GATHER: the perm entry of iteration j travels in the copy group of iteration j - MX_PFD - 1
-    // (into permring[j % MX_PR]), so it is in shared memory when iteration j's particle is fetched.
+    // lane's particle k (at slot q of set a) -> pbuf[k & 3]; a lane past its cell copies zeros.
+    // GATHER: the perm entry of particle k + 4 travels in particle k's copy group (into
+    // permring[(k + 4) & 7]), so it is in shared memory when particle k + 4 is fetched.
     auto canon = [&](int it) { return rbase + s_beg + sub + (long long)it * MX_LPC; };
-    auto prefetch = [&](int it, int slot, long long q, int jperm) {
-        const bool v = it < nmine;
-        cp_async16(&pbuf4[slot][tid], a.xyuv + q, v ? 16u : 0u);
-        cp_async4(&pbufz[slot][tid], a.uz + q, v ? 4u : 0u);
-        if (GATHER && jperm >= 0) {  // (the first MX_PFD groups carry no perm entry)
-            const bool vp = jperm < nmine;
-            cp_async4(reinterpret_cast<float *>(&permring[jperm % MX_PR][tid]), reinterpret_cast<const float *>(perm + (vp ? canon(jperm) : 0)),
-                      vp ? 4u : 0u);
+    auto prefetch = [&](int k, long long q) {
+        const bool v = k < nmine;
+        cp_async16(&pbuf4[k & 3][tid], a.xyuv + q, v ? 16u : 0u);
+        cp_async4(&pbufz[k & 3][tid], a.uz + q, v ? 4u : 0u);
+        if constexpr (GATHER) {
+            const int jp = k + 4;
+            const bool vp = jp < nmine;
+            cp_async4(reinterpret_cast<float *>(&permring[jp & 7][tid]), reinterpret_cast<const float *>(perm + (vp ? canon(jp) : 0)), vp ? 4u : 0u);
         }
         cp_async_commit();
     };
-    // the slot of set a that holds iteration it's particle
-    auto source = [&](int it) -> long long {
-        if constexpr (GATHER) return it < nmine ? (long long)permring[it % MX_PR][tid] : 0LL;
-        else return it < nmine ? canon(it) : 0LL;
+    auto source = [&](int k) -> long long {
+        if constexpr (GATHER) return k < nmine ? (long long)permring[k & 7][tid] : 0LL;
+        else return k < nmine ? canon(k) : 0LL;
     };
-    // iterations 0 .. MX_PFD-1 are fetched before the loop, their perm entries read directly;
-    // those of iterations MX_PFD .. 2 MX_PFD go into the ring directly too
     auto direct = [&](int j) -> long long {
         if constexpr (GATHER) return j < nmine ? (long long)__ldg(perm + canon(j)) : 0LL;
         else return j < nmine ? canon(j) : 0LL;
     };
     if constexpr (GATHER) {
-#pragma unroll
-        for (int j = MX_PFD; j <= 2 * MX_PFD; ++j) permring[j % MX_PR][tid] = (unsigned)direct(j);
+        permring[2][tid] = (unsigned)direct(2);
+        permring[3][tid] = (unsigned)direct(3);
     }
 #pragma unroll
-    for (int i = 0; i < MX_PFD; ++i) {
-        if (i < nwarp) prefetch(i, i, direct(i), -1);
-        else cp_async_commit();  // empty groups keep the wait count uniform
+    for (int i = 0; i < 2; ++i) {
+        if (i < nwarp) prefetch(i, direct(i));
+        else cp_async_commit();
     }
-    int rslot = 0, wslot = MX_PFD;  // slot read this iteration, slot the next prefetch fills
-    for (int it = 0; it < nwarp; ++it) {
+    // the six fields at a particle's offsets: Horner in hx then hy, two fields per packed FMA
+    auto gather = [&](const unsigned long long (&cw)[28], float dx, float dy, float (&f)[6]) {
+        const unsigned long long hx2 = pack2(dx - 0.5f, dx - 0.5f), hy2 = pack2(dy - 0.5f, dy - 0.5f);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            unsigned long long r[3];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) r[q] = fma2(hx2, fma2(hx2, cw[(q * 3 + 2) * 3 + j], cw[(q * 3 + 1) * 3 + j]), cw[(q * 3) * 3 + j]);
+            unpack2(fma2(hy2, fma2(hy2, r[2], r[1]), r[0]), f[2 * j], f[2 * j + 1]);
+        }
+    };
+    // the rest of one particle's step: lane particle it, record pin and uz, fields f
+    auto process = [&](int it, const float4 &pin, float u3, const float (&f)[6]) {
         const bool valid = it < nmine;
         const long long p = canon(it);
-        if (it + MX_PFD < nwarp) prefetch(it + MX_PFD, wslot, source(it + MX_PFD), it + 2 * MX_PFD + 1);
-        else cp_async_commit();
-        cp_async_wait<MX_PFD>();
-        const float4 pin = pbuf4[rslot][tid];
-        float u3 = pbufz[rslot][tid];
-        rslot = rslot + 1 == MX_NBUF ? 0 : rslot + 1;
-        wslot = wslot + 1 == MX_NBUF ? 0 : wslot + 1;
         const float dx = pin.x, dy = pin.y;
         float u1 = pin.z, u2 = pin.w;
         float sx0, sx1, sx2, sy0, sy1, sy2;
         shape3(dx - 0.5f, sx0, sx1, sx2);
         shape3(dy - 0.5f, sy0, sy1, sy2);
-        float f[6];
-        {
-            // Horner in hx then hy, two fields per packed FMA: C pair j of (q, p) = word (q*3 + p)*3 + j
-            const unsigned long long hx2 = pack2(dx - 0.5f, dx - 0.5f), hy2 = pack2(dy - 0.5f, dy - 0.5f);
-            unsigned long long cw[28];
-#pragma unroll
-            for (int q4 = 0; q4 < 14; ++q4) {
-                const ulonglong2 t = stencil[q4];
-                cw[2 * q4] = t.x;
-                cw[2 * q4 + 1] = t.y;
-            }
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                unsigned long long r[3];
-#pragma unroll
-                for (int q = 0; q < 3; ++q) r[q] = fma2(hx2, fma2(hx2, cw[(q * 3 + 2) * 3 + j], cw[(q * 3 + 1) * 3 + j]), cw[(q * 3) * 3 + j]);
-                unpack2(fma2(hy2, fma2(hy2, r[2], r[1]), r[0]), f[2 * j], f[2 * j + 1]);
-            }
-        }
         // Buneman-Boris
         float v1 = u1 + fac1 * f[3], v2 = u2 + fac1 * f[4], v3 = u3 + fac1 * f[5];
         const float g2 = kc.c2 + v1 * v1 + v2 * v2 + v3 * v3;
@@ -597,6 +575,31 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
         __syncwarp();
         bad |= valid & (rank >= (1 << (28 - MX_CB)));
         store_particle(b, p, nx1, ny1, u1, u2, u3, code, ((unsigned)rank << (4 + MX_CB)) | ((unsigned)c << 4) | (unsigned)d, valid);
+    };
+    // two particles per step of the loop: the cell's field coefficients are read once for both
+    for (int it = 0; it < nwarp; it += 2) {
+        const bool has_b = it + 1 < nwarp;  // (uniform over the warp)
+        if (it + 2 < nwarp) prefetch(it + 2, source(it + 2));
+        else cp_async_commit();
+        if (it + 3 < nwarp) prefetch(it + 3, source(it + 3));
+        else cp_async_commit();
+        cp_async_wait<2>();
+        const float4 pa = pbuf4[it & 3][tid], pb = pbuf4[(it + 1) & 3][tid];
+        const float za = pbufz[it & 3][tid], zb = pbufz[(it + 1) & 3][tid];
+        float fa[6], fb[6];
+        {
+            unsigned long long cw[28];
+#pragma unroll
+            for (int q4 = 0; q4 < 14; ++q4) {
+                const ulonglong2 t = stencil[q4];
+                cw[2 * q4] = t.x;
+                cw[2 * q4 + 1] = t.y;
+            }
+            gather(cw, pa.x, pa.y, fa);
+            gather(cw, pb.x, pb.y, fb);
+        }
+        process(it, pa, za, fa);
+        if (has_b) process(it + 1, pb, zb, fb);
     }
     // the queued particles of each cell that changed cell, deposited by the cell's lanes with the full form
     if constexpr (SPLIT) {
