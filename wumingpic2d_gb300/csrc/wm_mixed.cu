@@ -503,8 +503,8 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
         // each node's FMAs in the same order.  (The full form's other terms are zero for it, but for
         // the rounding residue of the cumulative sums cx(3) and cy(3), which the continuity equation
         // sets to zero and which are dropped.)  A particle that changes cell is queued in shared
-        // memory and deposited with the full form by its cell's lanes after the loop; if the cell's
-        // queue is full, the warp deposits it at once.
+        // memory and deposited with the full form by its cell's lanes after the loop; a tile whose
+        // queue overflows is recomputed by k_mixed_push_redo.
         const float mq = valid ? mqdd : 0.f;  // zero weights for a lane past its cell
         const float qg = valid ? qs * u3 * ig_dep : 0.f;
         const bool stay = !SPLIT || (incx == 0 && incy == 0);
