@@ -583,7 +583,8 @@ __device__ __forceinline__ void mx_push_tile(const WmGeom &g, const MxConst &kc,
         else cp_async_commit();
         if (it + 3 < nwarp) prefetch(it + 3, source(it + 3));
         else cp_async_commit();
-        cp_async_wait<2>();
+        cp_async_wait<2>();  // one copy group per particle: those of it and it+1 have landed, it+2 and it+3 fly
+        // (without a particle it+1, slot (it+1) & 3 holds an older record: gathered, never used)
         const float4 pa = pbuf4[it & 3][tid], pb = pbuf4[(it + 1) & 3][tid];
         const float za = pbufz[it & 3][tid], zb = pbufz[(it + 1) & 3][tid];
         float fa[6], fb[6];
