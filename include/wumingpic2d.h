@@ -335,10 +335,12 @@ int wm_fp64_fma_rate(double *tflops, double *ms);
 int wm_host_register(void *ptr, size_t bytes);
 int wm_host_unregister(void *ptr);
 
-/* Allocate / free page-locked host memory (cudaHostAlloc, portable across devices).  The state
- * arrays up and uf that wm_sim_step_host copies every call are best placed here: the copy engines
- * reach their full rate on such memory whatever the CPU did to it before, while a buffer that was
- * registered after the CPU first touched it can copy several times slower on Grace hosts. */
+/* Allocate / free page-locked host memory (cudaHostAlloc, portable across devices, mapped into the
+ * device's address space).  The state arrays up and uf that wm_sim_step_host copies every call are
+ * best placed here: the copies reach their full rate on such memory whatever the CPU did to it
+ * before, while a buffer that was registered after the CPU first touched it can copy several times
+ * slower on Grace hosts; the particle rows of such memory are read and (mixed path) written by the
+ * library's kernels directly. */
 int wm_host_alloc(void **ptr, size_t bytes);
 int wm_host_free(void *ptr);
 
